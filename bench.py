@@ -1,0 +1,346 @@
+"""Benchmark: FP64 energy+gradient evaluations per second on one GB300.
+
+Workload (BASELINE metric "grad evals/s ..., 1 GB300, 163k verts"): a level-7
+icosphere (163,842 vertices, 327,680 faces), vertices jittered by 13% of the
+mean edge length (seed 0), the energy of the very-large-mesh configuration
+(kb 20, ka 1e6, kv 1e6, kc 0, kt 1e5, kr 1e3, reduced-volume target 0.65,
+smooth tether lc0/lc1 = 1.15/0.85 mean edge, repulsion cut-off 0.8 mean edge
+via the cell list, exclusion 2).  One step = 10 x (positions displaced by
+N(0, 1e-4), one energy+gradient evaluation) + one cell-list rebuild, the
+evaluation loop of the large-mesh configuration applied to the 163k mesh.
+
+value:  device-resident evaluations (positions, gradient and energy in HBM),
+        every evaluation and rebuild timed with CUDA events on the launching
+        stream, L2 flushed (256 MB write) before each timed piece.
+e2e:    the same evaluations through the public API (trimem_gb300.core:
+        write the positions into TriMesh.points(), EnergyManager
+        .energy_gradient), i.e. host positions uploaded and the gradient read
+        back every evaluation.
+cpu_baseline / --impl reference: the reference algorithm restated on the
+        host cores (the reference itself cannot be built: its OpenMesh
+        submodule is empty), all threads, energy() + gradient() per
+        evaluation like the reference's Python drivers.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+LEVEL = 7
+EVALS_PER_STEP = 10
+METRIC = "grad evals/s (FP64 energy+gradient, 163,842-vertex icosphere)"
+UNIT = "evals/s"
+
+
+def workload():
+    from helpers import workload_params
+    from trimem_gb300 import meshgen
+
+    p, f = meshgen.jittered_icosphere(LEVEL, seed=0)
+    prm = workload_params(p, f, kappa_b=20.0, vfrac=0.65)
+    return p, f, prm
+
+
+def config(extra=None):
+    c = {"workload": "icosphere L7 (163842 vertices), FP64 energy+gradient, cell-list rebuild every 10 evals, "
+                     "N(0,1e-4) displacement between evals",
+         "vertices": 163842, "faces": 327680, "evals_per_step": EVALS_PER_STEP,
+         "l2": "flushed (256 MB write) before every timed evaluation and rebuild",
+         "parallelism": "replicas"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def read_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.proc = None
+        self.gpu = gpu
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            v = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(v[0]))
+                mx = float(v[1])
+            except ValueError:
+                continue
+            for n, x in zip(names, v[3:7]):
+                if x.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(p, f, prm, budget_s=20.0, max_evals=12):
+    """Oracle (reference algorithm on the host cores, all threads)."""
+    from oracle import oracle as O
+
+    nthreads = os.cpu_count() or 1
+    O.set_threads(nthreads)
+    mo = O.Mesh(p, f)
+    eo = O.Energy(mo, O.default_params(**prm))
+    eo.time_energy_gradient(mo, 1)  # warm-up
+    n, t = 0, 0.0
+    rng = np.random.default_rng(1)
+    x = mo.points()
+    while n < max_evals and t < budget_s:
+        t0 = time.perf_counter()
+        if n % EVALS_PER_STEP == 0:
+            eo.update_repulsion(mo)
+        x += rng.normal(0, 1e-4, size=x.shape)
+        eo.energy(mo)
+        eo.gradient(mo)
+        t += time.perf_counter() - t0
+        n += 1
+    return {"value": n / t, "unit": UNIT, "cores": O.get_threads(), "kind": "port",
+            "sample": f"{n} evaluations (energy + gradient calls, one cell-list rebuild per 10, displacement "
+                      f"N(0,1e-4)) of the 163,842-vertex workload, {t:.1f} s, OpenMP {O.get_threads()} threads"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    p, f, prm = workload()
+    for _ in range(max(args.warmup, 0)):
+        pass
+    cb = cpu_baseline(p, f, prm, budget_s=max(20.0, 5.0 * args.steps), max_evals=max(3, args.steps * 2))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(),
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--e2e-evals", type=int, default=30)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    from trimem_gb300 import capi, load_core
+
+    core = load_core()
+    p, f, prm = workload()
+    V = len(p)
+    mesh = capi.Mesh(p, f)
+    en = capi.Energy(mesh, capi.params(**prm))
+    L = capi.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    g = torch.empty_like(x)
+    e_dev = torch.empty(1, dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(1234 + rank)
+
+    def rebuild():
+        capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes_ptr(x), ctypes_ptr_s(stream)))
+
+    def evaluate():
+        x.add_(torch.randn(x.shape, dtype=torch.float64, device="cuda", generator=gen), alpha=1e-4)
+        capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes_ptr(x), ctypes_ptr(g), ctypes_ptr(e_dev),
+                                           ctypes_ptr_s(stream)))
+
+    def timed(fn):
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        return a, b
+
+    def step():
+        evs = [timed(rebuild)]
+        for _ in range(EVALS_PER_STEP):
+            evs.append(timed(evaluate))
+        return evs
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        w0 = time.perf_counter()
+        all_evs = [step() for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        w1 = time.perf_counter()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    dev_ms = sum(a.elapsed_time(b) for evs in all_evs for a, b in evs)
+    rebuild_ms = sum(evs[0][0].elapsed_time(evs[0][1]) for evs in all_evs) / args.steps
+    eval_ms = (dev_ms / args.steps - rebuild_ms) / EVALS_PER_STEP
+    if world > 1:
+        t = torch.tensor([dev_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    ms_per_step = dev_ms / args.steps
+    value = world * EVALS_PER_STEP * args.steps / (dev_ms / 1e3)
+
+    # ---- per-kernel times of one evaluation (cold L2) for the roofline -----
+    import ctypes
+
+    kms = []
+    for _ in range(5):
+        flush.fill_(1.0)
+        ms5 = (ctypes.c_float * 5)()
+        capi.check(L.tm_energy_eval_timed(en.h, mesh.h, ctypes_ptr(x), ctypes_ptr(g), ms5, ctypes_ptr_s(stream)))
+        kms.append(list(ms5))
+    kms = np.median(np.array(kms), axis=0)
+    names = ["k_face", "k_edge", "k_vertex", "k_grad"]
+    dom = int(np.argmax(kms[:4]))
+    F, E = len(f), 3 * len(f) // 2
+    # unique bytes each kernel must move (inputs + outputs) per launch
+    kbytes = {
+        "k_face": 3 * 4 * F + 24 * V + 64 * F,
+        "k_edge": 16 * E + 24 * V + 64 * F + 40 * E,
+        "k_vertex": 4 * V + 16 * 2 * E + 64 * F + 40 * E + 24 * V + 8 * V + 24 * V + 16 * V,
+        "k_grad": 4 * V + 16 * 2 * E + 24 * V + 8 * V + 64 * F + 32 * E + 24 * V + 24 * V,
+    }
+    peaks = read_peaks()
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "of measured" if hbm else "of fallback"
+    hbm = hbm or 6800.0
+    dname = names[dom]
+    achieved = kbytes[dname] / (kms[dom] * 1e-3) / 1e9
+    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
+    traffic = None
+    if os.path.exists(traffic_path):
+        traffic = json.load(open(traffic_path)).get(dname)
+    # whole evaluation: SURVEY per-vertex algorithmic bytes (132 B/vertex)
+    eval_bytes = 132 * V
+    roofline = {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 5), "traffic": traffic, "peak_source": peak_note,
+                "kernel_ms": {n: round(float(k), 5) for n, k in zip(names, kms[:4])},
+                "eval_ms_cold": round(float(kms[4]), 5),
+                "eval_algorithmic_bytes": eval_bytes,
+                "eval_frac": round(eval_bytes / (kms[4] * 1e-3) / 1e9 / hbm, 5),
+                "algorithmic_bytes": kbytes[dname]}
+
+    # ---- end to end through the public API ---------------------------------
+    cm = core.TriMesh(p, f)
+    ep = core.EnergyParams()
+    for k in ["kappa_b", "kappa_a", "kappa_v", "kappa_c", "kappa_t", "kappa_r", "area_frac", "volume_frac",
+              "curvature_frac"]:
+        setattr(ep, k, prm[k])
+    ep.bond_params.lc0, ep.bond_params.lc1, ep.bond_params.a0 = prm["bond_lc0"], prm["bond_lc1"], prm["bond_a0"]
+    ep.repulse_params.lc1, ep.repulse_params.rlist = prm["rep_lc1"], prm["rlist"]
+    estore = core.EnergyManager(cm, ep)
+    rng = np.random.default_rng(5)
+    host_x = [p + rng.normal(0, 1e-4, size=p.shape) for _ in range(4)]
+    pts = cm.points()
+    for i in range(3):
+        np.copyto(pts, host_x[i % 4])
+        estore.energy_gradient(cm)
+    n_e2e = args.e2e_evals
+    t0 = time.perf_counter()
+    for i in range(n_e2e):
+        if i % EVALS_PER_STEP == 0:
+            estore.update_repulsion(cm)
+        np.copyto(pts, host_x[i % 4])
+        en_val, grad = estore.energy_gradient(cm)
+    t1 = time.perf_counter()
+    e2e = {"value": n_e2e / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": EVALS_PER_STEP * 24 * V + 24 * V,
+           "d2h_bytes_per_step": EVALS_PER_STEP * (24 * V + 8),
+           "api": "np.copyto(TriMesh.points(), x); EnergyManager.energy_gradient(mesh); update_repulsion every 10"}
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(p, f, prm)
+
+    launches_per_step = 4 * EVALS_PER_STEP + 10
+    peaks_fp64 = {"fp64_gflops_measured_probe": 1196.0}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config({"eval_ms": round(eval_ms, 5), "rebuild_ms": round(rebuild_ms, 5),
+                              "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4)}),
+            "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
+            "gpu_launches": launches_per_step * args.steps, "notes": peaks_fp64}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def ctypes_ptr(t):
+    import ctypes
+
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def ctypes_ptr_s(s):
+    import ctypes
+
+    return ctypes.c_void_p(s)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,176 @@
+/*
+ * trimem_gb300 C ABI -- the drop-in boundary of the GB300 implementation of
+ * trimem's energy / gradient / neighbour-list / edge-flip path.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (TM_OK == 0, negative on failure) and leaves a message for
+ * tm_last_error().  Calls are synchronous with respect to the host unless the
+ * name ends in _device; a handle is not re-entrant (one CUDA stream each).
+ *
+ * Reference interfaces are cited as path:line within bio-phys/trimem.
+ */
+#ifndef TRIMEM_GPU_H
+#define TRIMEM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  TM_OK = 0,
+  TM_ERR_ARG = -1,      /* invalid argument (RuntimeError / ValueError)   */
+  TM_ERR_CUDA = -2,     /* CUDA runtime failure                            */
+  TM_ERR_TOPOLOGY = -3, /* non-manifold input or valence above TM_MAXVAL   */
+  TM_ERR_RANGE = -4,    /* std::range_error in the reference (flip ratio)   */
+  TM_ERR_TIMEOUT = -5,  /* a bounded device wait gave up                    */
+  TM_ERR_NOMEM = -6,    /* device or pinned allocation failed               */
+  TM_ERR_DEVICE = -7    /* a device-side check recorded a bad index         */
+};
+
+/* Largest vertex valence the device ring tables hold. */
+#define TM_MAXVAL 32
+
+/* EnergyParams with its nested BondParams, SurfaceRepulsionParams and
+ * ContinuationParams flattened (src/params.h:11-71). */
+typedef struct tm_params {
+  double kappa_b, kappa_a, kappa_v, kappa_c, kappa_t, kappa_r;
+  double area_frac, volume_frac, curvature_frac;
+  double bond_lc0, bond_lc1, bond_a0;
+  int32_t bond_r, bond_type; /* BondType: 0 Edge, 1 Area, 2 None */
+  double rep_lc1;
+  int32_t rep_r, n_search; /* n_search: 0 "cell-list", 1 "verlet-list" */
+  double rlist;
+  int32_t exclusion_level, pad0;
+  double cont_delta, cont_lambda;
+} tm_params;
+
+typedef struct tm_mesh tm_mesh;
+typedef struct tm_energy tm_energy;
+typedef struct tm_nlist tm_nlist;
+
+const char* tm_last_error(void);
+/* Name of the CUDA device the library runs on; fails when none is present. */
+int tm_device_name(char* buf, int len);
+
+/* ---- mesh ---------------------------------------------------------------
+ * TriMesh(points, faces): src/bindings.cpp:87-109, src/mesh_py.cpp:12-70.
+ * Face entries outside [0, n_points) are dropped; faces with fewer than three
+ * valid vertices, repeated vertices or an already used directed edge are
+ * skipped.  Edge e owns halfedges 2e and 2e+1. */
+int tm_mesh_create(const double* points, int64_t n_points, const int32_t* faces, int64_t n_faces,
+                   tm_mesh** out);
+int tm_mesh_destroy(tm_mesh* m);
+int tm_mesh_counts(tm_mesh* m, int64_t* n_vertices, int64_t* n_edges, int64_t* n_faces);
+/* Host copy of the positions (TriMesh.points(), src/mesh_py.cpp:96-106).
+ * It is page-locked and stays valid for the life of the mesh; callers write
+ * it in place and every host-side compute call uploads it. */
+double* tm_mesh_points(tm_mesh* m);
+/* TriMesh.fv_indices (src/mesh_py.cpp:73-93); out is (n_faces, 3). */
+int tm_mesh_fv_indices(tm_mesh* m, int32_t* out);
+/* Half-edge queries (src/bindings.cpp:147-175).  op: 0 halfedge_handle(edge
+ * = h) (first halfedge), 1 next, 2 opposite, 3 to-vertex, 4 from-vertex,
+ * 5 face (-1 on boundary). */
+int tm_mesh_halfedge(tm_mesh* m, int op, int64_t h, int64_t* out);
+/* Whole topology: to/next/face per halfedge, outgoing halfedge per vertex,
+ * halfedge per face (any pointer may be NULL). */
+int tm_mesh_topology(tm_mesh* m, int32_t* to, int32_t* next, int32_t* face, int32_t* vout, int32_t* fhe);
+/* Device-side invariant check: closed 2-manifold fans, valence >= 3, no
+ * double edges.  *status = 0 when valid, else a negative code. */
+int tm_mesh_check(tm_mesh* m, int* status);
+
+/* ---- geometry primitives (src/mesh_util.h:15-185, src/bindings.cpp:251-407)
+ * value and gradient of one halfedge's quantity; grad (rows x 3, row-major)
+ * may be NULL.  Rows: edge_length 2, face_area 3, face_volume 3,
+ * dihedral_angle 4. */
+int tm_edge_length(tm_mesh* m, int64_t he, double* value, double* grad);
+int tm_face_area(tm_mesh* m, int64_t he, double* value, double* grad);
+int tm_face_volume(tm_mesh* m, int64_t he, double* value, double* grad);
+int tm_dihedral_angle(tm_mesh* m, int64_t he, double* value, double* grad);
+
+/* ---- energy manager (src/energy.h:18-56, src/energy.cpp:13-151) --------
+ * Properties are ordered (area, volume, curvature, bending, tethering,
+ * repulsion) like VertexProperties (src/mesh_properties.h:14-48). */
+int tm_energy_create(tm_mesh* m, const tm_params* p, tm_energy** out);
+int tm_energy_destroy(tm_energy* e);
+int tm_energy_get_params(tm_energy* e, tm_params* out);
+int tm_energy_initial_props(tm_energy* e, double* out6);
+int tm_energy_properties(tm_energy* e, tm_mesh* m, double* out6);
+int tm_energy_vertex_properties(tm_energy* e, tm_mesh* m, double* out6v);
+int tm_energy_energy(tm_energy* e, tm_mesh* m, double* energy);
+int tm_energy_energy_props(tm_energy* e, const double* props6, double* energy);
+/* area, volume, area-difference, bending, tether, repulsion, total energy
+ * (the print_info breakdown, src/energy.cpp:126-151). */
+int tm_energy_components(tm_energy* e, tm_mesh* m, double* out7);
+/* Gradient of the energy wrt the positions, (n_vertices, 3); energy may be
+ * NULL (src/energy.cpp:93-124). */
+int tm_energy_gradient(tm_energy* e, tm_mesh* m, double* grad, double* energy);
+int tm_energy_update_reference_properties(tm_energy* e);
+int tm_energy_update_repulsion(tm_energy* e, tm_mesh* m);
+/* Local stencil precision: 0 FP64 (default), 1 FP32 (FP64 differences of
+ * positions and FP64 global sums). */
+int tm_energy_set_stencil_precision(tm_energy* e, int mode);
+
+/* Device-resident evaluation: positions, gradient and energy live in device
+ * memory, nothing is copied to the host and the call does not synchronise.
+ * Runs on `stream` (a cudaStream_t, NULL for the handle's own stream).
+ * d_grad or d_energy may be NULL. */
+int tm_energy_eval_device(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
+                          double* d_energy, void* stream);
+/* tm_energy_eval_device with CUDA events on the launching stream around each
+ * kernel; ms5 = {face, edge, vertex (+reduction), gradient, total} in ms.
+ * Synchronises.  A measurement aid, no counterpart in the reference. */
+int tm_energy_eval_timed(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, float* ms5,
+                         void* stream);
+/* Rebuilds the neighbour list from device-resident positions. */
+int tm_energy_update_repulsion_device(tm_energy* e, tm_mesh* m, const double* d_points, void* stream);
+
+/* ---- neighbour lists (src/nlists/nlist.h:15-40, nlist.cpp:10-53) --------
+ * n_search, exclusion_level and rlist are read from p.  Unknown n_search or
+ * exclusion level: TM_ERR_ARG (RuntimeError in the reference). */
+int tm_nlist_create(tm_mesh* m, const tm_params* p, tm_nlist** out);
+int tm_nlist_destroy(tm_nlist* nl);
+/* distance_matrix(mesh, rdist): the cell list returns each pair once as
+ * (i < j) with d <= rdist, the Verlet list both orders with d < rdist. */
+int tm_nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, double rdist, int64_t* count);
+/* point_distances(mesh, pid, rdist): x_pid - x_j for the neighbours j with
+ * |x_pid - x_j| < rdist. */
+int tm_nlist_point_distances(tm_nlist* nl, tm_mesh* m, int64_t pid, double rdist, int64_t* count);
+/* Copies the last result: distance_matrix -> (d, i, j); point_distances ->
+ * (d as (count,3), j); i may be NULL for the latter. */
+int tm_nlist_fetch(tm_nlist* nl, double* d, int32_t* i, int32_t* j);
+
+/* ---- edge flips (src/flips.cpp:22-165, src/bindings.cpp:839-891) --------
+ * Metropolis edge-flip sweep over floor(n_edges * ratio) proposals.
+ * mode 0 (flip): proposals are evaluated in proposal order; mode 1 (pflip):
+ * proposals are evaluated in conflict-free batches of `batch`, a proposal
+ * whose patch overlaps a lower one waits for the next batch.  ratio > 1 is
+ * TM_ERR_RANGE in mode 1.  Deterministic for a given seed. */
+int tm_flip(tm_mesh* m, tm_energy* e, double ratio, uint64_t seed, int mode, int batch, int32_t* accepted);
+/* The same sweep on device-resident positions (n_vertices*3 doubles); the
+ * topology of m is updated in place, *accepted is returned after the sweep. */
+int tm_flip_device(tm_mesh* m, tm_energy* e, const double* d_points, double ratio, uint64_t seed, int mode,
+                   int batch, int32_t* accepted, void* stream);
+
+/* ---- utilities (src/util.cpp:9-41, src/bindings.cpp:25-50) -------------- */
+int tm_area(tm_mesh* m, double* out);
+int tm_edges_length(tm_mesh* m, double* out);
+int tm_avg_tri_props(tm_mesh* m, double* mean_area, double* mean_length);
+/* Forward-difference gradient with step eps (3 * n_vertices energies). */
+int tm_fd_gradient(tm_mesh* m, tm_energy* e, double eps, double* grad);
+
+/* ---- device-resident HMC (src/trimem/mc/hmc.py:14-26,133-158) -----------
+ * One Metropolis step: momenta ~ N(0, m*T) drawn on the device from
+ * (seed, step), n_steps velocity-Verlet steps of size dt with mass m, then
+ * accept with probability min(1, exp(-dH/T)) using the uniform u.
+ * d_x (n_vertices*3) is updated in place when accepted.  out[0] = accepted,
+ * out[1] = H(start), out[2] = H(end), out[3] = energy of the returned state.
+ * The neighbour list is the one of the energy manager (not rebuilt). */
+int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double mass, double dt, int n_steps,
+                       double temperature, uint64_t seed, uint64_t step, double u, double* out4, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

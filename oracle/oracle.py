@@ -7,12 +7,13 @@ product package never imports it.
 """
 import ctypes
 import os
+import platform
 import subprocess
 
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_LIB_PATH = os.path.join(_HERE, "_build", platform.machine(), "liboracle.so")
 _lib = None
 
 _d = ctypes.c_double

@@ -1,0 +1,232 @@
+"""Parity of the CUDA path (called through the C ABI) with the oracle.
+
+Tolerances: FP64 properties, energies and gradients within 1e-10 relative
+(norm-wise for the gradient); neighbour pair sets, pair distances and flipped
+topologies bit-exact."""
+import numpy as np
+import pytest
+
+from helpers import autograd_primitives, facet_pair, unit_params, workload_params
+from oracle import oracle as O
+from trimem_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def C(built):
+    from trimem_gb300 import capi
+    return capi
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("alpha", [np.pi / 4, -np.pi / 4])
+def test_primitives_vs_autograd(C, alpha):
+    pts, cells = facet_pair(alpha)
+    m = C.Mesh(pts, cells)
+    for name, (rv, rg) in autograd_primitives(pts).items():
+        v, g = m.prim(name, 0)
+        assert abs(v - rv) <= RTOL * max(1.0, abs(rv)), name
+        assert rel(g, rg) < RTOL, name
+
+
+def _pair(C, p, f, prm):
+    mo = O.Mesh(p, f)
+    eo = O.Energy(mo, O.default_params(**prm))
+    mg = C.Mesh(p, f)
+    eg = C.Energy(mg, C.params(**prm))
+    return mo, eo, mg, eg
+
+
+CASES = [
+    ("L3 cell excl2 edge", 3, dict()),
+    ("L4 cell excl2 edge", 4, dict()),
+    ("L3 area bonds", 3, dict(bond_type=1)),
+    ("L3 verlet excl2", 3, dict(n_search=1)),
+    ("L3 repulsive excl1", 3, dict(excl=1, rep_scale=1.3)),
+    ("L3 repulsive excl0 verlet", 3, dict(excl=0, rep_scale=0.9, n_search=1)),
+]
+
+
+@pytest.mark.parametrize("name,level,kw", CASES, ids=[c[0] for c in CASES])
+def test_energy_and_gradient_parity(C, name, level, kw):
+    p, f = meshgen.jittered_icosphere(level, seed=level)
+    prm = workload_params(p, f, **kw)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    np.testing.assert_allclose(eg.initial_props(), eo.initial_props(), rtol=RTOL, atol=0)
+    # move the vertices after construction: the cell list keeps its bins
+    rng = np.random.default_rng(7)
+    d = rng.normal(0, 1e-3 * meshgen.mean_edge_length(p, f), size=p.shape)
+    mo.points()[:] += d
+    mg.points()[:] += d
+    po, pg = eo.properties(mo), eg.properties(mg)
+    for k in range(6):
+        assert abs(pg[k] - po[k]) <= RTOL * max(abs(po[k]), 1e-300), (k, pg[k], po[k])
+    assert abs(eg.energy(mg) - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+    np.testing.assert_allclose(eg.components(mg), eo.components(mo), rtol=RTOL, atol=1e-300)
+    vo, vg = eo.vertex_properties(mo), eg.vertex_properties(mg)
+    scale = np.abs(vo).max(axis=0) + 1e-300
+    assert (np.abs(vg - vo) / scale).max() < RTOL
+    go = eo.gradient(mo)
+    eng, gg = eg.gradient(mg, with_energy=True)
+    assert rel(gg, go) < RTOL
+    assert abs(eng - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+    if kw.get("rep_scale", 0.8) > 1.0:
+        assert po[5] > 0  # the repulsion is exercised
+
+
+def test_gradient_is_deterministic(C):
+    p, f = meshgen.jittered_icosphere(4, seed=1)
+    prm = workload_params(p, f)
+    mg = C.Mesh(p, f)
+    eg = C.Energy(mg, C.params(**prm))
+    g1 = eg.gradient(mg)
+    g2 = eg.gradient(mg)
+    assert np.array_equal(g1, g2)
+
+
+@pytest.mark.parametrize("bond_type", [0, 1])
+def test_gradient_vs_finite_differences(C, bond_type):
+    p, f = meshgen.icosphere(3)
+    mg = C.Mesh(p, f)
+    eg = C.Energy(mg, C.params(**unit_params(p, f, bond_type)))
+    fd = eg.fd_gradient(mg, 1e-8)
+    assert rel(eg.gradient(mg), fd) < 1e-4
+
+
+def test_reference_state_and_continuation(C):
+    p, f = meshgen.jittered_icosphere(3, seed=2)
+    prm = workload_params(p, f, vfrac=0.7)
+    prm.update(cont_delta=0.25, cont_lambda=0.0, area_frac=0.9, curvature_frac=0.8, kappa_c=10.0)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    for _ in range(6):
+        assert abs(eg.energy(mg) - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+        assert rel(eg.gradient(mg), eo.gradient(mo)) < RTOL
+        eg.update_reference_properties()
+        eo.update_reference_properties()
+
+
+def test_energy_of_given_properties(C):
+    p, f = meshgen.jittered_icosphere(3, seed=4)
+    prm = workload_params(p, f)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    props = eo.properties(mo) * 1.01
+    assert abs(eg.energy_props(props) - eo.energy_props(props)) <= RTOL * abs(eo.energy_props(props))
+
+
+@pytest.mark.parametrize("n_search", [0, 1])
+@pytest.mark.parametrize("excl,nn", [(0, 44), (1, 38), (2, 26)])
+def test_neighbour_exclusion_counts(C, n_search, excl, nn):
+    p, f = meshgen.rect(20, 20)
+    m = C.Mesh(p, f)
+    nl = C.NList(m, C.params(n_search=n_search, exclusion_level=excl, rlist=0.2))
+    _, j = nl.point_distances(m, 151, 0.2)
+    assert len(j) == nn
+
+
+def _pairs(d, i, j):
+    o = np.lexsort((j, i))
+    return np.stack([i[o], j[o]], 1), d[o]
+
+
+@pytest.mark.parametrize("n_search", [0, 1])
+@pytest.mark.parametrize("excl", [0, 1, 2])
+@pytest.mark.parametrize("mesh", ["rect", "sphere"])
+def test_pair_sets_bit_exact(C, n_search, excl, mesh):
+    if mesh == "rect":
+        p, f = meshgen.rect(20, 20)
+        rl, rq = 0.2, 0.123
+    else:
+        p, f = meshgen.jittered_icosphere(4, sigma_rel=0.2, seed=5)
+        l = meshgen.mean_edge_length(p, f)
+        rl, rq = 1.1 * l, 0.9 * l
+    mo = O.Mesh(p, f)
+    mg = C.Mesh(p, f)
+    no = O.NList(mo, n_search, excl, rl)
+    ng = C.NList(mg, C.params(n_search=n_search, exclusion_level=excl, rlist=rl))
+    # stale bins: query with moved positions
+    rng = np.random.default_rng(1)
+    d = rng.normal(0, 0.2 * rl, size=p.shape)
+    mo.points()[:] += d
+    mg.points()[:] += d
+    (po, do), (pg, dg) = _pairs(*no.distance_matrix(mo, rq)), _pairs(*ng.distance_matrix(mg, rq))
+    assert len(po) > 0
+    assert np.array_equal(po, pg)
+    assert np.array_equal(do, dg)  # bit-identical distances
+    for pid in range(0, len(p), max(1, len(p) // 37)):
+        d3o, jo = no.point_distances(mo, pid, rq)
+        d3g, jg = ng.point_distances(mg, pid, rq)
+        assert np.array_equal(jo, jg)
+        assert np.array_equal(d3o, d3g)
+
+
+def _flip_case(C, level=3, kb=1.0):
+    p, f = meshgen.icosphere(level)
+    prm = unit_params(p, f, 0, frac=1.0)
+    prm["kappa_b"] = kb
+    return p, f, prm
+
+
+@pytest.mark.parametrize("mode,batch", [(0, 256), (1, 64), (1, 1024)])
+def test_flip_sweeps_match_cpu_port(C, mode, batch):
+    p, f, prm = _flip_case(C)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    for seed in (3, 4):
+        ao = O.flip_windowed(mo, eo, 0.5, seed, mode, batch)
+        ag = C.flip(mg, eg, 0.5, seed, mode, batch)
+        assert ag == ao
+        assert mg.check() == 0 and mo.check() == 0
+        tg, to = mg.topology(), mo.topology()
+        for k in to:
+            assert np.array_equal(tg[k], to[k]), k
+        assert np.array_equal(mg.fv_indices(), mo.fv_indices())
+    assert ag > 100
+
+
+def test_flip_on_jittered_mesh_with_repulsion(C):
+    p, f = meshgen.jittered_icosphere(4, seed=9)
+    prm = workload_params(p, f, excl=1, rep_scale=1.2)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    ao = O.flip_windowed(mo, eo, 0.2, 21, 1, 512)
+    ag = C.flip(mg, eg, 0.2, 21, 1, 512)
+    assert ag == ao
+    assert np.array_equal(mg.fv_indices(), mo.fv_indices())
+    # energies on the flipped meshes agree as well
+    assert abs(eg.energy(mg) - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+
+
+def test_flip_ratio_errors(C):
+    p, f, prm = _flip_case(C)
+    mg = C.Mesh(p, f)
+    eg = C.Energy(mg, C.params(**prm))
+    with pytest.raises(C.TMError) as ei:
+        C.flip(mg, eg, 1.5, 1, 1)
+    assert ei.value.code == C.TM_ERR_RANGE
+
+
+def test_utilities(C):
+    p, f = meshgen.jittered_icosphere(4, seed=3)
+    mo, mg = O.Mesh(p, f), C.Mesh(p, f)
+    assert abs(mg.area() - O.area(mo)) <= RTOL * O.area(mo)
+    assert abs(mg.edges_length() - O.edges_length(mo)) <= RTOL * O.edges_length(mo)
+    a, l = mg.avg_tri_props()
+    assert abs(a - O.area(mo) / mo.n_faces()) <= RTOL * a
+
+
+def test_large_mesh_properties(C):
+    """Level-6 icosphere (40,962 vertices): parity with the oracle and the
+    size-independent invariances (closed surface: translation leaves the
+    energy unchanged, so the gradient sums to zero)."""
+    p, f = meshgen.jittered_icosphere(6, seed=0)
+    prm = workload_params(p, f)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    e, g = eg.gradient(mg, with_energy=True)
+    assert abs(e - eo.energy(mo)) <= RTOL * abs(e)
+    assert rel(g, eo.gradient(mo)) < RTOL
+    assert np.linalg.norm(g.sum(0)) < 1e-8 * np.linalg.norm(g)

@@ -1,0 +1,121 @@
+"""The oracle against the reference's own known answers
+(tests/test_properties.py, test_energy.py, test_gradient.py,
+test_neighbours.py, test_flips.py of the reference)."""
+import numpy as np
+import pytest
+
+from helpers import autograd_primitives, facet_pair, unit_params, workload_params
+from oracle import oracle as O
+from trimem_gb300 import meshgen
+
+
+@pytest.mark.parametrize("alpha", [np.pi / 4, -np.pi / 4])
+def test_primitives_vs_autograd(alpha):
+    pts, cells = facet_pair(alpha)
+    m = O.Mesh(pts, cells)
+    ref = autograd_primitives(pts)
+    for name, (rv, rg) in ref.items():
+        v, g = O.prim(m, name, 0)
+        assert abs(v - rv) <= 1e-10 * max(1.0, abs(rv))
+        assert np.linalg.norm(g - rg) / np.linalg.norm(rg) < 1e-10
+
+
+@pytest.mark.parametrize("name,radius", [("sphere", 1.0), ("sphere", 0.5), ("tube", 1.0), ("tube", 0.5)])
+def test_energy_aggregates(name, radius):
+    if name == "sphere":
+        p, f = meshgen.icosphere(5)
+        p = p * radius
+        ref = (4 * np.pi * radius**2, 4 / 3 * np.pi * radius**3, 4 * np.pi * radius, 8 * np.pi)
+    else:
+        p, f = meshgen.tube(length=1, radius=radius, segments=32)
+        ref = (2 * np.pi * radius, 2 / 3 * np.pi * radius**2, np.pi, np.pi / radius)
+    m = O.Mesh(p, f)
+    e = O.Energy(m, O.default_params())
+    pr = e.properties(m)
+    for k in range(4):
+        assert abs(pr[k] - ref[k]) / ref[k] < 1e-2
+
+
+@pytest.mark.parametrize("bond_type", [0, 1])
+def test_gradient_vs_finite_differences(bond_type):
+    p, f = meshgen.icosphere(3)
+    m = O.Mesh(p, f)
+    e = O.Energy(m, O.default_params(**unit_params(p, f, bond_type)))
+    fd = e.fd_gradient(m, 1e-8)
+    g = e.gradient(m)
+    assert np.linalg.norm(g - fd) / np.linalg.norm(fd) < 1e-4
+
+
+def test_gradient_with_repulsion_vs_finite_differences():
+    p, f = meshgen.jittered_icosphere(2, sigma_rel=0.3, seed=3)
+    m = O.Mesh(p, f)
+    prm = workload_params(p, f, rep_scale=1.2, excl=1)
+    e = O.Energy(m, O.default_params(**prm))
+    assert e.properties(m)[5] > 0  # some pairs inside the cut-off
+    fd = e.fd_gradient(m, 1e-8)
+    g = e.gradient(m)
+    assert np.linalg.norm(g - fd) / np.linalg.norm(fd) < 1e-4
+
+
+@pytest.mark.parametrize("n_search", [0, 1])
+@pytest.mark.parametrize("excl,nn", [(0, 44), (1, 38), (2, 26)])
+def test_neighbour_exclusion_counts(n_search, excl, nn):
+    p, f = meshgen.rect(20, 20)
+    m = O.Mesh(p, f)
+    nl = O.NList(m, n_search, excl, 0.2)
+    _, j = nl.point_distances(m, 151, 0.2)
+    assert len(j) == nn
+
+
+@pytest.mark.parametrize("n_search", [0, 1])
+@pytest.mark.parametrize("rlist", [0.2, 0.5, 1.2])
+def test_distance_matrix_vs_kdtree(n_search, rlist):
+    from scipy.sparse import coo_matrix
+    from scipy.spatial import KDTree
+
+    p, f = meshgen.rect(20, 20)
+    m = O.Mesh(p, f)
+    nl = O.NList(m, n_search, 0, rlist)
+    d, i, j = nl.distance_matrix(m, 0.123)
+    M = coo_matrix((d, (i, j)), shape=(len(p), len(p)))
+    if n_search == 0:
+        M = M + M.T
+    T = KDTree(p)
+    C = T.sparse_distance_matrix(T, 0.123)
+    assert np.allclose(C.todense(), M.todense())
+
+
+def _flip_setup():
+    p, f = meshgen.icosphere(3)
+    m = O.Mesh(p, f)
+    prm = unit_params(p, f, 0, frac=1.0)
+    prm["kappa_c"] = 1.0
+    e = O.Energy(m, O.default_params(**prm))
+    return m, e
+
+
+@pytest.mark.parametrize("fn", ["flip_serial", "flip_parallel"])
+def test_flips_accept_and_keep_manifold(fn):
+    m, e = _flip_setup()
+    acc = getattr(O, fn)(m, e, 0.5, 11)
+    assert acc > 100
+    assert m.check() == 0
+
+
+def test_windowed_flip_port_orders():
+    m0, e = _flip_setup()
+    res = []
+    for mode, batch in [(0, 1), (0, 64), (1, 64), (1, 512)]:
+        m = m0.clone()
+        acc = O.flip_windowed(m, e, 0.5, 5, mode, batch)
+        assert m.check() == 0
+        res.append((acc, m.fv_indices()))
+    # mode 0 decides in proposal order whatever the window size
+    assert res[0][0] == res[1][0] and (res[0][1] == res[1][1]).all()
+    assert all(r[0] > 100 for r in res)
+
+
+def test_parallel_flip_ratio_above_one_raises():
+    m, e = _flip_setup()
+    with pytest.raises(ValueError):
+        O.flip_parallel(m, e, 1.5, 1)

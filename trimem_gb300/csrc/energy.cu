@@ -1,0 +1,578 @@
+// Energy manager: vertex properties, penalty assembly and gradient.
+//
+// The reference evaluates, per vertex, every incident face and edge again
+// (src/mesh_properties.cpp:12-148), i.e. each face three times and each edge
+// two to four times per pass, with acos/tan per call.  On GB300 (FP64 issue
+// rate ~1/58 of FP32) the kernels instead compute each face and each edge once
+// per evaluation and gather them per vertex:
+//
+//   k_face   (one thread per face)  unit normal, area, signed volume and the
+//            cotangents of the three corners (u.v / |u x v|, no acos/tan)
+//   k_edge   (one thread per edge)  length, signed dihedral angle, tether
+//            bond value and derivative
+//   k_vertex (one thread per vertex) area/volume/curvature/tether sums of
+//            the ring, bending 2c^2/a, repulsion (and its gradient), a
+//            fixed-order block reduction of the six global sums; the last
+//            block reduces the block partials in fixed order and assembles
+//            energy and the penalty gradient factors on the device
+//   k_grad   (one thread per vertex) gather of dE/dx_i over the ring
+//
+// No atomics touch floating-point data, so every result is bit-reproducible.
+// With w_e = gC/2 + kb (rho_i + rho_j) (rho = curvature/area per vertex) the
+// gradient is
+//   sum_f [gA - 2/3 kb (rho_a^2+rho_b^2+rho_c^2) (+ kt dpen)] dA_f
+//   + gV dV_f + sum_e (w_e theta_e + kt dbond_e) dl_e + w_e l_e dtheta_e
+//   + kr drep,
+// which is the reference's gather (src/mesh_properties.cpp:51-148 with
+// src/kernel.h:124-137) regrouped per face and edge.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+#include "tm_internal.h"
+#include "tm_math.cuh"
+#include "tm_energy.cuh"
+
+using namespace tmg;
+
+#define TM_API_BEGIN try {
+#define TM_API_END                  \
+  }                                 \
+  catch (const tmg::Error& e) {     \
+    tmg::set_last_error(e.what());  \
+    return e.code;                  \
+  }                                 \
+  catch (const std::exception& e) { \
+    tmg::set_last_error(e.what());  \
+    return TM_ERR_ARG;              \
+  }                                 \
+  return TM_OK;
+
+namespace tmg {
+
+// ---- per-face and per-edge quantities ------------------------------------
+__global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__ fd) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= t.nf) return;
+  int a = t.fv[3 * f], b = t.fv[3 * f + 1], c = t.fv[3 * f + 2];
+  d3 pa = ld3(P, a), pb = ld3(P, b), pc = ld3(P, c);
+  d3 eab = pb - pa, eac = pc - pa, ebc = pc - pb;
+  d3 N = cross(eab, eac);
+  double nn = norm(N);
+  double inv = 1.0 / nn;
+  FaceD F;
+  F.nx = N.x * inv;
+  F.ny = N.y * inv;
+  F.nz = N.z * inv;
+  F.A = 0.5 * nn;
+  F.V = dot(cross(pa, pb), pc) * (1.0 / 6.0);
+  F.c0 = dot(eab, eac) * inv;
+  F.c1 = -dot(eab, ebc) * inv;
+  F.c2 = dot(eac, ebc) * inv;
+  fd[f] = F;
+}
+
+__global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd, EdgeD* __restrict__ ed,
+                       double* __restrict__ ebond, EP ep) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.ne) return;
+  int4 E = t.edge[e];
+  d3 pi = ld3(P, E.x), pj = ld3(P, E.y);
+  d3 ev = pj - pi;
+  double l = norm(ev);
+  EdgeD o;
+  o.l = l;
+  o.th = 0.0;
+  o.flag = 0.0;
+  if (E.z >= 0 && E.w >= 0) {
+    FaceD F0 = fd[E.z], F1 = fd[E.w];
+    d3 n0 = mk(F0.nx, F0.ny, F0.nz), n1 = mk(F1.nx, F1.ny, F1.nz);
+    double c = fmin(1.0, fmax(-1.0, dot(n0, n1)));
+    double a = acos(c);
+    o.th = dot(cross(n0, n1), ev) >= 0.0 ? a : -a;
+    o.flag = 1.0;
+  }
+  // flat-bottom edge penalty and its derivative (src/mesh_tether.h:29-85)
+  double val = 0.0, fac = 0.0;
+  if (ep.btype == 0) {
+    int r = ep.r;
+    if (l > ep.lc0) {
+      val = ipow((double)r, r + 1) * ipow(l - ep.lc0, r);
+      fac = ipow((double)r, r + 2) * ipow(l - ep.lc0, r - 1);
+    } else if (l < ep.lc1) {
+      val = exp(l / (l - ep.lc1)) / ipow(l, r);
+    }
+    if (l < ep.lc1) {
+      double lmc = l - ep.lc1;
+      fac -= ep.lc1 / (lmc * lmc) + r / l;
+      fac /= ipow(l, r);
+      fac *= exp(l / lmc);
+    }
+  }
+  o.db = fac;
+  ed[e] = o;
+  ebond[e] = val;
+}
+
+template <bool GRAD, bool VPROPS>
+__global__ void __launch_bounds__(VB) k_vertex(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd,
+                                              const EdgeD* __restrict__ ed, const double* __restrict__ ebond,
+                                              NLView nl, EP ep, double* __restrict__ rho, double* __restrict__ repg,
+                                              double* __restrict__ vprops, double* __restrict__ partial,
+                                              Globals* g) {
+  __shared__ double red[6][VB];
+  __shared__ bool last;
+  int v = blockIdx.x * VB + threadIdx.x;
+  double pr[6] = {0, 0, 0, 0, 0, 0};
+  if (v < t.nv) {
+    int d = t.val[v];
+    double A = 0, V = 0, LT = 0, T = 0;
+    for (int m = 0; m < d; ++m) {
+      int4 s = t.slot[(size_t)m * t.nv + v];
+      int f = slot_face(s.y);
+      if (f < 0) continue;
+      double fa = fd[f].A;
+      A += fa;
+      V += fd[f].V;
+      EdgeD E = ed[s.z];
+      LT += E.l * E.th;
+      if (ep.btype == 0) {
+        T += ebond[s.z];
+      } else {
+        double q = fa / ep.a0 - 1.0;
+        T += q * q;
+      }
+    }
+    double a = A / 3, c = 0.25 * LT;
+    pr[0] = a;
+    pr[1] = V / 3;
+    pr[2] = c;
+    pr[3] = 2 * c * c / a;
+    pr[4] = T / ep.tdiv;
+    d3 p = ld3(P, v);
+    double pot = 0.0;
+    d3 gr = mk(0, 0, 0);
+    const double lc1 = ep.rlc1;
+    const int rr = ep.rr;
+    for_each_neighbour(nl, t, P, v, p, lc1, [&](int, double l, d3 dvec) {
+      double lmc = l - lc1;
+      double ex = exp(l / lmc);
+      pot += ex / ipow(l, rr);
+      if (GRAD) {
+        double fac = -(lc1 / (lmc * lmc) + rr / l);
+        fac /= ipow(l, rr + 1);
+        fac *= ex;
+        gr += fac * dvec;
+      }
+    });
+    pr[5] = pot;
+    rho[v] = c / a;
+    if (GRAD) st3(repg, v, 2.0 * gr);
+    if (VPROPS)
+      for (int k = 0; k < 6; ++k) vprops[6 * (size_t)v + k] = pr[k];
+  }
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = pr[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) partial[8 * (size_t)blockIdx.x + k] = red[k][0];
+    __threadfence();
+    unsigned int tk = atomicAdd(&g->ticket, 1u);
+    last = (tk == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // last block: fixed-order reduction of the block partials
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += VB)
+    for (int k = 0; k < 6; ++k) acc[k] += ((volatile double*)partial)[8 * (size_t)b + k];
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) g->props[k] = red[k][0];
+    assemble(ep, g);
+    g->ticket = 0;
+  }
+}
+
+__global__ void k_assemble_props(EP ep, const double* props6, Globals* g) {
+  if (threadIdx.x || blockIdx.x) return;
+  for (int k = 0; k < 6; ++k) g->props[k] = props6[k];
+  assemble(ep, g);
+}
+
+// ---- gradient gather ------------------------------------------------------
+__global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd,
+                                             const EdgeD* __restrict__ ed, const double* __restrict__ rho,
+                                             const double* __restrict__ repg, const Globals* __restrict__ g, EP ep,
+                                             double* __restrict__ grad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.nv) return;
+  const double gA = g->gA, gV = g->gV, gC = g->gC;
+  const double kb = ep.kb;
+  const double hgC = 0.5 * gC;
+  const double kb23 = kb * (2.0 / 3.0);
+  d3 xi = ld3(P, i);
+  double ri = rho[i];
+  d3 acc = ep.kr * ld3(repg, i);
+  int d = t.val[i];
+  if (d > 0) {
+    const size_t nv = t.nv;
+    int4 sp = t.slot[(size_t)(d - 1) * nv + i];
+    d3 xk = ld3(P, sp.x);
+    double rk = rho[sp.x];
+    int4 sc = t.slot[i];
+    d3 xj = ld3(P, sc.x);
+    double rj = rho[sc.x];
+    FaceD Fc;
+    int fcur = slot_face(sc.y);
+    if (fcur >= 0) Fc = fd[fcur];
+    for (int m = 0; m < d; ++m) {
+      int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
+      int fnx = slot_face(sn.y);
+      FaceD Fn;
+      if (fnx >= 0) Fn = fd[fnx];
+      if (fcur >= 0) {
+        int ci = slot_corner(sc.y);
+        double cj = cot_at(Fc, ci == 2 ? 0 : ci + 1);
+        double ck = cot_at(Fc, ci == 0 ? 2 : ci - 1);
+        d3 n = mk(Fc.nx, Fc.ny, Fc.nz);
+        // face (i, j, k): area and volume terms
+        double alpha = gA - kb23 * (ri * ri + rj * rj + rk * rk);
+        if (ep.btype == 1) alpha += ep.kt * 2.0 * (Fc.A / ep.a0 - 1.0) / ep.a0;
+        acc += (0.5 * alpha) * cross(n, xk - xj);
+        acc += (gV * (1.0 / 6.0)) * cross(xj, xk);
+        // edge (i, j): length and dihedral terms
+        EdgeD E = ed[sc.z];
+        double w = hgC + kb * (ri + rj);
+        double cl = w * E.th + (ep.btype == 0 ? ep.kt * E.db : 0.0);
+        acc += (-cl / E.l) * (xj - xi);
+        if (E.flag != 0.0) {
+          int cin = slot_corner(sn.y);
+          double cjn = cot_at(Fn, cin == 0 ? 2 : cin - 1);
+          acc += w * (cj * n + cjn * mk(Fn.nx, Fn.ny, Fn.nz));
+        }
+        // edge (j, k) opposite i: dihedral term
+        if (ed[sc.w].flag != 0.0) {
+          double wo = hgC + kb * (rj + rk);
+          acc += (-wo * (cj + ck)) * n;
+        }
+      }
+      xk = xj;
+      rk = rj;
+      sc = sn;
+      fcur = fnx;
+      Fc = Fn;
+      xj = ld3(P, sn.x);
+      rj = rho[sn.x];
+    }
+  }
+  st3(grad, i, acc);
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+EP make_ep(const tm_energy* e) {
+  const tm_params& p = e->prm;
+  EP ep;
+  ep.kb = p.kappa_b;
+  ep.ka = p.kappa_a;
+  ep.kv = p.kappa_v;
+  ep.kc = p.kappa_c;
+  ep.kt = p.kappa_t;
+  ep.kr = p.kappa_r;
+  double lam = p.cont_lambda;
+  ep.refA = (1.0 - lam * (1.0 - p.area_frac)) * e->initial[0];
+  ep.refV = (1.0 - lam * (1.0 - p.volume_frac)) * e->initial[1];
+  ep.refC = (1.0 - lam * (1.0 - p.curvature_frac)) * e->initial[2];
+  ep.lc0 = p.bond_lc0;
+  ep.lc1 = p.bond_lc1;
+  ep.a0 = p.bond_a0;
+  ep.r = p.bond_r;
+  ep.btype = p.bond_type;
+  ep.rlc1 = p.rep_lc1;
+  ep.rr = p.rep_r;
+  ep.tdiv = p.bond_type == 0 ? 2.0 : 3.0;
+  return ep;
+}
+
+void energy_eval(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool want_vprops, double* d_grad,
+                 cudaStream_t s) {
+  energy_eval_marked(e, m, P, want_grad, want_vprops, d_grad, s, nullptr);
+}
+
+void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool want_vprops, double* d_grad,
+                        cudaStream_t s, cudaEvent_t* ev) {
+  if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
+  e->ensure(m->nv, m->ne, m->nf);
+  Topo t = m->topo();
+  EP ep = make_ep(e);
+  FaceD* fd = reinterpret_cast<FaceD*>(e->face.get());
+  EdgeD* ed = reinterpret_cast<EdgeD*>(e->edge.get());
+  if (t.nf) k_face<<<nblk(t.nf, 256), 256, 0, s>>>(t, P, fd);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
+  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
+  int nb = std::max(1, nblk(t.nv, VB));
+#define TM_KV(G, VP)                                                                                         \
+  k_vertex<G, VP><<<nb, VB, 0, s>>>(t, P, fd, ed, e->ebond.get(), e->nl.view, ep, e->rho.get(), e->repg.get(), \
+                                    e->vprops.get(), e->partials.get(), e->glob.get())
+  if (want_grad && want_vprops)
+    TM_KV(true, true);
+  else if (want_grad)
+    TM_KV(true, false);
+  else if (want_vprops)
+    TM_KV(false, true);
+  else
+    TM_KV(false, false);
+#undef TM_KV
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
+  if (want_grad && t.nv)
+    k_grad<<<nblk(t.nv, 256), 256, 0, s>>>(t, P, fd, ed, e->rho.get(), e->repg.get(), e->glob.get(), ep, d_grad);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[4], s));
+}
+
+void energy_from_props_device(tm_energy* e, const double* d_props6, double* /*unused*/, cudaStream_t s) {
+  EP ep = make_ep(e);
+  k_assemble_props<<<1, 1, 0, s>>>(ep, d_props6, e->glob.get());
+  TM_LAUNCH();
+}
+
+}  // namespace tmg
+
+void tm_energy::ensure(int nv_, int ne_, int nf_) {
+  if (nv_ == nv && ne_ == ne && nf_ == nf && glob.get()) return;
+  nv = nv_;
+  ne = ne_;
+  nf = nf_;
+  face.ensure(8 * (size_t)std::max(nf, 1));
+  edge.ensure(4 * (size_t)std::max(ne, 1));
+  ebond.ensure(std::max(ne, 1));
+  rho.ensure(std::max(nv, 1));
+  repg.ensure(3 * (size_t)std::max(nv, 1));
+  vprops.ensure(6 * (size_t)std::max(nv, 1));
+  int nb = std::max(1, (nv + tmg::VB - 1) / tmg::VB);
+  partials.ensure(8 * (size_t)nb);
+  grad.ensure(3 * (size_t)std::max(nv, 1));
+  work.ensure(64);
+  glob.ensure(1);
+  TM_CUDA(cudaMemsetAsync(glob.get(), 0, sizeof(tmg::Globals), stream));
+}
+
+tm_energy::~tm_energy() {
+  if (stream) cudaStreamDestroy(stream);
+}
+
+// --------------------------------------------------------------------------
+// C ABI
+// --------------------------------------------------------------------------
+static void check_params(const tm_params& p) {
+  if (p.bond_type != 0 && p.bond_type != 1) fail(TM_ERR_ARG, "Unknown bond potential");
+  if (p.n_search != 0 && p.n_search != 1) fail(TM_ERR_ARG, "Unknown neighbour search algorithm.");
+  if (p.exclusion_level < 0 || p.exclusion_level > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
+}
+
+static void fetch_globals(tm_energy* e, tmg::Globals* g) {
+  TM_CUDA(cudaMemcpyAsync(g, e->glob.get(), sizeof(tmg::Globals), cudaMemcpyDeviceToHost, e->stream));
+  TM_CUDA(cudaStreamSynchronize(e->stream));
+}
+
+static void eval_host(tm_energy* e, tm_mesh* m, bool grad, bool vprops) {
+  if (!e || !m) fail(TM_ERR_ARG, "NULL handle");
+  m->upload_points(e->stream);
+  tmg::energy_eval(e, m, m->d_pts.get(), grad, vprops, e->grad.get(), e->stream);
+}
+
+extern "C" {
+
+int tm_energy_create(tm_mesh* m, const tm_params* p, tm_energy** out) {
+  TM_API_BEGIN
+  if (!m || !p || !out) fail(TM_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  check_params(*p);
+  std::unique_ptr<tm_energy> e(new tm_energy());
+  e->prm = *p;
+  TM_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  m->upload_points(e->stream);
+  tmg::nlist_make(&e->nl, m, e->prm, m->d_pts.get(), e->stream);
+  // initial properties: the reference properties are still unset (zero) and
+  // only the sums matter here
+  tmg::energy_eval(e.get(), m, m->d_pts.get(), false, false, nullptr, e->stream);
+  tmg::Globals g;
+  fetch_globals(e.get(), &g);
+  for (int k = 0; k < 6; ++k) e->initial[k] = g.props[k];
+  *out = e.release();
+  TM_API_END
+}
+
+int tm_energy_destroy(tm_energy* e) {
+  delete e;
+  return TM_OK;
+}
+
+int tm_energy_get_params(tm_energy* e, tm_params* out) {
+  if (!e || !out) return TM_ERR_ARG;
+  *out = e->prm;
+  return TM_OK;
+}
+
+int tm_energy_initial_props(tm_energy* e, double* out6) {
+  if (!e || !out6) return TM_ERR_ARG;
+  std::memcpy(out6, e->initial, sizeof(double) * 6);
+  return TM_OK;
+}
+
+int tm_energy_properties(tm_energy* e, tm_mesh* m, double* out6) {
+  TM_API_BEGIN
+  if (!out6) fail(TM_ERR_ARG, "NULL output");
+  eval_host(e, m, false, false);
+  tmg::Globals g;
+  fetch_globals(e, &g);
+  std::memcpy(out6, g.props, sizeof(double) * 6);
+  TM_API_END
+}
+
+int tm_energy_vertex_properties(tm_energy* e, tm_mesh* m, double* out6v) {
+  TM_API_BEGIN
+  if (!out6v) fail(TM_ERR_ARG, "NULL output");
+  eval_host(e, m, false, true);
+  TM_CUDA(cudaMemcpyAsync(out6v, e->vprops.get(), sizeof(double) * 6 * m->nv, cudaMemcpyDeviceToHost, e->stream));
+  TM_CUDA(cudaStreamSynchronize(e->stream));
+  TM_API_END
+}
+
+int tm_energy_energy(tm_energy* e, tm_mesh* m, double* energy) {
+  TM_API_BEGIN
+  if (!energy) fail(TM_ERR_ARG, "NULL output");
+  eval_host(e, m, false, false);
+  tmg::Globals g;
+  fetch_globals(e, &g);
+  *energy = g.comps[6];
+  TM_API_END
+}
+
+int tm_energy_energy_props(tm_energy* e, const double* props6, double* energy) {
+  TM_API_BEGIN
+  if (!e || !props6 || !energy) fail(TM_ERR_ARG, "NULL argument");
+  e->ensure(std::max(e->nv, 1), std::max(e->ne, 1), std::max(e->nf, 1));
+  TM_CUDA(cudaMemcpyAsync(e->work.get(), props6, sizeof(double) * 6, cudaMemcpyHostToDevice, e->stream));
+  tmg::energy_from_props_device(e, e->work.get(), nullptr, e->stream);
+  tmg::Globals g;
+  fetch_globals(e, &g);
+  *energy = g.comps[6];
+  TM_API_END
+}
+
+int tm_energy_components(tm_energy* e, tm_mesh* m, double* out7) {
+  TM_API_BEGIN
+  if (!out7) fail(TM_ERR_ARG, "NULL output");
+  eval_host(e, m, false, false);
+  tmg::Globals g;
+  fetch_globals(e, &g);
+  std::memcpy(out7, g.comps, sizeof(double) * 7);
+  TM_API_END
+}
+
+int tm_energy_gradient(tm_energy* e, tm_mesh* m, double* grad, double* energy) {
+  TM_API_BEGIN
+  if (!grad) fail(TM_ERR_ARG, "NULL output");
+  eval_host(e, m, true, false);
+  TM_CUDA(cudaMemcpyAsync(grad, e->grad.get(), sizeof(double) * 3 * m->nv, cudaMemcpyDeviceToHost, e->stream));
+  if (energy)
+    TM_CUDA(cudaMemcpyAsync(energy, &e->glob.get()->comps[6], sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  TM_CUDA(cudaStreamSynchronize(e->stream));
+  TM_API_END
+}
+
+int tm_energy_update_reference_properties(tm_energy* e) {
+  if (!e) return TM_ERR_ARG;
+  if (e->prm.cont_lambda < 1.0) e->prm.cont_lambda += e->prm.cont_delta;
+  return TM_OK;
+}
+
+int tm_energy_update_repulsion(tm_energy* e, tm_mesh* m) {
+  TM_API_BEGIN
+  if (!e || !m) fail(TM_ERR_ARG, "NULL handle");
+  m->upload_points(e->stream);
+  tmg::nlist_make(&e->nl, m, e->prm, m->d_pts.get(), e->stream);
+  TM_CUDA(cudaStreamSynchronize(e->stream));
+  TM_API_END
+}
+
+int tm_energy_set_stencil_precision(tm_energy* e, int mode) {
+  TM_API_BEGIN
+  if (!e) fail(TM_ERR_ARG, "NULL handle");
+  if (mode != 0 && mode != 1) fail(TM_ERR_ARG, "mode must be 0 (FP64) or 1 (FP32)");
+  e->stencil = mode;
+  TM_API_END
+}
+
+int tm_energy_eval_device(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, double* d_energy,
+                          void* stream) {
+  TM_API_BEGIN
+  if (!e || !m || !d_points) fail(TM_ERR_ARG, "NULL argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  tmg::energy_eval(e, m, d_points, d_grad != nullptr, false, d_grad, s);
+  if (d_energy)
+    TM_CUDA(cudaMemcpyAsync(d_energy, &e->glob.get()->comps[6], sizeof(double), cudaMemcpyDeviceToDevice, s));
+  TM_API_END
+}
+
+int tm_energy_eval_timed(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, float* ms5,
+                         void* stream) {
+  TM_API_BEGIN
+  if (!e || !m || !d_points || !ms5) fail(TM_ERR_ARG, "NULL argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  cudaEvent_t ev[5];
+  for (int k = 0; k < 5; ++k) TM_CUDA(cudaEventCreate(&ev[k]));
+  tmg::energy_eval_marked(e, m, d_points, d_grad != nullptr, false, d_grad, s, ev);
+  TM_CUDA(cudaEventSynchronize(ev[4]));
+  for (int k = 0; k < 4; ++k) TM_CUDA(cudaEventElapsedTime(&ms5[k], ev[k], ev[k + 1]));
+  TM_CUDA(cudaEventElapsedTime(&ms5[4], ev[0], ev[4]));
+  for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
+  TM_API_END
+}
+
+int tm_energy_update_repulsion_device(tm_energy* e, tm_mesh* m, const double* d_points, void* stream) {
+  TM_API_BEGIN
+  if (!e || !m || !d_points) fail(TM_ERR_ARG, "NULL argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  tmg::nlist_make(&e->nl, m, e->prm, d_points, s);
+  TM_API_END
+}
+
+int tm_fd_gradient(tm_mesh* m, tm_energy* e, double eps, double* grad) {
+  TM_API_BEGIN
+  if (!m || !e || !grad) fail(TM_ERR_ARG, "NULL argument");
+  double e0 = 0;
+  int rc = tm_energy_energy(e, m, &e0);
+  if (rc) return rc;
+  for (int i = 0; i < m->nv; ++i)
+    for (int k = 0; k < 3; ++k) {
+      double* x = m->h_pts + 3 * (size_t)i + k;
+      *x += eps;
+      double en = 0;
+      rc = tm_energy_energy(e, m, &en);
+      *x -= eps;
+      if (rc) return rc;
+      grad[3 * (size_t)i + k] = (en - e0) / eps;
+    }
+  TM_API_END
+}
+
+}  // extern "C"

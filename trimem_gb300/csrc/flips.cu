@@ -1,0 +1,509 @@
+// Metropolis edge-flip sweep (src/flips.cpp:22-165, src/flip_utils.cpp:19-114).
+//
+// The reference draws random edges and either flips them one by one
+// (flip_serial) or lets OpenMP threads lock the edge patches of their
+// proposals and serialises the acceptance in a critical section
+// (flip_parallel_batches).  Here a sweep is a sequence of windows of
+// proposals, every step on the device:
+//   k_fill    window = deferred proposals (in order) + new proposals
+//   k_claim   each proposal claims the edges of its patch (the 1-ring edges
+//             of the quad's four vertices and the edges opposite them,
+//             flip_utils.cpp:43-68) with atomicMin of its window slot
+//   k_winner  a proposal whose patch it owns entirely is a winner; in
+//             serial mode the window is cut at the first loser, so proposals
+//             are decided in proposal order
+//   k_delta   8 threads per winner evaluate the vertex properties of the
+//             four quad vertices before and after a virtual flip (the mesh is
+//             not touched), including the repulsion with the post-flip
+//             exclusion rings
+//   k_metro   one thread walks the window in slot order: props -= dprops,
+//             Metropolis with T = 1 (flips.cpp:142-160), losers are queued
+//             for the next window
+//   k_commit  accepted flips rewrite their six halfedges, two faces, five
+//             edge rows and four ring rows; patches are disjoint, so commits
+//             never touch the same entries
+// Proposals come from a counter-based SplitMix64 stream of (seed, index), so
+// a sweep is reproducible and matches the CPU port of this algorithm.
+// A flip is also refused when it would raise a valence above TM_MAXVAL.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "tm_energy.cuh"
+#include "tm_internal.h"
+#include "tm_math.cuh"
+#include "tm_topo.cuh"
+
+using namespace tmg;
+
+#define TM_API_BEGIN try {
+#define TM_API_END                  \
+  }                                 \
+  catch (const tmg::Error& e) {     \
+    tmg::set_last_error(e.what());  \
+    return e.code;                  \
+  }                                 \
+  catch (const std::exception& e) { \
+    tmg::set_last_error(e.what());  \
+    return TM_ERR_ARG;              \
+  }                                 \
+  return TM_OK;
+
+namespace tmg {
+namespace {
+
+constexpr int MAXB = 4096;  // largest window
+
+__host__ __device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ unsigned long long flip_key(unsigned long long seed, long long p, int stream) {
+  return splitmix64(splitmix64(seed) ^ (unsigned long long)(2 * p + stream));
+}
+__device__ __forceinline__ int flip_edge_of(unsigned long long seed, long long p, int ne) {
+  return (int)(((flip_key(seed, p, 0) >> 32) * (unsigned long long)ne) >> 32);
+}
+__device__ __forceinline__ double flip_u_of(unsigned long long seed, long long p) {
+  return (double)(flip_key(seed, p, 1) >> 11) * 0x1.0p-53;
+}
+
+struct FlipState {
+  double props[8];
+  double e0;
+  int acc;
+  int limit;
+  int npend;
+  int status;
+};
+
+struct Quad {
+  int va0, va1, vb0, vb1;
+};
+__device__ __forceinline__ Quad quad_of(const TopoW& t, int e) {
+  Quad q;
+  int a0 = 2 * e, b0 = 2 * e + 1;
+  q.va0 = t.to[a0];
+  q.va1 = t.to[t.next[a0]];
+  q.vb0 = t.to[b0];
+  q.vb1 = t.to[t.next[b0]];
+  return q;
+}
+
+template <class F>
+__device__ __forceinline__ void for_patch(const TopoW& t, const Quad& q, F&& fn) {
+  int vs[4] = {q.va0, q.va1, q.vb0, q.vb1};
+  for (int k = 0; k < 4; ++k) {
+    int v = vs[k];
+    int d = t.val[v];
+    for (int m = 0; m < d; ++m) {
+      int4 s = t.slot[(size_t)m * t.nv + v];
+      fn(s.z);
+      fn(s.w);
+    }
+  }
+}
+
+__device__ bool flip_ok(const TopoW& t, int e) {
+  if (t.face[2 * e] < 0 || t.face[2 * e + 1] < 0) return false;
+  int c = t.to[t.next[2 * e]], d = t.to[t.next[2 * e + 1]];
+  if (c == d) return false;
+  int dc = t.val[c];
+  for (int m = 0; m < dc; ++m)
+    if (t.nbr[(size_t)m * t.nv + c] == d) return false;
+  if (t.val[c] >= TM_MAXVAL || t.val[d] >= TM_MAXVAL) return false;
+  return true;
+}
+
+// ---- vertex properties from an explicit ring ------------------------------
+struct Ring {
+  int n;
+  int r[TM_MAXVAL + 1];
+  bool f[TM_MAXVAL + 1];  // face (v, r_m, r_{m-1}) exists
+};
+
+__device__ void load_ring(const TopoW& t, int v, Ring& R) {
+  R.n = t.val[v];
+  for (int m = 0; m < R.n; ++m) {
+    int4 s = t.slot[(size_t)m * t.nv + v];
+    R.r[m] = s.x;
+    R.f[m] = s.y != -1;
+  }
+}
+__device__ void ring_remove(Ring& R, int x) {
+  int p = 0;
+  while (p < R.n && R.r[p] != x) ++p;
+  for (int m = p; m + 1 < R.n; ++m) {
+    R.r[m] = R.r[m + 1];
+    R.f[m] = R.f[m + 1];
+  }
+  if (p < R.n) R.n -= 1;
+}
+// insert y right before x
+__device__ void ring_insert_before(Ring& R, int x, int y) {
+  int p = 0;
+  while (p < R.n && R.r[p] != x) ++p;
+  for (int m = R.n; m > p; --m) {
+    R.r[m] = R.r[m - 1];
+    R.f[m] = R.f[m - 1];
+  }
+  R.r[p] = y;
+  R.f[p] = true;
+  R.n += 1;
+}
+
+// rings after the virtual flip of the quad
+__device__ void ring_after(const TopoW& t, const Quad& q, int v, Ring& R) {
+  load_ring(t, v, R);
+  if (v == q.va0) ring_remove(R, q.vb0);
+  else if (v == q.vb0) ring_remove(R, q.va0);
+  else if (v == q.va1) ring_insert_before(R, q.vb0, q.vb1);
+  else if (v == q.vb1) ring_insert_before(R, q.va0, q.va1);
+}
+
+struct OverlayExcl {  // exclusion on the topology after the virtual flip
+  const TopoW& t;
+  const Quad& q;
+  int excl;
+  __device__ bool adjacent_after(int a, int b) const {
+    if ((a == q.va0 && b == q.vb0) || (a == q.vb0 && b == q.va0)) return false;
+    if ((a == q.va1 && b == q.vb1) || (a == q.vb1 && b == q.va1)) return true;
+    int d = t.val[a];
+    for (int m = 0; m < d; ++m)
+      if (t.nbr[(size_t)m * t.nv + a] == b) return true;
+    return false;
+  }
+  __device__ bool operator()(int v, int j) const {
+    Ring R;
+    ring_after(t, q, v, R);
+    for (int m = 0; m < R.n; ++m) {
+      int w = R.r[m];
+      if (w == j) return true;
+      if (excl > 1 && adjacent_after(w, j)) return true;
+    }
+    return false;
+  }
+};
+struct TableExclW {
+  const TopoW& t;
+  int excl;
+  __device__ bool operator()(int v, int j) const {
+    int d = t.val[v];
+    for (int m = 0; m < d; ++m) {
+      int w = t.nbr[(size_t)m * t.nv + v];
+      if (w == j) return true;
+      if (excl > 1) {
+        int dw = t.val[w];
+        for (int q = 0; q < dw; ++q)
+          if (t.nbr[(size_t)q * t.nv + w] == j) return true;
+      }
+    }
+    return false;
+  }
+};
+
+// vertex_properties (src/mesh_properties.cpp:12-49) over an explicit ring
+template <class X>
+__device__ void vprops_ring(const Ring& R, int v, const double* P, const EP& ep, const NLView& nl, const X& excl,
+                            double* out) {
+  d3 xv = ld3(P, v);
+  double A = 0, V = 0, C = 0, T = 0;
+  int n = R.n;
+  for (int m = 0; m < n; ++m) {
+    if (!R.f[m]) continue;
+    int j = R.r[m], k = R.r[m == 0 ? n - 1 : m - 1];
+    int mn = m + 1 == n ? 0 : m + 1;
+    d3 xj = ld3(P, j), xk = ld3(P, k);
+    d3 ev = xj - xv;
+    double el = norm(ev);
+    d3 N0 = cross(ev, xk - xv);
+    double fa = norm(N0) / 2;
+    double th = 0.0;
+    if (R.f[mn]) {
+      d3 xn = ld3(P, R.r[mn]);
+      d3 N1 = cross(xn - xv, ev);
+      double den = norm(N0) * norm(N1);
+      if (den != 0.0) {
+        double c = fmin(1.0, fmax(-1.0, dot(N0, N1) / den));
+        double a = acos(c);
+        th = dot(cross(N0, N1), ev) >= 0.0 ? a : -a;
+      }
+    }
+    C += 0.5 * el * th;
+    A += fa;
+    V += dot(cross(xj, xk), xv) / 6;
+    if (ep.btype == 0) {
+      int r = ep.r;
+      if (el > ep.lc0)
+        T += ipow((double)r, r + 1) * ipow(el - ep.lc0, r);
+      else if (el < ep.lc1)
+        T += exp(el / (el - ep.lc1)) / ipow(el, r);
+    } else {
+      double q = fa / ep.a0 - 1.0;
+      T += q * q;
+    }
+  }
+  A /= 3;
+  V /= 3;
+  C /= 2;
+  T /= ep.tdiv;
+  out[0] = A;
+  out[1] = V;
+  out[2] = C;
+  out[3] = 2 * C * C / A;
+  out[4] = T;
+  double pot = 0.0;
+  const double lc1 = ep.rlc1;
+  const int rr = ep.rr;
+  for_each_neighbour_x(nl, P, v, xv, lc1, excl, [&](int, double l, d3) { pot += exp(l / (l - lc1)) / ipow(l, rr); });
+  out[5] = pot;
+}
+
+// ---- window kernels --------------------------------------------------------
+__global__ void k_flip_init(EP ep, const Globals* g, FlipState* st) {
+  if (threadIdx.x || blockIdx.x) return;
+  for (int k = 0; k < 6; ++k) st->props[k] = g->props[k];
+  st->e0 = energy_of(ep, st->props);
+  st->acc = 0;
+  st->npend = 0;
+  st->status = 0;
+}
+
+__global__ void k_fill(int W, long long next_new, const long long* pend, const FlipState* st, long long* win,
+                       int* limit) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) *limit = W;
+  if (s >= W) return;
+  int np = st->npend;
+  win[s] = s < np ? pend[s] : next_new + (s - np);
+}
+
+__global__ void k_claim(TopoW t, int W, unsigned long long seed, const long long* win, int* owner) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= W) return;
+  Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
+  for_patch(t, q, [&](int x) { atomicMin(&owner[x], s); });
+}
+
+__global__ void k_winner(TopoW t, int W, int mode, unsigned long long seed, const long long* win, const int* owner,
+                         unsigned char* winner, int* limit) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= W) return;
+  Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
+  bool ok = true;
+  for_patch(t, q, [&](int x) { ok = ok && (owner[x] == s); });
+  winner[s] = ok ? 1 : 0;
+  if (!ok && mode == 0) atomicMin(limit, s);
+}
+
+__global__ void k_release(TopoW t, int W, unsigned long long seed, const long long* win, int* owner) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= W) return;
+  Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
+  for_patch(t, q, [&](int x) { owner[x] = INT_MAX; });
+}
+
+// 8 threads per slot: (quad vertex 0..3) x (before, after)
+__global__ void k_delta(TopoW t, int W, unsigned long long seed, const long long* win, const unsigned char* winner,
+                        const int* limit, const double* P, EP ep, NLView nl, double* part, unsigned char* okf) {
+  int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = tid >> 3, sub = tid & 7;
+  if (s >= W) return;
+  double* o = part + 8 * 8 * (size_t)s + 8 * sub;
+  if (s >= *limit || !winner[s]) {
+    if (sub == 0) okf[s] = 0;
+    return;
+  }
+  int e = flip_edge_of(seed, win[s], t.ne);
+  bool ok = flip_ok(t, e);
+  if (sub == 0) okf[s] = ok ? 1 : 0;
+  if (!ok) return;
+  Quad q = quad_of(t, e);
+  int vs[4] = {q.va0, q.va1, q.vb0, q.vb1};
+  int v = vs[sub & 3];
+  Ring R;
+  if (sub < 4) {
+    load_ring(t, v, R);
+    TableExclW x{t, nl.excl};
+    vprops_ring(R, v, P, ep, nl, x, o);
+  } else {
+    ring_after(t, q, v, R);
+    OverlayExcl x{t, q, nl.excl};
+    vprops_ring(R, v, P, ep, nl, x, o);
+  }
+}
+
+__global__ void k_metro(int W, unsigned long long seed, const long long* win, const unsigned char* winner,
+                        const unsigned char* okf, const double* part, EP ep, FlipState* st, const int* limit,
+                        unsigned char* accepted, long long* pend) {
+  if (threadIdx.x || blockIdx.x) return;
+  int lim = *limit;
+  double props[6];
+  for (int k = 0; k < 6; ++k) props[k] = st->props[k];
+  double e0 = st->e0;
+  int acc = st->acc;
+  int np = 0;
+  for (int s = 0; s < W; ++s) {
+    accepted[s] = 0;
+    if (s >= lim || !winner[s]) {
+      pend[np++] = win[s];
+      continue;
+    }
+    if (!okf[s]) continue;
+    const double* o = part + 64 * (size_t)s;
+    double dp[6];
+    for (int k = 0; k < 6; ++k) {
+      double before = ((o[k] + o[8 + k]) + o[16 + k]) + o[24 + k];
+      // summation orders of edge_vertex_properties before (va0, va1, vb0,
+      // vb1) and after the flip (va1, vb0, vb1, va0)
+      double after = ((o[40 + k] + o[48 + k]) + o[56 + k]) + o[32 + k];
+      dp[k] = before - after;
+      props[k] -= dp[k];
+    }
+    double en = energy_of(ep, props);
+    double de = en - e0;
+    double alpha = de < 0.0 ? 1.0 : exp(-de);
+    if (flip_u_of(seed, win[s]) <= alpha) {
+      e0 = en;
+      acc += 1;
+      accepted[s] = 1;
+    } else {
+      for (int k = 0; k < 6; ++k) props[k] += dp[k];
+    }
+  }
+  for (int k = 0; k < 6; ++k) st->props[k] = props[k];
+  st->e0 = e0;
+  st->acc = acc;
+  st->npend = np;
+}
+
+__global__ void k_commit(TopoW t, int W, unsigned long long seed, const long long* win, const unsigned char* accepted,
+                         FlipState* st) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= W || !accepted[s]) return;
+  int e = flip_edge_of(seed, win[s], t.ne);
+  int a0 = 2 * e, b0 = 2 * e + 1;
+  int a1 = t.next[a0], a2 = t.next[a1], b1 = t.next[b0], b2 = t.next[b1];
+  int va0 = t.to[a0], va1 = t.to[a1], vb0 = t.to[b0], vb1 = t.to[b1];
+  int fa = t.face[a0], fb = t.face[b0];
+  t.to[a0] = va1;
+  t.to[b0] = vb1;
+  t.next[a0] = a2;
+  t.next[a2] = b1;
+  t.next[b1] = a0;
+  t.next[b0] = b2;
+  t.next[b2] = a1;
+  t.next[a1] = b0;
+  t.face[a1] = fb;
+  t.face[b1] = fa;
+  t.fhe[fa] = a0;
+  t.fhe[fb] = b0;
+  if (t.vout[va0] == b0) t.vout[va0] = a1;
+  if (t.vout[vb0] == a0) t.vout[vb0] = b1;
+  face_row(t, fa);
+  face_row(t, fb);
+  edge_row(t, e);
+  edge_row(t, a1 >> 1);
+  edge_row(t, a2 >> 1);
+  edge_row(t, b1 >> 1);
+  edge_row(t, b2 >> 1);
+  bool ok = ring_row(t, va0) & ring_row(t, va1) & ring_row(t, vb0) & ring_row(t, vb1);
+  if (!ok) atomicExch(&st->status, TM_ERR_TOPOLOGY);
+}
+
+__global__ void k_owner_init(int* owner, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) owner[i] = INT_MAX;
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+}  // namespace tmg
+
+static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, uint64_t seed, int mode, int batch,
+                      cudaStream_t s) {
+  if (mode != 0 && mode != 1) fail(TM_ERR_ARG, "mode must be 0 (serial order) or 1 (batched)");
+  if (mode == 1 && ratio > 1.0) fail(TM_ERR_RANGE, "flip_ratio must be <= 1.0");
+  if (batch < 1 || batch > MAXB) fail(TM_ERR_ARG, "batch must be in [1, 4096]");
+  int ne = m->ne;
+  long long nflips = (long long)(ne * ratio);
+  if (ne == 0 || nflips <= 0) return 0;
+  energy_eval(e, m, P, false, false, nullptr, s);
+  EP ep = make_ep(e);
+  TopoW t = m->topo_w();
+  DevBuf<int> owner;
+  DevBuf<long long> win, pend;
+  DevBuf<unsigned char> winner, okf, acc;
+  DevBuf<double> part;
+  DevBuf<FlipState> st;
+  DevBuf<int> limit;
+  owner.ensure(ne);
+  win.ensure(MAXB);
+  pend.ensure(MAXB);
+  winner.ensure(MAXB);
+  okf.ensure(MAXB);
+  acc.ensure(MAXB);
+  part.ensure(64 * (size_t)MAXB);
+  st.ensure(1);
+  limit.ensure(1);
+  k_owner_init<<<nblk(ne, 256), 256, 0, s>>>(owner.get(), ne);
+  TM_LAUNCH();
+  k_flip_init<<<1, 1, 0, s>>>(ep, e->glob.get(), st.get());
+  TM_LAUNCH();
+  FlipState hs;
+  hs.npend = 0;
+  long long next_new = 0;
+  int B = batch;
+  while (hs.npend > 0 || next_new < nflips) {
+    int W = (int)std::min<long long>(B, hs.npend + (nflips - next_new));
+    k_fill<<<nblk(W, 256), 256, 0, s>>>(W, next_new, pend.get(), st.get(), win.get(), limit.get());
+    TM_LAUNCH();
+    next_new += W - hs.npend;
+    k_claim<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), owner.get());
+    TM_LAUNCH();
+    k_winner<<<nblk(W, 128), 128, 0, s>>>(t, W, mode, seed, win.get(), owner.get(), winner.get(), limit.get());
+    TM_LAUNCH();
+    k_release<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), owner.get());
+    TM_LAUNCH();
+    k_delta<<<nblk(8L * W, 64), 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, e->nl.view,
+                                          part.get(), okf.get());
+    TM_LAUNCH();
+    k_metro<<<1, 1, 0, s>>>(W, seed, win.get(), winner.get(), okf.get(), part.get(), ep, st.get(), limit.get(),
+                            acc.get(), pend.get());
+    TM_LAUNCH();
+    k_commit<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), acc.get(), st.get());
+    TM_LAUNCH();
+    TM_CUDA(cudaMemcpyAsync(&hs, st.get(), sizeof(FlipState), cudaMemcpyDeviceToHost, s));
+    TM_CUDA(cudaStreamSynchronize(s));
+    if (hs.status) fail(TM_ERR_TOPOLOGY, "flip produced a valence above TM_MAXVAL");
+    // slot 0 of a window always owns its patch, so every window decides at
+    // least one proposal and the loop ends
+  }
+  m->host_topo_stale = true;
+  return hs.acc;
+}
+
+extern "C" int tm_flip(tm_mesh* m, tm_energy* e, double ratio, uint64_t seed, int mode, int batch,
+                       int32_t* accepted) {
+  TM_API_BEGIN
+  if (!m || !e || !accepted) fail(TM_ERR_ARG, "NULL argument");
+  *accepted = 0;
+  m->upload_points(e->stream);
+  *accepted = flip_sweep(m, e, m->d_pts.get(), ratio, seed, mode, batch, e->stream);
+  TM_API_END
+}
+
+extern "C" int tm_flip_device(tm_mesh* m, tm_energy* e, const double* d_points, double ratio, uint64_t seed,
+                              int mode, int batch, int32_t* accepted, void* stream) {
+  TM_API_BEGIN
+  if (!m || !e || !d_points || !accepted) fail(TM_ERR_ARG, "NULL argument");
+  *accepted = 0;
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  *accepted = flip_sweep(m, e, d_points, ratio, seed, mode, batch, s);
+  TM_API_END
+}

@@ -1,0 +1,556 @@
+// Neighbour lists: cell list and Verlet list (src/nlists/cell_list.h,
+// verlet_list.h, nlist.cpp).
+//
+// Cell list build (every rebuild, all on the device except the box):
+//   1. bounding box by a fixed-order min/max reduction, with the reference's
+//      initial values {DBL_MAX,0,0} / {-1,0,0} (cell_list.h:46-47), copied
+//      to the host, which derives r_list/shape/strides exactly like
+//      cell_list.h:56-65
+//   2. cell id per vertex with C truncation (cell_list.h:71-78), inserted
+//      into an open-addressing hash table of the non-empty cells
+//      (2x the vertex count, power of two) -> per-cell counts
+//   3. exclusive scan of the counts -> cell start offsets
+//   4. scatter of the vertex ids, then each cell sorted by vertex id, so a
+//      cell lists its vertices in ascending order like the reference's
+//      std::map<int, std::vector<int>>
+// Queries bin the query point with its CURRENT position but look up the
+// cells' build-time members, as the reference does (cell_list.h:131-219).
+// Distances are rounded operation by operation (no FMA), so pair sets match
+// the sequential CPU code bit for bit.
+// The Verlet list is a CSR built from the cell list with cut-off rlist
+// (verlet_list.h:18-35); its queries apply `< dmax`.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+#include "tm_internal.h"
+#include "tm_math.cuh"
+
+using namespace tmg;
+
+#define TM_API_BEGIN try {
+#define TM_API_END                  \
+  }                                 \
+  catch (const tmg::Error& e) {     \
+    tmg::set_last_error(e.what());  \
+    return e.code;                  \
+  }                                 \
+  catch (const std::exception& e) { \
+    tmg::set_last_error(e.what());  \
+    return TM_ERR_ARG;              \
+  }                                 \
+  return TM_OK;
+
+namespace tmg {
+
+__device__ __forceinline__ unsigned long long cell_hash2(long long key) {
+  unsigned long long z = (unsigned long long)key + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ int cell_lookup(const NLView& nl, long long key, int* start) {
+  unsigned long long h = cell_hash2(key) & nl.tmask;
+  for (unsigned long long p = 0; p <= nl.tmask; ++p) {
+    CellEntry c = nl.table[h];
+    if (c.key == key) {
+      *start = c.start;
+      return c.count;
+    }
+    if (c.key == -1) return 0;
+    h = (h + 1) & nl.tmask;
+  }
+  return 0;
+}
+
+__device__ bool nl_excluded(const Topo& t, int excl, int v, int j) {
+  if (excl <= 0) return false;
+  int d = t.val[v];
+  for (int m = 0; m < d; ++m) {
+    int w = t.nbr[(size_t)m * t.nv + v];
+    if (w == j) return true;
+    if (excl > 1) {
+      int dw = t.val[w];
+      for (int q = 0; q < dw; ++q)
+        if (t.nbr[(size_t)q * t.nv + w] == j) return true;
+    }
+  }
+  return false;
+}
+
+namespace {
+
+constexpr int BB = 256;
+
+__global__ void k_bbox(int nv, const double* P, double* part) {
+  __shared__ double s[6][BB];
+  double lo[3] = {DBL_MAX, 0.0, 0.0}, hi[3] = {-1.0, 0.0, 0.0};
+  for (int i = blockIdx.x * BB + threadIdx.x; i < nv; i += gridDim.x * BB)
+    for (int k = 0; k < 3; ++k) {
+      double x = P[3 * i + k];
+      if (x < lo[k]) lo[k] = x;
+      if (x > hi[k]) hi[k] = x;
+    }
+  for (int k = 0; k < 3; ++k) {
+    s[k][threadIdx.x] = lo[k];
+    s[3 + k][threadIdx.x] = hi[k];
+  }
+  __syncthreads();
+  for (int o = BB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 3; ++k) {
+        double a = s[k][threadIdx.x + o];
+        if (a < s[k][threadIdx.x]) s[k][threadIdx.x] = a;
+        double b = s[3 + k][threadIdx.x + o];
+        if (b > s[3 + k][threadIdx.x]) s[3 + k][threadIdx.x] = b;
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) part[6 * blockIdx.x + k] = s[k][0];
+}
+
+__global__ void k_bbox_final(int nb, const double* part, double* out) {
+  if (threadIdx.x || blockIdx.x) return;
+  double lo[3] = {DBL_MAX, 0.0, 0.0}, hi[3] = {-1.0, 0.0, 0.0};
+  for (int b = 0; b < nb; ++b)
+    for (int k = 0; k < 3; ++k) {
+      double a = part[6 * b + k], c = part[6 * b + 3 + k];
+      if (a < lo[k]) lo[k] = a;
+      if (c > hi[k]) hi[k] = c;
+    }
+  for (int k = 0; k < 3; ++k) {
+    out[k] = lo[k];
+    out[3 + k] = hi[k];
+  }
+}
+
+__global__ void k_table_init(CellEntry* T, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) {
+    T[i].key = -1;
+    T[i].start = 0;
+    T[i].count = 0;
+  }
+}
+
+__global__ void k_cell_insert(int nv, const double* P, NLView nl, CellEntry* T, long long* vcid, int* vcoord,
+                              int* vslot, int* status) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  long long id = 0;
+  for (int k = 0; k < 3; ++k) {
+    int c = (int)__ddiv_rn(__dsub_rn(P[3 * v + k], nl.bmin[k]), nl.rl[k]);
+    vcoord[3 * v + k] = c;
+    id += (long long)c * nl.stride[k];
+  }
+  vcid[v] = id;
+  unsigned long long h = cell_hash2(id) & nl.tmask;
+  int slot = -1;
+  for (unsigned long long p = 0; p <= nl.tmask; ++p) {
+    unsigned long long prev =
+        atomicCAS(reinterpret_cast<unsigned long long*>(&T[h].key), (unsigned long long)(-1LL), (unsigned long long)id);
+    if (prev == (unsigned long long)(-1LL) || prev == (unsigned long long)id) {
+      slot = (int)h;
+      break;
+    }
+    h = (h + 1) & nl.tmask;
+  }
+  if (slot < 0) {
+    atomicExch(status, 1);
+    vslot[v] = 0;
+    return;
+  }
+  vslot[v] = slot;
+  atomicAdd(&T[slot].count, 1);
+}
+
+__global__ void k_counts(const CellEntry* T, int n, int* cnt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cnt[i] = T[i].count;
+}
+__global__ void k_set_start(CellEntry* T, int n, const int* start) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) T[i].start = start[i];
+}
+__global__ void k_scatter(int nv, const int* vslot, const CellEntry* T, int* fill, int* cell_verts) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  int s = vslot[v];
+  int pos = T[s].start + atomicAdd(&fill[s], 1);
+  cell_verts[pos] = v;
+}
+__global__ void k_sort_cells(const CellEntry* T, int n, int* cell_verts) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = T[i].count;
+  if (c < 2) return;
+  int* a = cell_verts + T[i].start;
+  for (int x = 1; x < c; ++x) {
+    int key = a[x];
+    int y = x - 1;
+    while (y >= 0 && a[y] > key) {
+      a[y + 1] = a[y];
+      --y;
+    }
+    a[y + 1] = key;
+  }
+}
+
+// Pairs of the build-time cell neighbourhood of vertex a:
+//   mode 0: Verlet build, all b != a, d <= rd        (both orders)
+//   mode 1: distance_matrix of the cell list, each pair once with
+//           (cid_b > cid_a) or (same cell and b > a), d <= rd
+// pass 0 counts, pass 1 writes (d, i, j) at row offsets.
+__global__ void k_cell_pairs(int nv, const double* P, NLView nl, Topo t, const int* vcoord, const long long* vcid,
+                             double rd, int mode, int pass, int* cnt, const int* off, double* od, int* oi, int* oj) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nv) return;
+  d3 pa = ld3(P, a);
+  long long ca = vcid[a];
+  int n = 0;
+  int base = pass ? off[a] : 0;
+  for (int x = -1; x < 2; ++x) {
+    int ii = vcoord[3 * a] + x;
+    if (ii < 0 || ii >= nl.shape[0]) continue;
+    for (int y = -1; y < 2; ++y) {
+      int jj = vcoord[3 * a + 1] + y;
+      if (jj < 0 || jj >= nl.shape[1]) continue;
+      for (int z = -1; z < 2; ++z) {
+        int kk = vcoord[3 * a + 2] + z;
+        if (kk < 0 || kk >= nl.shape[2]) continue;
+        long long cid = ii * nl.stride[0] + jj * nl.stride[1] + kk * nl.stride[2];
+        if (mode == 1 && cid < ca) continue;
+        int st = 0;
+        int cnt_c = cell_lookup(nl, cid, &st);
+        for (int q = 0; q < cnt_c; ++q) {
+          int b = nl.cell_verts[st + q];
+          if (b == a) continue;
+          if (mode == 1 && cid == ca && b < a) continue;
+          double dd = exact_dist(pa, ld3(P, b));
+          if (!(dd <= rd)) continue;
+          if (nl_excluded(t, nl.excl, a, b)) continue;
+          if (pass) {
+            od[base + n] = dd;
+            if (mode == 0) {
+              oj[base + n] = b;
+            } else {
+              oi[base + n] = a < b ? a : b;
+              oj[base + n] = a < b ? b : a;
+            }
+          }
+          ++n;
+        }
+      }
+    }
+  }
+  if (!pass) cnt[a] = n;
+}
+
+// distance_matrix of the Verlet list: rows in vertex order, d < rd
+__global__ void k_verlet_dm(int nv, const double* P, const int* vrow, const int* vcol, double rd, int pass, int* cnt,
+                            const int* off, double* od, int* oi, int* oj) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nv) return;
+  d3 pa = ld3(P, a);
+  int n = 0;
+  int base = pass ? off[a] : 0;
+  for (int q = vrow[a]; q < vrow[a + 1]; ++q) {
+    int b = vcol[q];
+    double dd = exact_dist(pa, ld3(P, b));
+    if (dd < rd) {
+      if (pass) {
+        od[base + n] = dd;
+        oi[base + n] = a;
+        oj[base + n] = b;
+      }
+      ++n;
+    }
+  }
+  if (!pass) cnt[a] = n;
+}
+
+// point_distances for one vertex (single thread; API use only)
+__global__ void k_point(int pid, const double* P, NLView nl, Topo t, double rd, int pass, int* count, double* od,
+                        int* oj) {
+  if (threadIdx.x || blockIdx.x) return;
+  d3 p = ld3(P, pid);
+  int n = 0;
+  if (nl.kind == 0) {
+    int co[3];
+    const double* pp = &p.x;
+    for (int k = 0; k < 3; ++k) co[k] = (int)__ddiv_rn(__dsub_rn(pp[k], nl.bmin[k]), nl.rl[k]);
+    for (int a = -1; a < 2; ++a) {
+      int ii = co[0] + a;
+      if (ii < 0 || ii >= nl.shape[0]) continue;
+      for (int b = -1; b < 2; ++b) {
+        int jj = co[1] + b;
+        if (jj < 0 || jj >= nl.shape[1]) continue;
+        for (int c = -1; c < 2; ++c) {
+          int kk = co[2] + c;
+          if (kk < 0 || kk >= nl.shape[2]) continue;
+          long long cid = ii * nl.stride[0] + jj * nl.stride[1] + kk * nl.stride[2];
+          int st = 0;
+          int cc = cell_lookup(nl, cid, &st);
+          for (int q = 0; q < cc; ++q) {
+            int j = nl.cell_verts[st + q];
+            if (j == pid) continue;
+            if (nl_excluded(t, nl.excl, pid, j)) continue;
+            d3 pj = ld3(P, j);
+            if (exact_dist(p, pj) < rd) {
+              if (pass) {
+                st3(od, n, exact_diff(p, pj));
+                oj[n] = j;
+              }
+              ++n;
+            }
+          }
+        }
+      }
+    }
+  } else {
+    for (int q = nl.vrow[pid]; q < nl.vrow[pid + 1]; ++q) {
+      int j = nl.vcol[q];
+      d3 pj = ld3(P, j);
+      if (exact_dist(p, pj) < rd) {
+        if (pass) {
+          st3(od, n, exact_diff(p, pj));
+          oj[n] = j;
+        }
+        ++n;
+      }
+    }
+  }
+  if (!pass) *count = n;
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, cudaStream_t s) {
+  if (p.n_search != 0 && p.n_search != 1) fail(TM_ERR_ARG, "Unknown neighbour search algorithm.");
+  if (p.exclusion_level < 0 || p.exclusion_level > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
+  nl->prm = p;
+  int nv = m->nv;
+  nl->nv = nv;
+  NLView& V = nl->view;
+  V = NLView{};
+  V.kind = 0;
+  V.excl = p.exclusion_level;
+  // 1. box
+  int nb = std::max(1, std::min(1024, nblk(nv, BB)));
+  nl->bbox.ensure(6 * (size_t)nb + 6);
+  double box[6] = {DBL_MAX, 0, 0, -1, 0, 0};
+  if (nv > 0) {
+    k_bbox<<<nb, BB, 0, s>>>(nv, P, nl->bbox.get());
+    TM_LAUNCH();
+    k_bbox_final<<<1, 1, 0, s>>>(nb, nl->bbox.get(), nl->bbox.get() + 6 * nb);
+    TM_LAUNCH();
+    TM_CUDA(cudaMemcpyAsync(box, nl->bbox.get() + 6 * nb, sizeof(box), cudaMemcpyDeviceToHost, s));
+    TM_CUDA(cudaStreamSynchronize(s));
+  }
+  const double rlist = p.rlist, box_eps = 1.0e-6;
+  int shape[3];
+  for (int k = 0; k < 3; ++k) {
+    double dim = box[3 + k] - box[k] + box_eps;
+    int nk = int(dim / rlist);
+    V.rl[k] = nk > 0 ? dim / nk : dim;
+    shape[k] = nk > 0 ? nk : 1;
+    V.bmin[k] = box[k];
+    V.shape[k] = shape[k];
+  }
+  V.stride[0] = 1;
+  V.stride[1] = shape[0];
+  V.stride[2] = (long long)shape[0] * shape[1];
+  // 2. hash table of non-empty cells
+  size_t tsize = 64;
+  while (tsize < 2 * (size_t)std::max(nv, 1)) tsize <<= 1;
+  nl->table.ensure(tsize);
+  V.tmask = tsize - 1;
+  nl->vcid.ensure(std::max(nv, 1));
+  nl->vcoord.ensure(3 * (size_t)std::max(nv, 1));
+  nl->vslot.ensure(std::max(nv, 1));
+  nl->cnt.ensure(tsize + 1);
+  nl->fill.ensure(tsize);
+  nl->cell_verts.ensure(std::max(nv, 1));
+  nl->d_count.ensure(4);
+  k_table_init<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), tsize);
+  TM_LAUNCH();
+  TM_CUDA(cudaMemsetAsync(nl->d_count.get(), 0, sizeof(int), s));
+  V.table = nl->table.get();
+  V.cell_verts = nl->cell_verts.get();
+  if (nv > 0) {
+    k_cell_insert<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, nl->table.get(), nl->vcid.get(), nl->vcoord.get(),
+                                                nl->vslot.get(), nl->d_count.get());
+    TM_LAUNCH();
+    // 3. offsets
+    k_counts<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), (int)tsize, nl->cnt.get());
+    TM_LAUNCH();
+    exclusive_scan_int(nl->cnt.get(), nl->fill.get(), (int)tsize, nullptr, nl->tmp, s);
+    k_set_start<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), (int)tsize, nl->fill.get());
+    TM_LAUNCH();
+    // 4. scatter + per-cell sort
+    TM_CUDA(cudaMemsetAsync(nl->fill.get(), 0, sizeof(int) * tsize, s));
+    k_scatter<<<nblk(nv, 256), 256, 0, s>>>(nv, nl->vslot.get(), nl->table.get(), nl->fill.get(),
+                                            nl->cell_verts.get());
+    TM_LAUNCH();
+    k_sort_cells<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), (int)tsize, nl->cell_verts.get());
+    TM_LAUNCH();
+    int st = 0;
+    TM_CUDA(cudaMemcpyAsync(&st, nl->d_count.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+    TM_CUDA(cudaStreamSynchronize(s));
+    if (st) fail(TM_ERR_DEVICE, "cell table overflow");
+  }
+  if (p.n_search == 1) {
+    // Verlet CSR from the cell list at cut-off rlist
+    nl->vrow.ensure((size_t)nv + 1);
+    nl->tmp.ensure(4);
+    Topo t = m->topo();
+    int total = 0;
+    if (nv > 0) {
+      nl->cnt.ensure((size_t)nv + 1);
+      k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), nl->vcid.get(), rlist, 0, 0,
+                                                 nl->cnt.get(), nullptr, nullptr, nullptr, nullptr);
+      TM_LAUNCH();
+      TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
+      exclusive_scan_int(nl->cnt.get(), nl->vrow.get(), nv + 1, &total, nl->tmp, s);
+      nl->vcol.ensure(std::max(total, 1));
+      nl->d_res.ensure(std::max(total, 1));
+      k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), nl->vcid.get(), rlist, 0, 1,
+                                                 nullptr, nl->vrow.get(), nl->d_res.get(), nullptr, nl->vcol.get());
+      TM_LAUNCH();
+    } else {
+      TM_CUDA(cudaMemsetAsync(nl->vrow.get(), 0, sizeof(int), s));
+      nl->vcol.ensure(1);
+    }
+    V.kind = 1;
+    V.vrow = nl->vrow.get();
+    V.vcol = nl->vcol.get();
+  }
+}
+
+int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* P, double rd, cudaStream_t s) {
+  int nv = m->nv;
+  nl->res_d.clear();
+  nl->res_i.clear();
+  nl->res_j.clear();
+  if (nv == 0) return 0;
+  if (nv != nl->nv) fail(TM_ERR_ARG, "mesh does not match the neighbour list");
+  nl->cnt.ensure((size_t)nv + 1);
+  nl->fill.ensure((size_t)nv + 1);
+  Topo t = m->topo();
+  int total = 0;
+  if (nl->view.kind == 0)
+    k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->view, t, nl->vcoord.get(), nl->vcid.get(), rd, 1, 0,
+                                               nl->cnt.get(), nullptr, nullptr, nullptr, nullptr);
+  else
+    k_verlet_dm<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->vrow.get(), nl->vcol.get(), rd, 0, nl->cnt.get(), nullptr,
+                                              nullptr, nullptr, nullptr);
+  TM_LAUNCH();
+  TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
+  exclusive_scan_int(nl->cnt.get(), nl->fill.get(), nv + 1, &total, nl->tmp, s);
+  nl->d_res.ensure(std::max(total, 1));
+  nl->d_resi.ensure(std::max(total, 1));
+  nl->d_resj.ensure(std::max(total, 1));
+  if (nl->view.kind == 0)
+    k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->view, t, nl->vcoord.get(), nl->vcid.get(), rd, 1, 1,
+                                               nullptr, nl->fill.get(), nl->d_res.get(), nl->d_resi.get(),
+                                               nl->d_resj.get());
+  else
+    k_verlet_dm<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->vrow.get(), nl->vcol.get(), rd, 1, nullptr, nl->fill.get(),
+                                              nl->d_res.get(), nl->d_resi.get(), nl->d_resj.get());
+  TM_LAUNCH();
+  nl->res_d.resize(total);
+  nl->res_i.resize(total);
+  nl->res_j.resize(total);
+  if (total) {
+    TM_CUDA(cudaMemcpyAsync(nl->res_d.data(), nl->d_res.get(), sizeof(double) * total, cudaMemcpyDeviceToHost, s));
+    TM_CUDA(cudaMemcpyAsync(nl->res_i.data(), nl->d_resi.get(), sizeof(int) * total, cudaMemcpyDeviceToHost, s));
+    TM_CUDA(cudaMemcpyAsync(nl->res_j.data(), nl->d_resj.get(), sizeof(int) * total, cudaMemcpyDeviceToHost, s));
+  }
+  TM_CUDA(cudaStreamSynchronize(s));
+  return total;
+}
+
+int64_t nlist_point_distances(tm_nlist* nl, tm_mesh* m, const double* P, int pid, double rd, cudaStream_t s) {
+  nl->res_d.clear();
+  nl->res_i.clear();
+  nl->res_j.clear();
+  if (pid < 0 || pid >= m->nv) fail(TM_ERR_ARG, "pid out of range");
+  if (m->nv != nl->nv) fail(TM_ERR_ARG, "mesh does not match the neighbour list");
+  Topo t = m->topo();
+  nl->d_count.ensure(4);
+  k_point<<<1, 1, 0, s>>>(pid, P, nl->view, t, rd, 0, nl->d_count.get(), nullptr, nullptr);
+  TM_LAUNCH();
+  int n = 0;
+  TM_CUDA(cudaMemcpyAsync(&n, nl->d_count.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  TM_CUDA(cudaStreamSynchronize(s));
+  nl->d_res.ensure(3 * (size_t)std::max(n, 1));
+  nl->d_resj.ensure(std::max(n, 1));
+  k_point<<<1, 1, 0, s>>>(pid, P, nl->view, t, rd, 1, nullptr, nl->d_res.get(), nl->d_resj.get());
+  TM_LAUNCH();
+  nl->res_d.resize(3 * (size_t)n);
+  nl->res_j.resize(n);
+  if (n) {
+    TM_CUDA(cudaMemcpyAsync(nl->res_d.data(), nl->d_res.get(), sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s));
+    TM_CUDA(cudaMemcpyAsync(nl->res_j.data(), nl->d_resj.get(), sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  }
+  TM_CUDA(cudaStreamSynchronize(s));
+  return n;
+}
+
+}  // namespace tmg
+
+// --------------------------------------------------------------------------
+// C ABI
+// --------------------------------------------------------------------------
+
+
+extern "C" {
+
+int tm_nlist_create(tm_mesh* m, const tm_params* p, tm_nlist** out) {
+  TM_API_BEGIN
+  if (!m || !p || !out) fail(TM_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  std::unique_ptr<tm_nlist> nl(new tm_nlist());
+  m->upload_points(m->stream);
+  tmg::nlist_make(nl.get(), m, *p, m->d_pts.get(), m->stream);
+  TM_CUDA(cudaStreamSynchronize(m->stream));
+  *out = nl.release();
+  TM_API_END
+}
+
+int tm_nlist_destroy(tm_nlist* nl) {
+  delete nl;
+  return TM_OK;
+}
+
+int tm_nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, double rdist, int64_t* count) {
+  TM_API_BEGIN
+  if (!nl || !m || !count) fail(TM_ERR_ARG, "NULL argument");
+  m->upload_points(m->stream);
+  *count = tmg::nlist_distance_matrix(nl, m, m->d_pts.get(), rdist, m->stream);
+  TM_API_END
+}
+
+int tm_nlist_point_distances(tm_nlist* nl, tm_mesh* m, int64_t pid, double rdist, int64_t* count) {
+  TM_API_BEGIN
+  if (!nl || !m || !count) fail(TM_ERR_ARG, "NULL argument");
+  m->upload_points(m->stream);
+  *count = tmg::nlist_point_distances(nl, m, m->d_pts.get(), (int)pid, rdist, m->stream);
+  TM_API_END
+}
+
+int tm_nlist_fetch(tm_nlist* nl, double* d, int32_t* i, int32_t* j) {
+  if (!nl) return TM_ERR_ARG;
+  if (d && !nl->res_d.empty()) std::memcpy(d, nl->res_d.data(), sizeof(double) * nl->res_d.size());
+  if (i && !nl->res_i.empty()) std::memcpy(i, nl->res_i.data(), sizeof(int) * nl->res_i.size());
+  if (j && !nl->res_j.empty()) std::memcpy(j, nl->res_j.data(), sizeof(int) * nl->res_j.size());
+  return TM_OK;
+}
+
+}  // extern "C"

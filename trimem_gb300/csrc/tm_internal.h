@@ -1,0 +1,183 @@
+// Internal declarations shared by the translation units of libtrimem_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "trimem_gpu.h"
+
+namespace tmg {
+
+// Errors travel as exceptions inside the library and become a status code
+// plus tm_last_error() text at the C ABI.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+void set_last_error(const std::string& m);
+[[noreturn]] void fail(int code, const std::string& m);
+void cuda_check(cudaError_t e, const char* what, const char* file, int line);
+#define TM_CUDA(x) ::tmg::cuda_check((x), #x, __FILE__, __LINE__)
+#define TM_LAUNCH() ::tmg::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+
+// Owning device buffer (no copy; grows on demand).
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void ensure(size_t count) {
+    if (count <= n && p) return;
+    release();
+    size_t c = count ? count : 1;
+    if (cudaMalloc(&p, c * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      fail(TM_ERR_NOMEM, "device allocation of " + std::to_string(c * sizeof(T)) + " bytes failed");
+    }
+    n = c;
+  }
+  T* get() const { return p; }
+};
+
+// One ring slot of a vertex v (slot-major tables [TM_MAXVAL][nv]):
+//   x: neighbour r_m (target of the m-th outgoing halfedge h_m)
+//   y: face of h_m in bits 0..29, corner of v in that face's stored vertex
+//      order in bits 30..31; -1 (all bits) on a boundary halfedge
+//   z: edge of h_m
+//   w: edge of next(h_m), the edge opposite v in the face
+// Slots follow the rotation h -> next(opposite(h)), so the face of slot m is
+// (v, r_m, r_{m-1}) in face orientation.
+__host__ __device__ inline int slot_face(int y) { return y == -1 ? -1 : (y & 0x3fffffff); }
+__host__ __device__ inline int slot_corner(int y) { return (int)(((unsigned)y) >> 30); }
+
+// Read-only topology view handed to kernels.
+struct Topo {
+  int nv, ne, nf;
+  const int* to;
+  const int* next;
+  const int* face;
+  const int* vout;
+  const int* fhe;
+  const int4* slot;  // [TM_MAXVAL][nv]
+  const int* nbr;    // [TM_MAXVAL][nv]
+  const int* val;    // [nv]
+  const int* fv;     // [3*nf]
+  const int4* edge;  // [ne]: from, to, face of 2e, face of 2e+1
+};
+
+// Neighbour-list view used by the repulsion penalty.
+struct CellEntry {
+  long long key;  // cell id, -1 empty
+  int start, count;
+};
+struct NLView {
+  int kind;  // 0 cell list, 1 Verlet list
+  int excl;
+  double bmin[3], rl[3];
+  int shape[3];
+  long long stride[3];
+  const CellEntry* table;
+  unsigned long long tmask;
+  const int* cell_verts;
+  const int* vrow;  // Verlet CSR
+  const int* vcol;
+};
+
+struct TopoW;
+
+}  // namespace tmg
+
+// --------------------------------------------------------------------------
+// Handles (opaque in the C ABI)
+// --------------------------------------------------------------------------
+struct tm_mesh {
+  int nv = 0, ne = 0, nf = 0;
+  bool closed = true;
+  double* h_pts = nullptr;  // page-locked host positions (points() view)
+  std::vector<int> h_to, h_next, h_face, h_vout, h_fhe;
+  bool host_topo_stale = false;
+  tmg::DevBuf<double> d_pts;
+  tmg::DevBuf<int> d_to, d_next, d_face, d_vout, d_fhe;
+  tmg::DevBuf<int4> d_slot;
+  tmg::DevBuf<int> d_nbr, d_val, d_fv;
+  tmg::DevBuf<int4> d_edge;
+  tmg::DevBuf<double> d_scratch;  // primitives / utilities
+  tmg::DevBuf<int> d_status;
+  cudaStream_t stream = nullptr;
+  tmg::Topo topo() const;
+  tmg::TopoW topo_w();
+  void rebuild_tables(cudaStream_t s);  // faces, edges, rings from halfedges
+  void upload_points(cudaStream_t s);
+  void sync_host_topology();
+  ~tm_mesh();
+};
+
+struct tm_nlist {
+  tmg::NLView view{};
+  tm_params prm{};
+  int nv = 0;
+  tmg::DevBuf<tmg::CellEntry> table;
+  tmg::DevBuf<int> cell_verts, vslot, vcoord, cnt, fill, vrow, vcol, tmp;
+  tmg::DevBuf<long long> vcid;
+  tmg::DevBuf<double> bbox;
+  // last query result
+  std::vector<double> res_d;
+  std::vector<int> res_i, res_j;
+  tmg::DevBuf<double> d_res;
+  tmg::DevBuf<int> d_resi, d_resj, d_count;
+  void build(tm_mesh* m, const double* d_points, cudaStream_t s);
+};
+
+namespace tmg {
+// device-side scalar state of an energy manager
+struct Globals {
+  double props[8];  // area, volume, curvature, bending, tethering, repulsion
+  double comps[8];  // area, volume, area-diff, bending, tether, repulsion, total
+  double gA, gV, gC;
+  unsigned int ticket;
+  int status;
+};
+}  // namespace tmg
+
+struct tm_energy {
+  tm_params prm{};
+  double initial[6] = {0, 0, 0, 0, 0, 0};
+  int stencil = 0;  // 0 FP64, 1 FP32
+  tm_nlist nl;
+  int nv = 0, ne = 0, nf = 0;
+  tmg::DevBuf<double> face, edge, ebond, rho, repg, vprops, partials, grad, work;
+  tmg::DevBuf<tmg::Globals> glob;
+  cudaStream_t stream = nullptr;
+  void ensure(int nv_, int ne_, int nf_);
+  ~tm_energy();
+};
+
+namespace tmg {
+// energy.cu
+void energy_eval(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, bool want_vprops,
+                 double* d_grad, cudaStream_t s);
+// same, recording ev[0..4] around the face, edge, vertex and gradient kernels
+void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, bool want_vprops,
+                        double* d_grad, cudaStream_t s, cudaEvent_t* ev);
+void energy_from_props_device(tm_energy* e, const double* d_props6, double* d_out8, cudaStream_t s);
+// nlist.cu
+void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* d_points, cudaStream_t s);
+int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* d_points, double rdist, cudaStream_t s);
+int64_t nlist_point_distances(tm_nlist* nl, tm_mesh* m, const double* d_points, int pid, double rdist,
+                              cudaStream_t s);
+// scan.cu helpers
+void exclusive_scan_int(const int* in, int* out, int n, int* total_host, DevBuf<int>& tmp, cudaStream_t s);
+}  // namespace tmg
