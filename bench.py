@@ -116,7 +116,7 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def cpu_baseline(p, f, prm, budget_s=20.0, max_evals=12):
+def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400):
     """Oracle (reference algorithm on the host cores, all threads)."""
     from oracle import oracle as O
 
@@ -189,7 +189,12 @@ def main():
     mesh = capi.Mesh(p, f)
     en = capi.Energy(mesh, capi.params(**prm))
     L = capi.lib()
-    stream = torch.cuda.current_stream().cuda_stream
+    # a dedicated stream: the library runs on it and the timing events are
+    # recorded on it (the NULL handle would select the library's own stream)
+    side = torch.cuda.Stream()
+    torch.cuda.set_stream(side)
+    stream = side.cuda_stream
+    assert stream != 0
     x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
     g = torch.empty_like(x)
     e_dev = torch.empty(1, dtype=torch.float64, device="cuda")

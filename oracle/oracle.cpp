@@ -954,6 +954,115 @@ static inline double flip_u_of(uint64_t seed, uint64_t p) {
   return (double)(flip_key(seed, p, 1) >> 11) * 0x1.0p-53;
 }
 
+// ---- ring form of vertex_properties used by the device flip sweep --------
+// The device evaluates the four quad vertices over explicit rings (before and
+// after a virtual flip); this restates that arithmetic operation by operation
+// (the device file is compiled without FMA contraction), so ill-conditioned
+// quads (nearly antiparallel faces, where the sign of the dihedral angle is
+// decided by rounding) are decided identically.
+struct PortRing {
+  int n = 0;
+  int r[40];
+  bool f[40];
+};
+static void port_ring_before(const Mesh& m, int v, PortRing& R) {
+  R.n = 0;
+  m.voh(v, [&](int h) {
+    R.r[R.n] = m.to[h];
+    R.f[R.n] = m.fc[h] >= 0;
+    R.n++;
+  });
+}
+static void port_ring_remove(PortRing& R, int x) {
+  int p = 0;
+  while (p < R.n && R.r[p] != x) ++p;
+  for (int k = p; k + 1 < R.n; ++k) {
+    R.r[k] = R.r[k + 1];
+    R.f[k] = R.f[k + 1];
+  }
+  if (p < R.n) R.n -= 1;
+}
+static void port_ring_insert_before(PortRing& R, int x, int y) {
+  int p = 0;
+  while (p < R.n && R.r[p] != x) ++p;
+  for (int k = R.n; k > p; --k) {
+    R.r[k] = R.r[k - 1];
+    R.f[k] = R.f[k - 1];
+  }
+  R.r[p] = y;
+  R.f[p] = true;
+  R.n += 1;
+}
+static inline double port_ipow(double x, int n) {
+  int a = n < 0 ? -n : n;
+  double r = 1.0;
+  for (int k = 0; k < a; ++k) r *= x;
+  return n < 0 ? 1.0 / r : r;
+}
+// geometry and tether part; the repulsion term is added by the caller
+static void port_ring_props(const Mesh& m, const PortRing& R, int v, const om_params& prm, double* out) {
+  const V3 xv = m.P[v];
+  double A = 0, Vv = 0, C = 0, T = 0;
+  int n = R.n;
+  double tdiv = prm.bond_type == 0 ? 2.0 : 3.0;
+  for (int k = 0; k < n; ++k) {
+    if (!R.f[k]) continue;
+    int j = R.r[k], kk = R.r[k == 0 ? n - 1 : k - 1];
+    int mn = k + 1 == n ? 0 : k + 1;
+    V3 xj = m.P[j], xk = m.P[kk];
+    V3 ev = xj - xv;
+    double el = ev.norm();
+    V3 N0 = cross(ev, xk - xv);
+    double fa = N0.norm() / 2;
+    double th = 0.0;
+    if (R.f[mn]) {
+      V3 xn = m.P[R.r[mn]];
+      V3 N1 = cross(xn - xv, ev);
+      double den = N0.norm() * N1.norm();
+      if (den != 0.0) {
+        double c = std::min(1.0, std::max(-1.0, dot(N0, N1) / den));
+        double a = std::acos(c);
+        th = dot(cross(N0, N1), ev) >= 0.0 ? a : -a;
+      }
+    }
+    C += 0.5 * el * th;
+    A += fa;
+    Vv += dot(cross(xj, xk), xv) / 6;
+    if (prm.bond_type == 0) {
+      int r = prm.bond_r;
+      if (el > prm.bond_lc0)
+        T += port_ipow((double)r, r + 1) * port_ipow(el - prm.bond_lc0, r);
+      else if (el < prm.bond_lc1)
+        T += std::exp(el / (el - prm.bond_lc1)) / port_ipow(el, r);
+    } else {
+      double q = fa / prm.bond_a0 - 1.0;
+      T += q * q;
+    }
+  }
+  A /= 3;
+  Vv /= 3;
+  C /= 2;
+  T /= tdiv;
+  out[0] = A;
+  out[1] = Vv;
+  out[2] = C;
+  out[3] = 2 * C * C / A;
+  out[4] = T;
+}
+static double port_repulsion(const Mesh& m, const Energy& E, int v) {
+  std::vector<V3> d;
+  std::vector<int> j;
+  double lc1 = E.prm.rep_lc1;
+  int rr = E.prm.rep_r;
+  E.nl->point_distances(m, v, lc1, d, j);
+  double pot = 0.0;
+  for (auto& x : d) {
+    double l = x.norm();
+    pot += std::exp(l / (l - lc1)) / port_ipow(l, rr);
+  }
+  return pot;
+}
+
 // CPU port of the device sweep (see oracle.h).
 static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, int mode, int batch) {
   if (ratio > 1.0 && mode == 1) throw std::range_error("flip_ratio must be <= 1.0");
@@ -998,27 +1107,60 @@ static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, 
       if (!winner[s]) continue;
       int e = flip_edge_of(seed, win[s], ne);
       if (!m.flip_ok(e)) continue;
+      {  // the device refuses flips that would raise a valence above 32
+        int c = m.to[m.nxt[2 * e]], d = m.to[m.nxt[2 * e + 1]];
+        int vc = 0, vd = 0;
+        m.voh(c, [&](int) { ++vc; });
+        m.voh(d, [&](int) { ++vd; });
+        if (vc >= 32 || vd >= 32) continue;
+      }
       ok[s] = 1;
-      Props before = edge_vertex_properties(m, e, E);
-      // flip on a snapshot-restorable basis
       int a0 = 2 * e, b0 = 2 * e + 1;
       int a1 = m.nxt[a0], a2 = m.nxt[a1], b1 = m.nxt[b0], b2 = m.nxt[b1];
-      int va0 = m.to[a0], vb0 = m.to[b0];
+      int va0 = m.to[a0], va1 = m.to[a1], vb0 = m.to[b0], vb1 = m.to[b1];
       int fa = m.fc[a0], fb = m.fc[b0];
+      int quad[4] = {va0, va1, vb0, vb1};
+      double ob[4][6], oa[4][6];
+      PortRing R;
+      for (int q = 0; q < 4; ++q) {  // before: the current rings
+        port_ring_before(m, quad[q], R);
+        port_ring_props(m, R, quad[q], E.prm, ob[q]);
+        ob[q][5] = port_repulsion(m, E, quad[q]);
+      }
+      for (int q = 0; q < 4; ++q) {  // after: rings edited like the device
+        int v = quad[q];
+        port_ring_before(m, v, R);
+        if (v == va0) port_ring_remove(R, vb0);
+        else if (v == vb0) port_ring_remove(R, va0);
+        else if (v == va1) port_ring_insert_before(R, vb0, vb1);
+        else port_ring_insert_before(R, va0, va1);
+        port_ring_props(m, R, v, E.prm, oa[q]);
+      }
+      // the repulsion after the flip sees the flipped exclusion rings
       int sv_to[2] = {m.to[a0], m.to[b0]};
       int sv_nx[6] = {m.nxt[a0], m.nxt[a1], m.nxt[a2], m.nxt[b0], m.nxt[b1], m.nxt[b2]};
       int sv_fc[2] = {m.fc[a1], m.fc[b1]};
       int sv_fh[2] = {m.fhe[fa], m.fhe[fb]};
       int sv_vo[2] = {m.vout[va0], m.vout[vb0]};
       m.flip(e);
-      Props after = edge_vertex_properties(m, e, E);
+      for (int q = 0; q < 4; ++q) oa[q][5] = port_repulsion(m, E, quad[q]);
       m.to[a0] = sv_to[0]; m.to[b0] = sv_to[1];
       m.nxt[a0] = sv_nx[0]; m.nxt[a1] = sv_nx[1]; m.nxt[a2] = sv_nx[2];
       m.nxt[b0] = sv_nx[3]; m.nxt[b1] = sv_nx[4]; m.nxt[b2] = sv_nx[5];
       m.fc[a1] = sv_fc[0]; m.fc[b1] = sv_fc[1];
       m.fhe[fa] = sv_fh[0]; m.fhe[fb] = sv_fh[1];
       m.vout[va0] = sv_vo[0]; m.vout[vb0] = sv_vo[1];
-      before -= after;
+      // summation orders of edge_vertex_properties before (va0, va1, vb0,
+      // vb1) and after the flip (va1, vb0, vb1, va0)
+      double dpv[6];
+      for (int k = 0; k < 6; ++k) {
+        double bsum = ((ob[0][k] + ob[1][k]) + ob[2][k]) + ob[3][k];
+        double asum = ((oa[1][k] + oa[2][k]) + oa[3][k]) + oa[0][k];
+        dpv[k] = bsum - asum;
+      }
+      Props before;
+      before.area = dpv[0]; before.volume = dpv[1]; before.curvature = dpv[2];
+      before.bending = dpv[3]; before.tethering = dpv[4]; before.repulsion = dpv[5];
       dps[s] = before;
     }
     // sequential Metropolis in window order, then commit

@@ -145,7 +145,7 @@ def test_pair_sets_bit_exact(C, n_search, excl, mesh):
     else:
         p, f = meshgen.jittered_icosphere(4, sigma_rel=0.2, seed=5)
         l = meshgen.mean_edge_length(p, f)
-        rl, rq = 1.1 * l, 0.9 * l
+        rl, rq = 2.4 * l, 2.1 * l  # beyond the 2-ring, so every exclusion level keeps pairs
     mo = O.Mesh(p, f)
     mg = C.Mesh(p, f)
     no = O.NList(mo, n_search, excl, rl)

@@ -27,6 +27,9 @@ BUILD = os.path.join(PKG, "_build", platform.machine())
 LIB = os.path.join(PKG, "libtrimem_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+# The flip sweep's accept decisions are checked bit for bit against a CPU
+# port; without FMA contraction both round every operation the same way.
+PER_FILE = {"flips.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -84,7 +87,7 @@ def build(verbose=False, jobs=None):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if _newer(obj, [src] + headers):
-            todo.append([nvcc] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            todo.append([nvcc] + NVCC_FLAGS + PER_FILE.get(os.path.basename(src), []) + ["-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, max(1, os.cpu_count() or 1))) as ex:
         for f in [ex.submit(_run, c, verbose) for c in todo]:
             f.result()

@@ -52,8 +52,14 @@ using namespace tmg;
 namespace tmg {
 
 // ---- per-face and per-edge quantities ------------------------------------
-__global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__ fd) {
+__global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__ fd, float* __restrict__ P32) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
+  // the float copy of the positions used by the neighbour prefilter
+  for (int v = f; v < t.nv; v += gridDim.x * blockDim.x) {
+    P32[3 * v] = (float)P[3 * v];
+    P32[3 * v + 1] = (float)P[3 * v + 1];
+    P32[3 * v + 2] = (float)P[3 * v + 2];
+  }
   if (f >= t.nf) return;
   int a = t.fv[3 * f], b = t.fv[3 * f + 1], c = t.fv[3 * f + 2];
   d3 pa = ld3(P, a), pb = ld3(P, b), pc = ld3(P, c);
@@ -155,7 +161,7 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const double* __restrict_
     d3 gr = mk(0, 0, 0);
     const double lc1 = ep.rlc1;
     const int rr = ep.rr;
-    for_each_neighbour(nl, t, P, v, p, lc1, [&](int, double l, d3 dvec) {
+    for_each_neighbour(nl, t, P, v, p, lc1, ep.rT, [&](int, double l, d3 dvec) {
       double lmc = l - lc1;
       double ex = exp(l / lmc);
       pot += ex / ipow(l, rr);
@@ -302,6 +308,7 @@ EP make_ep(const tm_energy* e) {
   ep.r = p.bond_r;
   ep.btype = p.bond_type;
   ep.rlc1 = p.rep_lc1;
+  ep.rT = sq_threshold(p.rep_lc1);
   ep.rr = p.rep_r;
   ep.tdiv = p.bond_type == 0 ? 2.0 : 3.0;
   return ep;
@@ -320,7 +327,10 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
   EP ep = make_ep(e);
   FaceD* fd = reinterpret_cast<FaceD*>(e->face.get());
   EdgeD* ed = reinterpret_cast<EdgeD*>(e->edge.get());
-  if (t.nf) k_face<<<nblk(t.nf, 256), 256, 0, s>>>(t, P, fd);
+  NLView nlv = e->nl.view;
+  nlv.pos32 = e->pos32.get();
+  int nfb = std::max(nblk(std::max(t.nf, t.nv), 256), 1);
+  k_face<<<nfb, 256, 0, s>>>(t, P, fd, e->pos32.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
   if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep);
@@ -328,7 +338,7 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
   int nb = std::max(1, nblk(t.nv, VB));
 #define TM_KV(G, VP)                                                                                         \
-  k_vertex<G, VP><<<nb, VB, 0, s>>>(t, P, fd, ed, e->ebond.get(), e->nl.view, ep, e->rho.get(), e->repg.get(), \
+  k_vertex<G, VP><<<nb, VB, 0, s>>>(t, P, fd, ed, e->ebond.get(), nlv, ep, e->rho.get(), e->repg.get(), \
                                     e->vprops.get(), e->partials.get(), e->glob.get())
   if (want_grad && want_vprops)
     TM_KV(true, true);
@@ -366,6 +376,7 @@ void tm_energy::ensure(int nv_, int ne_, int nf_) {
   rho.ensure(std::max(nv, 1));
   repg.ensure(3 * (size_t)std::max(nv, 1));
   vprops.ensure(6 * (size_t)std::max(nv, 1));
+  pos32.ensure(3 * (size_t)std::max(nv, 1));
   int nb = std::max(1, (nv + tmg::VB - 1) / tmg::VB);
   partials.ensure(8 * (size_t)nb);
   grad.ensure(3 * (size_t)std::max(nv, 1));

@@ -259,7 +259,8 @@ __device__ void vprops_ring(const Ring& R, int v, const double* P, const EP& ep,
   double pot = 0.0;
   const double lc1 = ep.rlc1;
   const int rr = ep.rr;
-  for_each_neighbour_x(nl, P, v, xv, lc1, excl, [&](int, double l, d3) { pot += exp(l / (l - lc1)) / ipow(l, rr); });
+  for_each_neighbour_x(nl, P, v, xv, lc1, ep.rT, excl,
+                       [&](int, double l, d3) { pot += exp(l / (l - lc1)) / ipow(l, rr); });
   out[5] = pot;
 }
 
@@ -435,6 +436,8 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   if (ne == 0 || nflips <= 0) return 0;
   energy_eval(e, m, P, false, false, nullptr, s);
   EP ep = make_ep(e);
+  NLView nlv = e->nl.view;
+  nlv.pos32 = e->pos32.get();  // written by the evaluation above
   TopoW t = m->topo_w();
   DevBuf<int> owner;
   DevBuf<long long> win, pend;
@@ -470,7 +473,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     TM_LAUNCH();
     k_release<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), owner.get());
     TM_LAUNCH();
-    k_delta<<<nblk(8L * W, 64), 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, e->nl.view,
+    k_delta<<<nblk(8L * W, 64), 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv,
                                           part.get(), okf.get());
     TM_LAUNCH();
     k_metro<<<1, 1, 0, s>>>(W, seed, win.get(), winner.get(), okf.get(), part.get(), ep, st.get(), limit.get(),

@@ -113,7 +113,9 @@ __global__ void k_bbox(int nv, const double* P, double* part) {
     for (int k = 0; k < 6; ++k) part[6 * blockIdx.x + k] = s[k][0];
 }
 
-__global__ void k_bbox_final(int nb, const double* part, double* out) {
+// Bounding box with the reference's initial values, then r_list, shape and
+// strides exactly like src/nlists/cell_list.h:56-65.
+__global__ void k_bbox_final(int nb, const double* part, double rlist, NLGeom* G) {
   if (threadIdx.x || blockIdx.x) return;
   double lo[3] = {DBL_MAX, 0.0, 0.0}, hi[3] = {-1.0, 0.0, 0.0};
   for (int b = 0; b < nb; ++b)
@@ -122,10 +124,17 @@ __global__ void k_bbox_final(int nb, const double* part, double* out) {
       if (a < lo[k]) lo[k] = a;
       if (c > hi[k]) hi[k] = c;
     }
+  const double box_eps = 1.0e-6;
   for (int k = 0; k < 3; ++k) {
-    out[k] = lo[k];
-    out[3 + k] = hi[k];
+    double dim = __dadd_rn(__dsub_rn(hi[k], lo[k]), box_eps);
+    int nk = (int)__ddiv_rn(dim, rlist);
+    G->rl[k] = nk > 0 ? __ddiv_rn(dim, (double)nk) : dim;
+    G->shape[k] = nk > 0 ? nk : 1;
+    G->bmin[k] = lo[k];
   }
+  G->stride[0] = 1;
+  G->stride[1] = G->shape[0];
+  G->stride[2] = (long long)G->shape[0] * G->shape[1];
 }
 
 __global__ void k_table_init(CellEntry* T, size_t n) {
@@ -141,11 +150,12 @@ __global__ void k_cell_insert(int nv, const double* P, NLView nl, CellEntry* T, 
                               int* vslot, int* status) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
+  const NLGeom& G = *nl.geom;
   long long id = 0;
   for (int k = 0; k < 3; ++k) {
-    int c = (int)__ddiv_rn(__dsub_rn(P[3 * v + k], nl.bmin[k]), nl.rl[k]);
+    int c = (int)__ddiv_rn(__dsub_rn(P[3 * v + k], G.bmin[k]), G.rl[k]);
     vcoord[3 * v + k] = c;
-    id += (long long)c * nl.stride[k];
+    id += (long long)c * G.stride[k];
   }
   vcid[v] = id;
   unsigned long long h = cell_hash2(id) & nl.tmask;
@@ -183,11 +193,12 @@ __global__ void k_scatter(int nv, const int* vslot, const CellEntry* T, int* fil
   int pos = T[s].start + atomicAdd(&fill[s], 1);
   cell_verts[pos] = v;
 }
-__global__ void k_sort_cells(const CellEntry* T, int n, int* cell_verts) {
+// sort each cell's members ascending and record each vertex's rank in its cell
+__global__ void k_sort_cells(const CellEntry* T, int n, int* cell_verts, int* vrank) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int c = T[i].count;
-  if (c < 2) return;
+  if (c < 1) return;
   int* a = cell_verts + T[i].start;
   for (int x = 1; x < c; ++x) {
     int key = a[x];
@@ -197,6 +208,60 @@ __global__ void k_sort_cells(const CellEntry* T, int n, int* cell_verts) {
       --y;
     }
     a[y + 1] = key;
+  }
+  for (int x = 0; x < c; ++x) vrank[a[x]] = x;
+}
+
+// Position of the pair {v, u} in the reference's distance_matrix traversal
+// (cell pairs in ascending first-cell id, neighbour offsets x-outer/z-inner,
+// then the rank of the first-cell vertex, then of the second).
+struct PairKey {
+  long long icell;
+  int off, ra, rb;
+};
+__device__ __forceinline__ PairKey pair_key(int v, int u, const long long* vcid, const int* vcoord,
+                                            const int* vrank) {
+  long long cv = vcid[v], cu = vcid[u];
+  int a = v, b = u;
+  if (cu < cv || (cu == cv && u < v)) {
+    a = u;
+    b = v;
+  }
+  PairKey k;
+  k.icell = vcid[a];
+  int dx = vcoord[3 * b] - vcoord[3 * a], dy = vcoord[3 * b + 1] - vcoord[3 * a + 1];
+  int dz = vcoord[3 * b + 2] - vcoord[3 * a + 2];
+  k.off = (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1);
+  k.ra = vrank[a];
+  k.rb = vrank[b];
+  return k;
+}
+__device__ __forceinline__ bool key_less(const PairKey& x, const PairKey& y) {
+  if (x.icell != y.icell) return x.icell < y.icell;
+  if (x.off != y.off) return x.off < y.off;
+  if (x.ra != y.ra) return x.ra < y.ra;
+  return x.rb < y.rb;
+}
+
+// order each Verlet row like the reference's push_back sequence
+// (src/nlists/verlet_list.h:26-34)
+__global__ void k_verlet_sort(int nv, const int* vrow, int* vcol, double* vd, const long long* vcid,
+                              const int* vcoord, const int* vrank) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  int lo = vrow[v], hi = vrow[v + 1];
+  for (int x = lo + 1; x < hi; ++x) {
+    int u = vcol[x];
+    double du = vd[x];
+    PairKey ku = pair_key(v, u, vcid, vcoord, vrank);
+    int y = x - 1;
+    while (y >= lo && key_less(ku, pair_key(v, vcol[y], vcid, vcoord, vrank))) {
+      vcol[y + 1] = vcol[y];
+      vd[y + 1] = vd[y];
+      --y;
+    }
+    vcol[y + 1] = u;
+    vd[y + 1] = du;
   }
 }
 
@@ -211,18 +276,19 @@ __global__ void k_cell_pairs(int nv, const double* P, NLView nl, Topo t, const i
   if (a >= nv) return;
   d3 pa = ld3(P, a);
   long long ca = vcid[a];
+  const NLGeom& G = *nl.geom;
   int n = 0;
   int base = pass ? off[a] : 0;
   for (int x = -1; x < 2; ++x) {
     int ii = vcoord[3 * a] + x;
-    if (ii < 0 || ii >= nl.shape[0]) continue;
+    if (ii < 0 || ii >= G.shape[0]) continue;
     for (int y = -1; y < 2; ++y) {
       int jj = vcoord[3 * a + 1] + y;
-      if (jj < 0 || jj >= nl.shape[1]) continue;
+      if (jj < 0 || jj >= G.shape[1]) continue;
       for (int z = -1; z < 2; ++z) {
         int kk = vcoord[3 * a + 2] + z;
-        if (kk < 0 || kk >= nl.shape[2]) continue;
-        long long cid = ii * nl.stride[0] + jj * nl.stride[1] + kk * nl.stride[2];
+        if (kk < 0 || kk >= G.shape[2]) continue;
+        long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
         if (mode == 1 && cid < ca) continue;
         int st = 0;
         int cnt_c = cell_lookup(nl, cid, &st);
@@ -242,6 +308,39 @@ __global__ void k_cell_pairs(int nv, const double* P, NLView nl, Topo t, const i
               oj[base + n] = a < b ? b : a;
             }
           }
+          ++n;
+        }
+      }
+    }
+  }
+  if (!pass) cnt[a] = n;
+}
+
+// candidate rows: members of the 27 build-time neighbour cells of vertex a in
+// the reference's scan order (x outer, z inner; members ascending), self
+// excluded.  pass 0 counts, pass 1 writes.
+__global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt, const int* off, int* out) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nv) return;
+  const NLGeom& G = *nl.geom;
+  int n = 0;
+  int base = pass ? off[a] : 0;
+  for (int x = -1; x < 2; ++x) {
+    int ii = vcoord[3 * a] + x;
+    if (ii < 0 || ii >= G.shape[0]) continue;
+    for (int y = -1; y < 2; ++y) {
+      int jj = vcoord[3 * a + 1] + y;
+      if (jj < 0 || jj >= G.shape[1]) continue;
+      for (int z = -1; z < 2; ++z) {
+        int kk = vcoord[3 * a + 2] + z;
+        if (kk < 0 || kk >= G.shape[2]) continue;
+        long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
+        int st = 0;
+        int c = cell_lookup(nl, cid, &st);
+        for (int q = 0; q < c; ++q) {
+          int b = nl.cell_verts[st + q];
+          if (b == a) continue;
+          if (pass) out[base + n] = b;
           ++n;
         }
       }
@@ -280,19 +379,20 @@ __global__ void k_point(int pid, const double* P, NLView nl, Topo t, double rd, 
   d3 p = ld3(P, pid);
   int n = 0;
   if (nl.kind == 0) {
+    const NLGeom& G = *nl.geom;
     int co[3];
     const double* pp = &p.x;
-    for (int k = 0; k < 3; ++k) co[k] = (int)__ddiv_rn(__dsub_rn(pp[k], nl.bmin[k]), nl.rl[k]);
+    for (int k = 0; k < 3; ++k) co[k] = (int)__ddiv_rn(__dsub_rn(pp[k], G.bmin[k]), G.rl[k]);
     for (int a = -1; a < 2; ++a) {
       int ii = co[0] + a;
-      if (ii < 0 || ii >= nl.shape[0]) continue;
+      if (ii < 0 || ii >= G.shape[0]) continue;
       for (int b = -1; b < 2; ++b) {
         int jj = co[1] + b;
-        if (jj < 0 || jj >= nl.shape[1]) continue;
+        if (jj < 0 || jj >= G.shape[1]) continue;
         for (int c = -1; c < 2; ++c) {
           int kk = co[2] + c;
-          if (kk < 0 || kk >= nl.shape[2]) continue;
-          long long cid = ii * nl.stride[0] + jj * nl.stride[1] + kk * nl.stride[2];
+          if (kk < 0 || kk >= G.shape[2]) continue;
+          long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
           int st = 0;
           int cc = cell_lookup(nl, cid, &st);
           for (int q = 0; q < cc; ++q) {
@@ -341,32 +441,18 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
   V = NLView{};
   V.kind = 0;
   V.excl = p.exclusion_level;
-  // 1. box
+  // 1. box and cell geometry (device only, no host round trip)
   int nb = std::max(1, std::min(1024, nblk(nv, BB)));
   nl->bbox.ensure(6 * (size_t)nb + 6);
-  double box[6] = {DBL_MAX, 0, 0, -1, 0, 0};
+  nl->geom.ensure(1);
+  V.geom = nl->geom.get();
   if (nv > 0) {
     k_bbox<<<nb, BB, 0, s>>>(nv, P, nl->bbox.get());
     TM_LAUNCH();
-    k_bbox_final<<<1, 1, 0, s>>>(nb, nl->bbox.get(), nl->bbox.get() + 6 * nb);
-    TM_LAUNCH();
-    TM_CUDA(cudaMemcpyAsync(box, nl->bbox.get() + 6 * nb, sizeof(box), cudaMemcpyDeviceToHost, s));
-    TM_CUDA(cudaStreamSynchronize(s));
   }
-  const double rlist = p.rlist, box_eps = 1.0e-6;
-  int shape[3];
-  for (int k = 0; k < 3; ++k) {
-    double dim = box[3 + k] - box[k] + box_eps;
-    int nk = int(dim / rlist);
-    V.rl[k] = nk > 0 ? dim / nk : dim;
-    shape[k] = nk > 0 ? nk : 1;
-    V.bmin[k] = box[k];
-    V.shape[k] = shape[k];
-  }
-  V.stride[0] = 1;
-  V.stride[1] = shape[0];
-  V.stride[2] = (long long)shape[0] * shape[1];
-  // 2. hash table of non-empty cells
+  k_bbox_final<<<1, 1, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
+  TM_LAUNCH();
+  // 2. hash table of the non-empty cells: 2x the vertex count, power of two
   size_t tsize = 64;
   while (tsize < 2 * (size_t)std::max(nv, 1)) tsize <<= 1;
   nl->table.ensure(tsize);
@@ -374,13 +460,13 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
   nl->vcid.ensure(std::max(nv, 1));
   nl->vcoord.ensure(3 * (size_t)std::max(nv, 1));
   nl->vslot.ensure(std::max(nv, 1));
+  nl->vrank.ensure(std::max(nv, 1));
   nl->cnt.ensure(tsize + 1);
   nl->fill.ensure(tsize);
   nl->cell_verts.ensure(std::max(nv, 1));
   nl->d_count.ensure(4);
   k_table_init<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), tsize);
   TM_LAUNCH();
-  TM_CUDA(cudaMemsetAsync(nl->d_count.get(), 0, sizeof(int), s));
   V.table = nl->table.get();
   V.cell_verts = nl->cell_verts.get();
   if (nv > 0) {
@@ -393,35 +479,55 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
     exclusive_scan_int(nl->cnt.get(), nl->fill.get(), (int)tsize, nullptr, nl->tmp, s);
     k_set_start<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), (int)tsize, nl->fill.get());
     TM_LAUNCH();
-    // 4. scatter + per-cell sort
+    // 4. scatter + per-cell sort (members ascending, rank of each vertex)
     TM_CUDA(cudaMemsetAsync(nl->fill.get(), 0, sizeof(int) * tsize, s));
     k_scatter<<<nblk(nv, 256), 256, 0, s>>>(nv, nl->vslot.get(), nl->table.get(), nl->fill.get(),
                                             nl->cell_verts.get());
     TM_LAUNCH();
-    k_sort_cells<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), (int)tsize, nl->cell_verts.get());
+    k_sort_cells<<<nblk((long)tsize, 256), 256, 0, s>>>(nl->table.get(), (int)tsize, nl->cell_verts.get(),
+                                                        nl->vrank.get());
     TM_LAUNCH();
-    int st = 0;
-    TM_CUDA(cudaMemcpyAsync(&st, nl->d_count.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
-    TM_CUDA(cudaStreamSynchronize(s));
-    if (st) fail(TM_ERR_DEVICE, "cell table overflow");
+  }
+  if (p.n_search == 0 && nv > 0) {
+    // candidate rows for the queries of points that stay in their build cell
+    nl->crow.ensure((size_t)nv + 1);
+    nl->cnt.ensure((size_t)nv + 1);
+    k_cand<<<nblk(nv, 256), 256, 0, s>>>(nv, V, nl->vcoord.get(), 0, nl->cnt.get(), nullptr, nullptr);
+    TM_LAUNCH();
+    TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
+    int total = 0;
+    exclusive_scan_int(nl->cnt.get(), nl->crow.get(), nv + 1, &total, nl->tmp, s);
+    // rows are only kept while they stay small (coarse grids fall back to the
+    // cell table)
+    if ((long long)total <= 64LL * nv) {
+      nl->ccol.ensure(std::max(total, 1));
+      k_cand<<<nblk(nv, 256), 256, 0, s>>>(nv, V, nl->vcoord.get(), 1, nullptr, nl->crow.get(), nl->ccol.get());
+      TM_LAUNCH();
+      V.crow = nl->crow.get();
+      V.ccol = nl->ccol.get();
+      V.bcoord = nl->vcoord.get();
+    }
   }
   if (p.n_search == 1) {
-    // Verlet CSR from the cell list at cut-off rlist
+    // Verlet CSR from the cell list at cut-off rlist, rows in the reference's
+    // insertion order
     nl->vrow.ensure((size_t)nv + 1);
-    nl->tmp.ensure(4);
     Topo t = m->topo();
     int total = 0;
     if (nv > 0) {
       nl->cnt.ensure((size_t)nv + 1);
-      k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), nl->vcid.get(), rlist, 0, 0,
+      k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), nl->vcid.get(), p.rlist, 0, 0,
                                                  nl->cnt.get(), nullptr, nullptr, nullptr, nullptr);
       TM_LAUNCH();
       TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
       exclusive_scan_int(nl->cnt.get(), nl->vrow.get(), nv + 1, &total, nl->tmp, s);
       nl->vcol.ensure(std::max(total, 1));
       nl->d_res.ensure(std::max(total, 1));
-      k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), nl->vcid.get(), rlist, 0, 1,
+      k_cell_pairs<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), nl->vcid.get(), p.rlist, 0, 1,
                                                  nullptr, nl->vrow.get(), nl->d_res.get(), nullptr, nl->vcol.get());
+      TM_LAUNCH();
+      k_verlet_sort<<<nblk(nv, 128), 128, 0, s>>>(nv, nl->vrow.get(), nl->vcol.get(), nl->d_res.get(),
+                                                  nl->vcid.get(), nl->vcoord.get(), nl->vrank.get());
       TM_LAUNCH();
     } else {
       TM_CUDA(cudaMemsetAsync(nl->vrow.get(), 0, sizeof(int), s));

@@ -12,7 +12,7 @@ struct EP {
   double refA, refV, refC;
   double lc0, lc1, a0;
   int r, btype;  // btype 0 edge bonds, 1 area bonds
-  double rlc1;
+  double rlc1, rT;  // repulsion cut-off and its exact squared threshold
   int rr;
   double tdiv;
 };
@@ -71,56 +71,101 @@ struct TableExcl {  // exclusion on the current topology tables
   __device__ bool operator()(int v, int j) const { return excluded(t, excl, v, j); }
 };
 
+// Distance test of candidate j against the query point p of vertex v:
+// an FP32 prefilter (skips only candidates that are certainly outside,
+// margin from the float rounding of both points) and the exact test
+// sqrt(s) < dmax  <=>  s < T with s rounded operation by operation.
+struct PairTest {
+  double T;     // exact squared threshold of dmax
+  float bound;  // prefilter bound on the float squared distance
+  float3 p32;
+  bool pre;
+};
+__device__ __forceinline__ PairTest make_pair_test(const NLView& nl, int v, double dmax, double T) {
+  PairTest t;
+  t.T = T;
+  t.pre = nl.pos32 != nullptr;
+  if (t.pre) {
+    t.p32 = make_float3(nl.pos32[3 * v], nl.pos32[3 * v + 1], nl.pos32[3 * v + 2]);
+    float pinf = fmaxf(fabsf(t.p32.x), fmaxf(fabsf(t.p32.y), fabsf(t.p32.z)));
+    float dm = (float)dmax;
+    float eps = 1.7320508f * (2.0f * pinf + 2.0f * dm) * 1.1920929e-07f;  // 2 ulp(1) per unit
+    float r = dm + eps;
+    t.bound = r * r * (1.0f + 9.5367431e-07f);
+  }
+  return t;
+}
+// returns true (and s, the exact squared distance) when |p - x_j| < dmax
+__device__ __forceinline__ bool pair_within(const PairTest& t, const NLView& nl, const double* P, d3 p, int j,
+                                            d3* pj_out, double* s_out) {
+  if (t.pre) {
+    float dx = nl.pos32[3 * j] - t.p32.x, dy = nl.pos32[3 * j + 1] - t.p32.y, dz = nl.pos32[3 * j + 2] - t.p32.z;
+    float s32 = dx * dx + dy * dy + dz * dz;
+    if (s32 > t.bound) return false;
+  }
+  d3 pj = ld3(P, j);
+  double dx = __dsub_rn(p.x, pj.x), dy = __dsub_rn(p.y, pj.y), dz = __dsub_rn(p.z, pj.z);
+  double s = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  *pj_out = pj;
+  *s_out = s;
+  return s < t.T;
+}
+
 // Calls fn(j, |p - x_j|, p - x_j) for every neighbour j of vertex v (at p)
-// closer than dmax, in the reference's order: the 27 cells (x outer, z
-// inner), each cell's members in ascending order; or the Verlet row.
+// closer than dmax (T = sq_threshold(dmax)), in the reference's order: the
+// 27 cells (x outer, z inner), each cell's members in ascending order; or the
+// Verlet row.
 template <class F, class X>
 __device__ __forceinline__ void for_each_neighbour_x(const NLView& nl, const double* P, int v, d3 p, double dmax,
-                                                     const X& is_excluded, F&& fn) {
+                                                     double T, const X& is_excluded, F&& fn) {
+  PairTest pt = make_pair_test(nl, v, dmax, T);
+  auto visit = [&](int j) {
+    d3 pj;
+    double s;
+    if (!pair_within(pt, nl, P, p, j, &pj, &s)) return;
+    if (nl.excl > 0 && is_excluded(v, j)) return;
+    fn(j, __dsqrt_rn(s), exact_diff(p, pj));
+  };
   if (nl.kind == 0) {
+    const NLGeom& G = *nl.geom;
     int co[3];
     const double* pp = &p.x;
-    for (int k = 0; k < 3; ++k) co[k] = (int)__ddiv_rn(__dsub_rn(pp[k], nl.bmin[k]), nl.rl[k]);
+    for (int k = 0; k < 3; ++k) co[k] = (int)__ddiv_rn(__dsub_rn(pp[k], G.bmin[k]), G.rl[k]);
+    if (nl.crow && co[0] == nl.bcoord[3 * v] && co[1] == nl.bcoord[3 * v + 1] && co[2] == nl.bcoord[3 * v + 2]) {
+      int lo = nl.crow[v], hi = nl.crow[v + 1];
+      for (int q = lo; q < hi; ++q) visit(nl.ccol[q]);
+      return;
+    }
     for (int a = -1; a < 2; ++a) {
       int ii = co[0] + a;
-      if (ii < 0 || ii >= nl.shape[0]) continue;
+      if (ii < 0 || ii >= G.shape[0]) continue;
       for (int b = -1; b < 2; ++b) {
         int jj = co[1] + b;
-        if (jj < 0 || jj >= nl.shape[1]) continue;
+        if (jj < 0 || jj >= G.shape[1]) continue;
         for (int c = -1; c < 2; ++c) {
           int kk = co[2] + c;
-          if (kk < 0 || kk >= nl.shape[2]) continue;
-          long long cid = ii * nl.stride[0] + jj * nl.stride[1] + kk * nl.stride[2];
+          if (kk < 0 || kk >= G.shape[2]) continue;
+          long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
           int st = 0;
           int cnt = cell_find(nl, cid, &st);
           for (int q = 0; q < cnt; ++q) {
             int j = nl.cell_verts[st + q];
-            if (j == v) continue;
-            d3 pj = ld3(P, j);
-            double l = exact_dist(p, pj);
-            if (!(l < dmax)) continue;
-            if (nl.excl > 0 && is_excluded(v, j)) continue;
-            fn(j, l, exact_diff(p, pj));
+            if (j != v) visit(j);
           }
         }
       }
     }
   } else {
     int lo = nl.vrow[v], hi = nl.vrow[v + 1];
-    for (int q = lo; q < hi; ++q) {
-      int j = nl.vcol[q];
-      d3 pj = ld3(P, j);
-      double l = exact_dist(p, pj);
-      if (l < dmax) fn(j, l, exact_diff(p, pj));
-    }
+    for (int q = lo; q < hi; ++q) visit(nl.vcol[q]);
   }
 }
 
 template <class F>
 __device__ __forceinline__ void for_each_neighbour(const NLView& nl, const Topo& t, const double* P, int v, d3 p,
-                                                   double dmax, F&& fn) {
+                                                   double dmax, double T, F&& fn) {
   TableExcl x{t, nl.excl};
-  for_each_neighbour_x(nl, P, v, p, dmax, x, fn);
+  for_each_neighbour_x(nl, P, v, p, dmax, T, x, fn);
 }
 
 // ---- per-vertex properties + block reduction + device-side assembly -------

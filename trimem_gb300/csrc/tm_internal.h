@@ -83,17 +83,29 @@ struct CellEntry {
   long long key;  // cell id, -1 empty
   int start, count;
 };
+// Cell geometry, derived on the device from the bounding box.
+struct NLGeom {
+  double bmin[3], rl[3];
+  int shape[3];
+  int pad;
+  long long stride[3];
+};
 struct NLView {
   int kind;  // 0 cell list, 1 Verlet list
   int excl;
-  double bmin[3], rl[3];
-  int shape[3];
-  long long stride[3];
+  const NLGeom* geom;
   const CellEntry* table;
   unsigned long long tmask;
   const int* cell_verts;
   const int* vrow;  // Verlet CSR
   const int* vcol;
+  // cell list: members of the 27 build-time neighbour cells of each vertex
+  // (reference scan order, self excluded), used while the query point is
+  // still inside its build cell
+  const int* crow;
+  const int* ccol;
+  const int* bcoord;   // build-time cell coordinates, 3 per vertex
+  const float* pos32;  // positions rounded to float (prefilter), may be NULL
 };
 
 struct TopoW;
@@ -130,7 +142,8 @@ struct tm_nlist {
   tm_params prm{};
   int nv = 0;
   tmg::DevBuf<tmg::CellEntry> table;
-  tmg::DevBuf<int> cell_verts, vslot, vcoord, cnt, fill, vrow, vcol, tmp;
+  tmg::DevBuf<int> cell_verts, vslot, vcoord, vrank, cnt, fill, vrow, vcol, crow, ccol, tmp;
+  tmg::DevBuf<tmg::NLGeom> geom;
   tmg::DevBuf<long long> vcid;
   tmg::DevBuf<double> bbox;
   // last query result
@@ -159,6 +172,7 @@ struct tm_energy {
   tm_nlist nl;
   int nv = 0, ne = 0, nf = 0;
   tmg::DevBuf<double> face, edge, ebond, rho, repg, vprops, partials, grad, work;
+  tmg::DevBuf<float> pos32;
   tmg::DevBuf<tmg::Globals> glob;
   cudaStream_t stream = nullptr;
   void ensure(int nv_, int ne_, int nf_);
@@ -178,6 +192,9 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* d_po
 int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* d_points, double rdist, cudaStream_t s);
 int64_t nlist_point_distances(tm_nlist* nl, tm_mesh* m, const double* d_points, int pid, double rdist,
                               cudaStream_t s);
+// smallest double T with sqrt(T) >= d (IEEE round-to-nearest sqrt), so that
+// sqrt(s) < d  <=>  s < T for every double s >= 0
+double sq_threshold(double d);
 // scan.cu helpers
 void exclusive_scan_int(const int* in, int* out, int n, int* total_host, DevBuf<int>& tmp, cudaStream_t s);
 }  // namespace tmg

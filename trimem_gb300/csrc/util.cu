@@ -1,4 +1,5 @@
 // Error plumbing and deterministic scan / reduction helpers.
+#include <cmath>
 #include <cstdio>
 #include <string>
 
@@ -19,6 +20,18 @@ void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
   snprintf(buf, sizeof(buf), "CUDA error %s (%s) at %s:%d in %s", cudaGetErrorName(e), cudaGetErrorString(e), file,
            line, what);
   fail(TM_ERR_CUDA, buf);
+}
+
+double sq_threshold(double d) {
+  if (!(d > 0)) return d != d ? d : 0.0;
+  if (std::isinf(d)) return d;
+  double s = d * d;
+  if (std::sqrt(s) >= d) {
+    while (s > 0 && std::sqrt(std::nextafter(s, 0.0)) >= d) s = std::nextafter(s, 0.0);
+  } else {
+    while (std::sqrt(s) < d) s = std::nextafter(s, INFINITY);
+  }
+  return s;
 }
 
 // ---- exclusive scan of int counts (three phases, 1024 items per block) ----
