@@ -61,6 +61,21 @@ def config(extra=None):
     return c
 
 
+def read_traffic():
+    """DRAM bytes per launch of each evaluation kernel from the committed ncu
+    summary (profiles/eval_kernels_L7_full.md)."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "eval_kernels_L7_full.md")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 2 and parts[0].startswith("k_") and parts[1].isdigit():
+                out[parts[0]] = int(parts[1])
+    except OSError:
+        pass
+    return out
+
+
 def read_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -275,10 +290,7 @@ def main():
     hbm = hbm or 6800.0
     dname = names[dom]
     achieved = kbytes[dname] / (kms[dom] * 1e-3) / 1e9
-    traffic_path = os.path.join(ROOT, "profiles", "traffic.json")
-    traffic = None
-    if os.path.exists(traffic_path):
-        traffic = json.load(open(traffic_path)).get(dname)
+    traffic = read_traffic().get(dname)
     # whole evaluation: SURVEY per-vertex algorithmic bytes (132 B/vertex)
     eval_bytes = 132 * V
     roofline = {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
@@ -288,6 +300,30 @@ def main():
                 "eval_algorithmic_bytes": eval_bytes,
                 "eval_frac": round(eval_bytes / (kms[4] * 1e-3) / 1e9 / hbm, 5),
                 "algorithmic_bytes": kbytes[dname]}
+
+    # ---- FP32-stencil variant: speed and error against FP64 ---------------
+    g64 = g.clone()
+    capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes_ptr(x), ctypes_ptr(g64), ctypes_ptr(e_dev),
+                                       ctypes_ptr_s(stream)))
+    torch.cuda.synchronize()
+    e64 = float(e_dev.item())
+    capi.check(L.tm_energy_set_stencil_precision(en.h, 1))
+    k32 = []
+    for _ in range(5):
+        flush.fill_(1.0)
+        ms5 = (ctypes.c_float * 5)()
+        capi.check(L.tm_energy_eval_timed(en.h, mesh.h, ctypes_ptr(x), ctypes_ptr(g), ms5, ctypes_ptr_s(stream)))
+        k32.append(list(ms5))
+    capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes_ptr(x), ctypes_ptr(g), ctypes_ptr(e_dev),
+                                       ctypes_ptr_s(stream)))
+    torch.cuda.synchronize()
+    e32 = float(e_dev.item())
+    capi.check(L.tm_energy_set_stencil_precision(en.h, 0))
+    k32 = np.median(np.array(k32), axis=0)
+    fp32 = {"eval_ms_cold": round(float(k32[4]), 5), "evals_per_s_cold": round(1e3 / float(k32[4]), 1),
+            "kernel_ms": {n: round(float(k), 5) for n, k in zip(names, k32[:4])},
+            "energy_rel_err": abs(e32 - e64) / abs(e64),
+            "grad_rel_err": float(torch.linalg.norm(g - g64) / torch.linalg.norm(g64))}
 
     # ---- end to end through the public API ---------------------------------
     cm = core.TriMesh(p, f)
@@ -327,7 +363,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config({"eval_ms": round(eval_ms, 5), "rebuild_ms": round(rebuild_ms, 5),
                               "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4)}),
-            "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
+            "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(), "fp32_stencil": fp32,
             "gpu_launches": launches_per_step * args.steps, "notes": peaks_fp64}
     if rank == 0:
         print(json.dumps(line), flush=True)

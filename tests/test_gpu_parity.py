@@ -230,3 +230,24 @@ def test_large_mesh_properties(C):
     assert abs(e - eo.energy(mo)) <= RTOL * abs(e)
     assert rel(g, eo.gradient(mo)) < RTOL
     assert np.linalg.norm(g.sum(0)) < 1e-8 * np.linalg.norm(g)
+
+
+def test_fp32_stencil_error_bounds(C):
+    """FP32-stencil variant: local geometry in FP32, global sums FP64.  Its
+    error against the FP64 result is bounded per quantity (energy and global
+    properties 1e-5 relative, gradient 1e-4 relative norm-wise)."""
+    p, f = meshgen.jittered_icosphere(5, seed=2)
+    prm = workload_params(p, f, excl=1, rep_scale=1.2)
+    mg = C.Mesh(p, f)
+    eg = C.Energy(mg, C.params(**prm))
+    e64, g64 = eg.gradient(mg, with_energy=True)
+    p64 = eg.properties(mg)
+    eg.set_stencil_precision(1)
+    e32, g32 = eg.gradient(mg, with_energy=True)
+    p32 = eg.properties(mg)
+    eg.set_stencil_precision(0)
+    assert np.array_equal(eg.gradient(mg), g64)  # switching back restores FP64
+    assert abs(e32 - e64) <= 1e-5 * abs(e64)
+    for k in range(6):
+        assert abs(p32[k] - p64[k]) <= 1e-5 * max(abs(p64[k]), 1e-12), k
+    assert rel(g32, g64) < 1e-4

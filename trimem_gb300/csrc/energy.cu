@@ -321,6 +321,10 @@ void energy_eval(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool
 
 void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool want_vprops, double* d_grad,
                         cudaStream_t s, cudaEvent_t* ev) {
+  if (e->stencil == 1 && !want_vprops) {
+    energy_eval32(e, m, P, want_grad, want_vprops, d_grad, s, ev);
+    return;
+  }
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
   e->ensure(m->nv, m->ne, m->nf);
   Topo t = m->topo();

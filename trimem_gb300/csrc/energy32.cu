@@ -1,0 +1,354 @@
+// FP32-stencil variant of the energy / gradient evaluation
+// (tm_energy_set_stencil_precision(e, 1)).
+//
+// Positions stay FP64 in memory.  Each evaluation splits them into float
+// hi + lo parts, so an edge vector (x_b - x_a) = (hi_b - hi_a) + (lo_b - lo_a)
+// keeps FP32 relative accuracy even though |x| >> |x_b - x_a|; everything
+// local (normals, areas, cotangents, dihedral angles, potentials, the
+// gradient gather) is then FP32.  Face volumes use x_a . N_f / 6 (N_f from the
+// accurate edge vectors), not the triple product of absolute positions.  The
+// dihedral angle is atan2(|n0 x n1|, n0 . n1), accurate for the small angles
+// of fine meshes where acosf is not.  The global sums, the penalty assembly
+// and the neighbour-pair decisions (exact FP64 threshold) stay FP64, so the
+// pair set is the same as in FP64.
+#include <algorithm>
+#include <cmath>
+
+#include "tm_energy.cuh"
+#include "tm_internal.h"
+#include "tm_math.cuh"
+
+namespace tmg {
+
+struct __align__(16) FaceF {
+  float nx, ny, nz, A, V, c0, c1, c2;
+};
+struct __align__(16) EdgeF {
+  float l, th, db, flag;
+};
+
+namespace {
+
+struct f3 {
+  float x, y, z;
+};
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ f3& operator+=(f3& a, f3 b) {
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+  return a;
+}
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 fcross(f3 a, f3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ float fnorm(f3 a) { return sqrtf(fdot(a, a)); }
+__device__ __forceinline__ float fipow(float x, int n) {
+  int a = n < 0 ? -n : n;
+  float r = 1.0f;
+  for (int k = 0; k < a; ++k) r *= x;
+  return n < 0 ? 1.0f / r : r;
+}
+
+struct Split {
+  const float* hi;
+  const float* lo;
+  __device__ f3 h(int v) const { return {hi[3 * v], hi[3 * v + 1], hi[3 * v + 2]}; }
+  // x_b - x_a with FP32 relative accuracy
+  __device__ f3 diff(int b, int a) const {
+    return {(hi[3 * b] - hi[3 * a]) + (lo[3 * b] - lo[3 * a]), (hi[3 * b + 1] - hi[3 * a + 1]) + (lo[3 * b + 1] - lo[3 * a + 1]),
+            (hi[3 * b + 2] - hi[3 * a + 2]) + (lo[3 * b + 2] - lo[3 * a + 2])};
+  }
+};
+
+__global__ void k_split(int nv, const double* __restrict__ P, float* __restrict__ hi, float* __restrict__ lo) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * nv) return;
+  double x = P[i];
+  float h = (float)x;
+  hi[i] = h;
+  lo[i] = (float)(x - (double)h);
+}
+
+__global__ void k_face32(Topo t, Split S, FaceF* __restrict__ fd) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= t.nf) return;
+  int a = t.fv[3 * f], b = t.fv[3 * f + 1], c = t.fv[3 * f + 2];
+  f3 eab = S.diff(b, a), eac = S.diff(c, a), ebc = S.diff(c, b);
+  f3 N = fcross(eab, eac);
+  float nn = fnorm(N);
+  float inv = 1.0f / nn;
+  FaceF F;
+  F.nx = N.x * inv;
+  F.ny = N.y * inv;
+  F.nz = N.z * inv;
+  F.A = 0.5f * nn;
+  F.V = fdot(S.h(a), N) * (1.0f / 6.0f);
+  F.c0 = fdot(eab, eac) * inv;
+  F.c1 = -fdot(eab, ebc) * inv;
+  F.c2 = fdot(eac, ebc) * inv;
+  fd[f] = F;
+}
+
+__global__ void k_edge32(Topo t, Split S, const FaceF* __restrict__ fd, EdgeF* __restrict__ ed,
+                         float* __restrict__ ebond, EP ep) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.ne) return;
+  int4 E = t.edge[e];
+  f3 ev = S.diff(E.y, E.x);
+  float l = fnorm(ev);
+  EdgeF o;
+  o.l = l;
+  o.th = 0.0f;
+  o.flag = 0.0f;
+  if (E.z >= 0 && E.w >= 0) {
+    FaceF F0 = fd[E.z], F1 = fd[E.w];
+    f3 n0 = {F0.nx, F0.ny, F0.nz}, n1 = {F1.nx, F1.ny, F1.nz};
+    f3 cr = fcross(n0, n1);
+    float a = atan2f(fnorm(cr), fdot(n0, n1));
+    o.th = fdot(cr, ev) >= 0.0f ? a : -a;
+    o.flag = 1.0f;
+  }
+  float val = 0.0f, fac = 0.0f;
+  if (ep.btype == 0) {
+    int r = ep.r;
+    float lc0 = (float)ep.lc0, lc1 = (float)ep.lc1;
+    if (l > lc0) {
+      val = fipow((float)r, r + 1) * fipow(l - lc0, r);
+      fac = fipow((float)r, r + 2) * fipow(l - lc0, r - 1);
+    } else if (l < lc1) {
+      val = expf(l / (l - lc1)) / fipow(l, r);
+    }
+    if (l < lc1) {
+      float lmc = l - lc1;
+      fac -= lc1 / (lmc * lmc) + r / l;
+      fac /= fipow(l, r);
+      fac *= expf(l / lmc);
+    }
+  }
+  o.db = fac;
+  ed[e] = o;
+  ebond[e] = val;
+}
+
+template <bool GRAD, bool VPROPS>
+__global__ void __launch_bounds__(VB) k_vertex32(Topo t, const double* __restrict__ P, Split S,
+                                                const FaceF* __restrict__ fd, const EdgeF* __restrict__ ed,
+                                                const float* __restrict__ ebond, NLView nl, EP ep,
+                                                float* __restrict__ rho, float* __restrict__ repg,
+                                                double* __restrict__ vprops, double* __restrict__ partial,
+                                                Globals* g) {
+  __shared__ double red[6][VB];
+  __shared__ bool last;
+  int v = blockIdx.x * VB + threadIdx.x;
+  double pr[6] = {0, 0, 0, 0, 0, 0};
+  if (v < t.nv) {
+    int d = t.val[v];
+    float A = 0, V = 0, LT = 0, T = 0;
+    for (int m = 0; m < d; ++m) {
+      int4 s = t.slot[(size_t)m * t.nv + v];
+      int f = slot_face(s.y);
+      if (f < 0) continue;
+      float fa = fd[f].A;
+      A += fa;
+      V += fd[f].V;
+      EdgeF E = ed[s.z];
+      LT += E.l * E.th;
+      if (ep.btype == 0) {
+        T += ebond[s.z];
+      } else {
+        float q = fa / (float)ep.a0 - 1.0f;
+        T += q * q;
+      }
+    }
+    float a = A / 3, c = 0.25f * LT;
+    pr[0] = a;
+    pr[1] = V / 3;
+    pr[2] = c;
+    pr[3] = 2 * c * c / a;
+    pr[4] = T / (float)ep.tdiv;
+    d3 p = ld3(P, v);
+    float pot = 0.0f;
+    f3 gr = {0, 0, 0};
+    const float lc1 = (float)ep.rlc1;
+    const int rr = ep.rr;
+    for_each_neighbour(nl, t, P, v, p, ep.rlc1, ep.rT, [&](int j, double ld, d3) {
+      float l = (float)ld;
+      float lmc = l - lc1;
+      float ex = expf(l / lmc);
+      pot += ex / fipow(l, rr);
+      if (GRAD) {
+        float fac = -(lc1 / (lmc * lmc) + rr / l);
+        fac /= fipow(l, rr + 1);
+        fac *= ex;
+        gr += fac * S.diff(v, j);
+      }
+    });
+    pr[5] = pot;
+    rho[v] = c / a;
+    if (GRAD) {
+      repg[3 * v] = 2.0f * gr.x;
+      repg[3 * v + 1] = 2.0f * gr.y;
+      repg[3 * v + 2] = 2.0f * gr.z;
+    }
+    if (VPROPS)
+      for (int k = 0; k < 6; ++k) vprops[6 * (size_t)v + k] = pr[k];
+  }
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = pr[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) partial[8 * (size_t)blockIdx.x + k] = red[k][0];
+    __threadfence();
+    unsigned int tk = atomicAdd(&g->ticket, 1u);
+    last = (tk == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += VB)
+    for (int k = 0; k < 6; ++k) acc[k] += ((volatile double*)partial)[8 * (size_t)b + k];
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) g->props[k] = red[k][0];
+    assemble(ep, g);
+    g->ticket = 0;
+  }
+}
+
+__device__ __forceinline__ float cotf_at(const FaceF& F, int c) { return c == 0 ? F.c0 : (c == 1 ? F.c1 : F.c2); }
+
+__global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __restrict__ fd,
+                                               const EdgeF* __restrict__ ed, const float* __restrict__ rho,
+                                               const float* __restrict__ repg, const Globals* __restrict__ g, EP ep,
+                                               double* __restrict__ grad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.nv) return;
+  const float gA = (float)g->gA, gV = (float)g->gV, gC = (float)g->gC;
+  const float kb = (float)ep.kb, kt = (float)ep.kt, a0 = (float)ep.a0;
+  const float hgC = 0.5f * gC;
+  const float kb23 = kb * (2.0f / 3.0f);
+  float ri = rho[i];
+  f3 acc = (float)ep.kr * f3{repg[3 * i], repg[3 * i + 1], repg[3 * i + 2]};
+  int d = t.val[i];
+  if (d > 0) {
+    const size_t nv = t.nv;
+    // neighbour positions relative to x_i (accurate small vectors)
+    int4 sp = t.slot[(size_t)(d - 1) * nv + i];
+    f3 xk = S.diff(sp.x, i);
+    float rk = rho[sp.x];
+    int4 sc = t.slot[i];
+    f3 xj = S.diff(sc.x, i);
+    float rj = rho[sc.x];
+    FaceF Fc;
+    int fcur = slot_face(sc.y);
+    if (fcur >= 0) Fc = fd[fcur];
+    f3 xi_abs = S.h(i);
+    for (int m = 0; m < d; ++m) {
+      int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
+      int fnx = slot_face(sn.y);
+      FaceF Fn;
+      if (fnx >= 0) Fn = fd[fnx];
+      if (fcur >= 0) {
+        int ci = slot_corner(sc.y);
+        float cj = cotf_at(Fc, ci == 2 ? 0 : ci + 1);
+        float ck = cotf_at(Fc, ci == 0 ? 2 : ci - 1);
+        f3 n = {Fc.nx, Fc.ny, Fc.nz};
+        float alpha = gA - kb23 * (ri * ri + rj * rj + rk * rk);
+        if (ep.btype == 1) alpha += kt * 2.0f * (Fc.A / a0 - 1.0f) / a0;
+        acc += (0.5f * alpha) * fcross(n, xk - xj);
+        // (x_j x x_k)/6 with x = x_i + d: x_i x (d_k - d_j) + d_j x d_k
+        f3 vj = fcross(xi_abs, xk - xj) + fcross(xj, xk);
+        acc += (gV * (1.0f / 6.0f)) * vj;
+        EdgeF E = ed[sc.z];
+        float w = hgC + kb * (ri + rj);
+        float cl = w * E.th + (ep.btype == 0 ? kt * E.db : 0.0f);
+        acc += (-cl / E.l) * xj;
+        if (E.flag != 0.0f) {
+          int cin = slot_corner(sn.y);
+          float cjn = cotf_at(Fn, cin == 0 ? 2 : cin - 1);
+          acc += w * (cj * n + cjn * f3{Fn.nx, Fn.ny, Fn.nz});
+        }
+        if (ed[sc.w].flag != 0.0f) {
+          float wo = hgC + kb * (rj + rk);
+          acc += (-wo * (cj + ck)) * n;
+        }
+      }
+      xk = xj;
+      rk = rj;
+      sc = sn;
+      fcur = fnx;
+      Fc = Fn;
+      xj = S.diff(sn.x, i);
+      rj = rho[sn.x];
+    }
+  }
+  grad[3 * i] = acc.x;
+  grad[3 * i + 1] = acc.y;
+  grad[3 * i + 2] = acc.z;
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+void energy_eval32(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool want_vprops, double* d_grad,
+                   cudaStream_t s, cudaEvent_t* ev) {
+  e->ensure(m->nv, m->ne, m->nf);
+  size_t nv = std::max(m->nv, 1), ne = std::max(m->ne, 1), nf = std::max(m->nf, 1);
+  // FP32 records live in the FP64 buffers (they are smaller)
+  Topo t = m->topo();
+  EP ep = make_ep(e);
+  e->pos32.ensure(3 * nv);
+  float* lo = reinterpret_cast<float*>(e->vprops.get());  // 6*nv doubles >= 3*nv floats
+  Split S{e->pos32.get(), lo};
+  FaceF* fd = reinterpret_cast<FaceF*>(e->face.get());
+  EdgeF* ed = reinterpret_cast<EdgeF*>(e->edge.get());
+  float* eb = reinterpret_cast<float*>(e->ebond.get());
+  float* rho = reinterpret_cast<float*>(e->rho.get());
+  float* repg = reinterpret_cast<float*>(e->repg.get());
+  (void)nf;
+  (void)ne;
+  if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
+  if (m->nv) k_split<<<nblk(3L * m->nv, 256), 256, 0, s>>>(m->nv, P, e->pos32.get(), lo);
+  TM_LAUNCH();
+  if (t.nf) k_face32<<<nblk(t.nf, 256), 256, 0, s>>>(t, S, fd);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
+  if (t.ne) k_edge32<<<nblk(t.ne, 256), 256, 0, s>>>(t, S, fd, ed, eb, ep);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
+  NLView nlv = e->nl.view;
+  nlv.pos32 = e->pos32.get();
+  int nb = std::max(1, nblk(t.nv, VB));
+  // per-vertex properties would overwrite the lo parts: they are only
+  // requested through the FP64 path
+  (void)want_vprops;
+  if (want_grad)
+    k_vertex32<true, false><<<nb, VB, 0, s>>>(t, P, S, fd, ed, eb, nlv, ep, rho, repg, nullptr,
+                                               e->partials.get(), e->glob.get());
+  else
+    k_vertex32<false, false><<<nb, VB, 0, s>>>(t, P, S, fd, ed, eb, nlv, ep, rho, repg, nullptr,
+                                                e->partials.get(), e->glob.get());
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
+  if (want_grad && t.nv) k_grad32<<<nblk(t.nv, 256), 256, 0, s>>>(t, S, fd, ed, rho, repg, e->glob.get(), ep, d_grad);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[4], s));
+}
+
+}  // namespace tmg

@@ -114,23 +114,40 @@ __global__ void k_bbox(int nv, const double* P, double* part) {
 }
 
 // Bounding box with the reference's initial values, then r_list, shape and
-// strides exactly like src/nlists/cell_list.h:56-65.
+// strides exactly like src/nlists/cell_list.h:56-65.  One block reduces the
+// block partials (min/max are exact, so the order does not matter).
 __global__ void k_bbox_final(int nb, const double* part, double rlist, NLGeom* G) {
-  if (threadIdx.x || blockIdx.x) return;
+  __shared__ double s[6][BB];
   double lo[3] = {DBL_MAX, 0.0, 0.0}, hi[3] = {-1.0, 0.0, 0.0};
-  for (int b = 0; b < nb; ++b)
+  for (int b = threadIdx.x; b < nb; b += BB)
     for (int k = 0; k < 3; ++k) {
       double a = part[6 * b + k], c = part[6 * b + 3 + k];
       if (a < lo[k]) lo[k] = a;
       if (c > hi[k]) hi[k] = c;
     }
+  for (int k = 0; k < 3; ++k) {
+    s[k][threadIdx.x] = lo[k];
+    s[3 + k][threadIdx.x] = hi[k];
+  }
+  __syncthreads();
+  for (int o = BB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 3; ++k) {
+        double a = s[k][threadIdx.x + o];
+        if (a < s[k][threadIdx.x]) s[k][threadIdx.x] = a;
+        double c = s[3 + k][threadIdx.x + o];
+        if (c > s[3 + k][threadIdx.x]) s[3 + k][threadIdx.x] = c;
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x) return;
   const double box_eps = 1.0e-6;
   for (int k = 0; k < 3; ++k) {
-    double dim = __dadd_rn(__dsub_rn(hi[k], lo[k]), box_eps);
+    double dim = __dadd_rn(__dsub_rn(s[3 + k][0], s[k][0]), box_eps);
     int nk = (int)__ddiv_rn(dim, rlist);
     G->rl[k] = nk > 0 ? __ddiv_rn(dim, (double)nk) : dim;
     G->shape[k] = nk > 0 ? nk : 1;
-    G->bmin[k] = lo[k];
+    G->bmin[k] = s[k][0];
   }
   G->stride[0] = 1;
   G->stride[1] = G->shape[0];
@@ -450,7 +467,7 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
     k_bbox<<<nb, BB, 0, s>>>(nv, P, nl->bbox.get());
     TM_LAUNCH();
   }
-  k_bbox_final<<<1, 1, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
+  k_bbox_final<<<1, BB, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
   TM_LAUNCH();
   // 2. hash table of the non-empty cells: 2x the vertex count, power of two
   size_t tsize = 64;

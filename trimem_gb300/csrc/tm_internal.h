@@ -186,6 +186,10 @@ void energy_eval(tm_energy* e, tm_mesh* m, const double* d_points, bool want_gra
 // same, recording ev[0..4] around the face, edge, vertex and gradient kernels
 void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, bool want_vprops,
                         double* d_grad, cudaStream_t s, cudaEvent_t* ev);
+// FP32-stencil variant (stencil mode 1); per-vertex properties are not
+// produced by it
+void energy_eval32(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, bool want_vprops,
+                   double* d_grad, cudaStream_t s, cudaEvent_t* ev);
 void energy_from_props_device(tm_energy* e, const double* d_props6, double* d_out8, cudaStream_t s);
 // nlist.cu
 void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* d_points, cudaStream_t s);
