@@ -108,8 +108,10 @@ int tm_energy_components(tm_energy* e, tm_mesh* m, double* out7);
 int tm_energy_gradient(tm_energy* e, tm_mesh* m, double* grad, double* energy);
 int tm_energy_update_reference_properties(tm_energy* e);
 int tm_energy_update_repulsion(tm_energy* e, tm_mesh* m);
-/* Local stencil precision: 0 FP64 (default), 1 FP32 (FP64 differences of
- * positions and FP64 global sums). */
+/* Local stencil precision: 0 FP64 (default), 1 FP32 (positions split into
+ * float hi/lo parts, FP64 global sums), 2 double-float (pairs of floats on
+ * the FP32 pipe, ~48-bit significands; FP64 global sums, exact pair tests).
+ * Per-vertex properties are always computed with the FP64 stencil. */
 int tm_energy_set_stencil_precision(tm_energy* e, int mode);
 
 /* Device-resident evaluation: positions, gradient and energy live in device
@@ -123,6 +125,17 @@ int tm_energy_eval_device(tm_energy* e, tm_mesh* m, const double* d_points, doub
  * Synchronises.  A measurement aid, no counterpart in the reference. */
 int tm_energy_eval_timed(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, float* ms5,
                          void* stream);
+/* Size of the device scratch array used by tm_energy_eval_device_noalloc. */
+#define TM_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+/* tm_energy_eval_device (FP64 stencil) for callers that must not allocate
+ * device memory during the evaluation: the scratch lives in one file-scope
+ * device array of TM_NOALLOC_SCRATCH_BYTES (about 57,000 vertices; larger
+ * meshes are rejected with TM_ERR_ARG) instead of the energy manager's
+ * buffers.  The first call on a device looks up the array's address and must
+ * precede any stream capture; calls that overlap on the GPU share the array
+ * and race.  No counterpart in the reference. */
+int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
+                                  double* d_energy, void* stream);
 /* Rebuilds the neighbour list from device-resident positions. */
 int tm_energy_update_repulsion_device(tm_energy* e, tm_mesh* m, const double* d_points, void* stream);
 

@@ -86,6 +86,7 @@ _SIGS = {
     "tm_energy_eval_device": (_i32, [_p, _p, _p, _p, _p, _p]),
     "tm_energy_update_repulsion_device": (_i32, [_p, _p, _p, _p]),
     "tm_energy_eval_timed": (_i32, [_p, _p, _p, _p, ctypes.POINTER(ctypes.c_float), _p]),
+    "tm_energy_eval_device_noalloc": (_i32, [_p, _p, _p, _p, _p, _p]),
     "tm_nlist_create": (_i32, [_p, ctypes.POINTER(Params), _pp]),
     "tm_nlist_destroy": (_i32, [_p]),
     "tm_nlist_distance_matrix": (_i32, [_p, _p, _d, _i64p]),

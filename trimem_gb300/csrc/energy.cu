@@ -325,6 +325,10 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
     energy_eval32(e, m, P, want_grad, want_vprops, d_grad, s, ev);
     return;
   }
+  if (e->stencil == 2 && !want_vprops) {
+    energy_eval_df(e, m, P, want_grad, d_grad, s, ev);
+    return;
+  }
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
   e->ensure(m->nv, m->ne, m->nf);
   Topo t = m->topo();
@@ -532,7 +536,7 @@ int tm_energy_update_repulsion(tm_energy* e, tm_mesh* m) {
 int tm_energy_set_stencil_precision(tm_energy* e, int mode) {
   TM_API_BEGIN
   if (!e) fail(TM_ERR_ARG, "NULL handle");
-  if (mode != 0 && mode != 1) fail(TM_ERR_ARG, "mode must be 0 (FP64) or 1 (FP32)");
+  if (mode < 0 || mode > 2) fail(TM_ERR_ARG, "mode must be 0 (FP64), 1 (FP32) or 2 (double-float)");
   e->stencil = mode;
   TM_API_END
 }
@@ -591,3 +595,98 @@ int tm_fd_gradient(tm_mesh* m, tm_energy* e, double eps, double* grad) {
 }
 
 }  // extern "C"
+
+// --------------------------------------------------------------------------
+// Evaluation without allocation.
+//
+// Some callers cannot call cudaMalloc while they evaluate the energy: a host
+// that runs under a strict device-memory budget owned by someone else (an
+// embedding application or a pool allocator that forbids side allocations),
+// or code that must not enter the CUDA allocator while other streams of the
+// process are busy.  tm_energy_eval_device_noalloc evaluates the FP64 energy
+// and gradient of a mesh whose scratch (face and edge records, per-vertex
+// intermediates, block partials and the reduction state) fits into one
+// file-scope device array of TM_NOALLOC_SCRATCH_BYTES, instead of the energy
+// manager's own buffers.  It allocates nothing and frees nothing.
+//
+// The array's host-side name is only a stand-in for the device symbol, so its
+// device address is looked up with cudaGetSymbolAddress once per device, on
+// the first call made with that device current; make that first call before
+// any stream capture.  All calls share the array and it keeps the last call's
+// contents: each call clears the reduction state it needs at zero, and calls
+// whose executions overlap on the GPU (other streams, other threads) race on
+// the shared scratch and must be serialised by the caller.
+// --------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+static __device__ __align__(256) unsigned char g_noalloc_scratch[TM_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+unsigned char* noalloc_scratch_for_current_device() {
+  int dev = 0;
+  TM_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) fail(TM_ERR_ARG, "device index out of range for the no-alloc scratch");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    TM_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+  }
+  return g_noalloc_ptr[dev];
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+}  // namespace
+
+extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
+                                             double* d_energy, void* stream) {
+  TM_API_BEGIN
+  if (!e || !m || !d_points || !d_grad) fail(TM_ERR_ARG, "NULL argument");
+  const size_t nv = std::max(m->nv, 1), ne = std::max(m->ne, 1), nf = std::max(m->nf, 1);
+  const int nb = std::max(1, (m->nv + VB - 1) / VB);
+  // scratch layout, 256-byte aligned pieces
+  size_t off_face = 0;
+  size_t off_edge = off_face + align256(sizeof(FaceD) * nf);
+  size_t off_ebond = off_edge + align256(sizeof(EdgeD) * ne);
+  size_t off_rho = off_ebond + align256(sizeof(double) * ne);
+  size_t off_repg = off_rho + align256(sizeof(double) * nv);
+  size_t off_pos32 = off_repg + align256(3 * sizeof(double) * nv);
+  size_t off_part = off_pos32 + align256(3 * sizeof(float) * nv);
+  size_t off_glob = off_part + align256(8 * sizeof(double) * nb);
+  size_t need = off_glob + align256(sizeof(Globals));
+  if (need > (size_t)TM_NOALLOC_SCRATCH_BYTES)
+    fail(TM_ERR_ARG, "mesh needs " + std::to_string(need) + " bytes of scratch, more than the " +
+                         std::to_string((size_t)TM_NOALLOC_SCRATCH_BYTES) +
+                         " bytes of tm_energy_eval_device_noalloc (about 57,000 vertices)");
+  unsigned char* base = noalloc_scratch_for_current_device();
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  FaceD* fd = reinterpret_cast<FaceD*>(base + off_face);
+  EdgeD* ed = reinterpret_cast<EdgeD*>(base + off_edge);
+  double* ebond = reinterpret_cast<double*>(base + off_ebond);
+  double* rho = reinterpret_cast<double*>(base + off_rho);
+  double* repg = reinterpret_cast<double*>(base + off_repg);
+  float* pos32 = reinterpret_cast<float*>(base + off_pos32);
+  double* part = reinterpret_cast<double*>(base + off_part);
+  Globals* g = reinterpret_cast<Globals*>(base + off_glob);
+  // the block ticket of the reduction must start at zero
+  TM_CUDA(cudaMemsetAsync(g, 0, sizeof(Globals), s));
+  Topo t = m->topo();
+  EP ep = make_ep(e);
+  NLView nlv = e->nl.view;
+  nlv.pos32 = pos32;
+  int nfb = std::max(nblk(std::max(t.nf, t.nv), 256), 1);
+  k_face<<<nfb, 256, 0, s>>>(t, d_points, fd, pos32);
+  TM_LAUNCH();
+  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, d_points, fd, ed, ebond, ep);
+  TM_LAUNCH();
+  k_vertex<true, false><<<nb, VB, 0, s>>>(t, d_points, fd, ed, ebond, nlv, ep, rho, repg, nullptr, part, g);
+  TM_LAUNCH();
+  if (t.nv) k_grad<<<nblk(t.nv, 256), 256, 0, s>>>(t, d_points, fd, ed, rho, repg, g, ep, d_grad);
+  TM_LAUNCH();
+  if (d_energy) TM_CUDA(cudaMemcpyAsync(d_energy, &g->comps[6], sizeof(double), cudaMemcpyDeviceToDevice, s));
+  TM_API_END
+}
