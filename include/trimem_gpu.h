@@ -129,7 +129,7 @@ int tm_energy_eval_timed(tm_energy* e, tm_mesh* m, const double* d_points, doubl
 #define TM_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
 /* tm_energy_eval_device (FP64 stencil) for callers that must not allocate
  * device memory during the evaluation: the scratch lives in one file-scope
- * device array of TM_NOALLOC_SCRATCH_BYTES (about 57,000 vertices; larger
+ * device array of TM_NOALLOC_SCRATCH_BYTES (about 55,000 vertices; larger
  * meshes are rejected with TM_ERR_ARG) instead of the energy manager's
  * buffers.  The first call on a device looks up the array's address and must
  * precede any stream capture; calls that overlap on the GPU share the array

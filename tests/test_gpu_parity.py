@@ -54,11 +54,14 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("stencil", [0, 2], ids=["fp64", "df64"])
 @pytest.mark.parametrize("name,level,kw", CASES, ids=[c[0] for c in CASES])
-def test_energy_and_gradient_parity(C, name, level, kw):
+def test_energy_and_gradient_parity(C, name, level, kw, stencil):
+    """FP64 and double-float stencils against the oracle, 1e-10 relative."""
     p, f = meshgen.jittered_icosphere(level, seed=level)
     prm = workload_params(p, f, **kw)
     mo, eo, mg, eg = _pair(C, p, f, prm)
+    eg.set_stencil_precision(stencil)
     np.testing.assert_allclose(eg.initial_props(), eo.initial_props(), rtol=RTOL, atol=0)
     # move the vertices after construction: the cell list keeps its bins
     rng = np.random.default_rng(7)
@@ -219,13 +222,15 @@ def test_utilities(C):
     assert abs(a - O.area(mo) / mo.n_faces()) <= RTOL * a
 
 
-def test_large_mesh_properties(C):
+@pytest.mark.parametrize("stencil", [0, 2], ids=["fp64", "df64"])
+def test_large_mesh_properties(C, stencil):
     """Level-6 icosphere (40,962 vertices): parity with the oracle and the
     size-independent invariances (closed surface: translation leaves the
     energy unchanged, so the gradient sums to zero)."""
     p, f = meshgen.jittered_icosphere(6, seed=0)
     prm = workload_params(p, f)
     mo, eo, mg, eg = _pair(C, p, f, prm)
+    eg.set_stencil_precision(stencil)
     e, g = eg.gradient(mg, with_energy=True)
     assert abs(e - eo.energy(mo)) <= RTOL * abs(e)
     assert rel(g, eo.gradient(mo)) < RTOL

@@ -572,8 +572,8 @@ PYBIND11_MODULE(core, m) {
       .def(
           "set_stencil_precision",
           [](EnergyManager& e, const std::string& p) {
-            int mode = p == "fp64" ? 0 : (p == "fp32" ? 1 : -1);
-            if (mode < 0) throw py::value_error("precision must be 'fp64' or 'fp32'");
+            int mode = p == "fp64" ? 0 : (p == "fp32" ? 1 : (p == "df64" ? 2 : -1));
+            if (mode < 0) throw py::value_error("precision must be 'fp64', 'fp32' or 'df64'");
             check(tm_energy_set_stencil_precision(e.h, mode));
           },
           py::arg("precision"))

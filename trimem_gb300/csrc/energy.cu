@@ -121,12 +121,11 @@ __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __rest
   ebond[e] = val;
 }
 
-template <bool GRAD, bool VPROPS>
-__global__ void __launch_bounds__(VB) k_vertex(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd,
-                                              const EdgeD* __restrict__ ed, const double* __restrict__ ebond,
-                                              NLView nl, EP ep, double* __restrict__ rho, double* __restrict__ repg,
-                                              double* __restrict__ vprops, double* __restrict__ partial,
-                                              Globals* g) {
+template <bool VPROPS>
+__global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__ fd, const EdgeD* __restrict__ ed,
+                                              const double* __restrict__ ebond, const double* __restrict__ reppot,
+                                              EP ep, double* __restrict__ rho, double* __restrict__ vprops,
+                                              double* __restrict__ partial, Globals* g) {
   __shared__ double red[6][VB];
   __shared__ bool last;
   int v = blockIdx.x * VB + threadIdx.x;
@@ -156,25 +155,8 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const double* __restrict_
     pr[2] = c;
     pr[3] = 2 * c * c / a;
     pr[4] = T / ep.tdiv;
-    d3 p = ld3(P, v);
-    double pot = 0.0;
-    d3 gr = mk(0, 0, 0);
-    const double lc1 = ep.rlc1;
-    const int rr = ep.rr;
-    for_each_neighbour(nl, t, P, v, p, lc1, ep.rT, [&](int, double l, d3 dvec) {
-      double lmc = l - lc1;
-      double ex = exp(l / lmc);
-      pot += ex / ipow(l, rr);
-      if (GRAD) {
-        double fac = -(lc1 / (lmc * lmc) + rr / l);
-        fac /= ipow(l, rr + 1);
-        fac *= ex;
-        gr += fac * dvec;
-      }
-    });
-    pr[5] = pot;
+    pr[5] = reppot[v];
     rho[v] = c / a;
-    if (GRAD) st3(repg, v, 2.0 * gr);
     if (VPROPS)
       for (int k = 0; k < 6; ++k) vprops[6 * (size_t)v + k] = pr[k];
   }
@@ -344,19 +326,15 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
   if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
+  repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
+                 e->slow.get() + std::max(m->nv, 1), s);
   int nb = std::max(1, nblk(t.nv, VB));
-#define TM_KV(G, VP)                                                                                         \
-  k_vertex<G, VP><<<nb, VB, 0, s>>>(t, P, fd, ed, e->ebond.get(), nlv, ep, e->rho.get(), e->repg.get(), \
-                                    e->vprops.get(), e->partials.get(), e->glob.get())
-  if (want_grad && want_vprops)
-    TM_KV(true, true);
-  else if (want_grad)
-    TM_KV(true, false);
-  else if (want_vprops)
-    TM_KV(false, true);
+  if (want_vprops)
+    k_vertex<true><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, e->rho.get(),
+                                     e->vprops.get(), e->partials.get(), e->glob.get());
   else
-    TM_KV(false, false);
-#undef TM_KV
+    k_vertex<false><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, e->rho.get(), nullptr,
+                                      e->partials.get(), e->glob.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
   if (want_grad && t.nv)
@@ -383,6 +361,8 @@ void tm_energy::ensure(int nv_, int ne_, int nf_) {
   ebond.ensure(std::max(ne, 1));
   rho.ensure(std::max(nv, 1));
   repg.ensure(3 * (size_t)std::max(nv, 1));
+  reppot.ensure(std::max(nv, 1));
+  slow.ensure((size_t)std::max(nv, 1) + 1);
   vprops.ensure(6 * (size_t)std::max(nv, 1));
   pos32.ensure(3 * (size_t)std::max(nv, 1));
   int nb = std::max(1, (nv + tmg::VB - 1) / tmg::VB);
@@ -655,13 +635,15 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   size_t off_rho = off_ebond + align256(sizeof(double) * ne);
   size_t off_repg = off_rho + align256(sizeof(double) * nv);
   size_t off_pos32 = off_repg + align256(3 * sizeof(double) * nv);
-  size_t off_part = off_pos32 + align256(3 * sizeof(float) * nv);
+  size_t off_pot = off_pos32 + align256(3 * sizeof(float) * nv);
+  size_t off_slow = off_pot + align256(sizeof(double) * nv);
+  size_t off_part = off_slow + align256(sizeof(int) * (nv + 1));
   size_t off_glob = off_part + align256(8 * sizeof(double) * nb);
   size_t need = off_glob + align256(sizeof(Globals));
   if (need > (size_t)TM_NOALLOC_SCRATCH_BYTES)
     fail(TM_ERR_ARG, "mesh needs " + std::to_string(need) + " bytes of scratch, more than the " +
                          std::to_string((size_t)TM_NOALLOC_SCRATCH_BYTES) +
-                         " bytes of tm_energy_eval_device_noalloc (about 57,000 vertices)");
+                         " bytes of tm_energy_eval_device_noalloc (about 55,000 vertices)");
   unsigned char* base = noalloc_scratch_for_current_device();
   cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
   FaceD* fd = reinterpret_cast<FaceD*>(base + off_face);
@@ -670,6 +652,8 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   double* rho = reinterpret_cast<double*>(base + off_rho);
   double* repg = reinterpret_cast<double*>(base + off_repg);
   float* pos32 = reinterpret_cast<float*>(base + off_pos32);
+  double* reppot = reinterpret_cast<double*>(base + off_pot);
+  int* slow = reinterpret_cast<int*>(base + off_slow);
   double* part = reinterpret_cast<double*>(base + off_part);
   Globals* g = reinterpret_cast<Globals*>(base + off_glob);
   // the block ticket of the reduction must start at zero
@@ -683,7 +667,8 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   TM_LAUNCH();
   if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, d_points, fd, ed, ebond, ep);
   TM_LAUNCH();
-  k_vertex<true, false><<<nb, VB, 0, s>>>(t, d_points, fd, ed, ebond, nlv, ep, rho, repg, nullptr, part, g);
+  repulsion_eval(e, m, d_points, pos32, true, reppot, repg, slow, slow + nv, s);
+  k_vertex<false><<<nb, VB, 0, s>>>(t, fd, ed, ebond, reppot, ep, rho, nullptr, part, g);
   TM_LAUNCH();
   if (t.nv) k_grad<<<nblk(t.nv, 256), 256, 0, s>>>(t, d_points, fd, ed, rho, repg, g, ep, d_grad);
   TM_LAUNCH();

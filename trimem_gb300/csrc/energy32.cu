@@ -134,12 +134,9 @@ __global__ void k_edge32(Topo t, Split S, const FaceF* __restrict__ fd, EdgeF* _
   ebond[e] = val;
 }
 
-template <bool GRAD, bool VPROPS>
-__global__ void __launch_bounds__(VB) k_vertex32(Topo t, const double* __restrict__ P, Split S,
-                                                const FaceF* __restrict__ fd, const EdgeF* __restrict__ ed,
-                                                const float* __restrict__ ebond, NLView nl, EP ep,
-                                                float* __restrict__ rho, float* __restrict__ repg,
-                                                double* __restrict__ vprops, double* __restrict__ partial,
+__global__ void __launch_bounds__(VB) k_vertex32(Topo t, const FaceF* __restrict__ fd, const EdgeF* __restrict__ ed,
+                                                const float* __restrict__ ebond, const double* __restrict__ reppot,
+                                                EP ep, float* __restrict__ rho, double* __restrict__ partial,
                                                 Globals* g) {
   __shared__ double red[6][VB];
   __shared__ bool last;
@@ -170,32 +167,8 @@ __global__ void __launch_bounds__(VB) k_vertex32(Topo t, const double* __restric
     pr[2] = c;
     pr[3] = 2 * c * c / a;
     pr[4] = T / (float)ep.tdiv;
-    d3 p = ld3(P, v);
-    float pot = 0.0f;
-    f3 gr = {0, 0, 0};
-    const float lc1 = (float)ep.rlc1;
-    const int rr = ep.rr;
-    for_each_neighbour(nl, t, P, v, p, ep.rlc1, ep.rT, [&](int j, double ld, d3) {
-      float l = (float)ld;
-      float lmc = l - lc1;
-      float ex = expf(l / lmc);
-      pot += ex / fipow(l, rr);
-      if (GRAD) {
-        float fac = -(lc1 / (lmc * lmc) + rr / l);
-        fac /= fipow(l, rr + 1);
-        fac *= ex;
-        gr += fac * S.diff(v, j);
-      }
-    });
-    pr[5] = pot;
+    pr[5] = reppot[v];
     rho[v] = c / a;
-    if (GRAD) {
-      repg[3 * v] = 2.0f * gr.x;
-      repg[3 * v + 1] = 2.0f * gr.y;
-      repg[3 * v + 2] = 2.0f * gr.z;
-    }
-    if (VPROPS)
-      for (int k = 0; k < 6; ++k) vprops[6 * (size_t)v + k] = pr[k];
   }
   for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = pr[k];
   __syncthreads();
@@ -234,7 +207,7 @@ __device__ __forceinline__ float cotf_at(const FaceF& F, int c) { return c == 0 
 
 __global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __restrict__ fd,
                                                const EdgeF* __restrict__ ed, const float* __restrict__ rho,
-                                               const float* __restrict__ repg, const Globals* __restrict__ g, EP ep,
+                                               const double* __restrict__ repg, const Globals* __restrict__ g, EP ep,
                                                double* __restrict__ grad) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= t.nv) return;
@@ -243,7 +216,7 @@ __global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __
   const float hgC = 0.5f * gC;
   const float kb23 = kb * (2.0f / 3.0f);
   float ri = rho[i];
-  f3 acc = (float)ep.kr * f3{repg[3 * i], repg[3 * i + 1], repg[3 * i + 2]};
+  f3 acc = (float)ep.kr * f3{(float)repg[3 * i], (float)repg[3 * i + 1], (float)repg[3 * i + 2]};
   int d = t.val[i];
   if (d > 0) {
     const size_t nv = t.nv;
@@ -320,7 +293,7 @@ void energy_eval32(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bo
   EdgeF* ed = reinterpret_cast<EdgeF*>(e->edge.get());
   float* eb = reinterpret_cast<float*>(e->ebond.get());
   float* rho = reinterpret_cast<float*>(e->rho.get());
-  float* repg = reinterpret_cast<float*>(e->repg.get());
+  double* repg = e->repg.get();
   (void)nf;
   (void)ne;
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
@@ -332,18 +305,11 @@ void energy_eval32(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bo
   if (t.ne) k_edge32<<<nblk(t.ne, 256), 256, 0, s>>>(t, S, fd, ed, eb, ep);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
-  NLView nlv = e->nl.view;
-  nlv.pos32 = e->pos32.get();
+  repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), repg, e->slow.get(),
+                 e->slow.get() + std::max(m->nv, 1), s);
   int nb = std::max(1, nblk(t.nv, VB));
-  // per-vertex properties would overwrite the lo parts: they are only
-  // requested through the FP64 path
   (void)want_vprops;
-  if (want_grad)
-    k_vertex32<true, false><<<nb, VB, 0, s>>>(t, P, S, fd, ed, eb, nlv, ep, rho, repg, nullptr,
-                                               e->partials.get(), e->glob.get());
-  else
-    k_vertex32<false, false><<<nb, VB, 0, s>>>(t, P, S, fd, ed, eb, nlv, ep, rho, repg, nullptr,
-                                                e->partials.get(), e->glob.get());
+  k_vertex32<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), ep, rho, e->partials.get(), e->glob.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
   if (want_grad && t.nv) k_grad32<<<nblk(t.nv, 256), 256, 0, s>>>(t, S, fd, ed, rho, repg, e->glob.get(), ep, d_grad);

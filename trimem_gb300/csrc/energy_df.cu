@@ -1,0 +1,334 @@
+// Double-float stencil variant of the energy / gradient evaluation
+// (tm_energy_set_stencil_precision(e, 2)).
+//
+// The FP64 kernels of energy.cu run the FP64 pipe at ~87% (measured), and on
+// GB300 that pipe retires 1/58 of the FP32 rate.  These kernels compute the
+// same quantities with double-float numbers (df64.cuh: pairs of floats,
+// ~48-bit significands, error-free transformations on the FP32 pipe):
+//   * positions are split once per evaluation into float hi/lo parts; edge
+//     vectors are double-float differences, so |x| >> |x_b - x_a| costs no
+//     accuracy;
+//   * face records, edge records, vertex sums and the gradient gather are
+//     double-float; the dihedral angle is atan2(|n0 x n1|, n0 . n1) refined
+//     from a float estimate (FP64 atan2 only above 0.8 rad);
+//   * FP64 stays for the flat-bottom potentials outside the flat bottom,
+//     the repulsion pairs (exact pair decisions), the global sums and the
+//     penalty assembly.
+// The results agree with the FP64 oracle to ~1e-13 relative (the 1e-10 bound
+// of the parity tests); they are not bitwise equal to the FP64 kernels.
+#include <algorithm>
+#include <cmath>
+
+#include "df64.cuh"
+#include "tm_energy.cuh"
+#include "tm_internal.h"
+#include "tm_math.cuh"
+
+namespace tmg {
+
+struct __align__(16) FaceDF {
+  df nx, ny, nz, A, V, c0, c1, c2;
+};
+struct __align__(16) EdgeDF {
+  df l, th, db, flag;
+};
+
+namespace {
+
+// double-float constants 1/3 and 1/6 (hi = float(c), lo = float(c - hi))
+__device__ __forceinline__ df third() { return {3.333333433e-01f, -9.934107481e-09f}; }
+__device__ __forceinline__ df sixth() { return {1.666666716e-01f, -4.967053740e-09f}; }
+
+struct PosDF {
+  const float* hi;
+  const float* lo;
+  __device__ __forceinline__ df3 at(int v) const {
+    return {{hi[3 * v], lo[3 * v]}, {hi[3 * v + 1], lo[3 * v + 1]}, {hi[3 * v + 2], lo[3 * v + 2]}};
+  }
+};
+
+// double-float parameters (hi/lo from the host)
+struct EPD {
+  df kb, kt, kr, kb23, a0, inv_a0, inv_tdiv;
+};
+
+__global__ void k_split_df(int n3, const double* __restrict__ P, float* __restrict__ hi, float* __restrict__ lo) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  double x = P[i];
+  float h = (float)x;
+  hi[i] = h;
+  lo[i] = (float)(x - (double)h);
+}
+
+__global__ void __launch_bounds__(256) k_face_df(Topo t, PosDF X, FaceDF* __restrict__ fd) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= t.nf) return;
+  int a = t.fv[3 * f], b = t.fv[3 * f + 1], c = t.fv[3 * f + 2];
+  df3 pa = X.at(a), pb = X.at(b), pc = X.at(c);
+  df3 eab = pb - pa, eac = pc - pa, ebc = pc - pb;
+  df3 N = dcross(eab, eac);
+  df nn = df_sqrt(ddot(N, N));
+  df inv = df_make(1.0f) / nn;
+  FaceDF F;
+  F.nx = inv * N.x;
+  F.ny = inv * N.y;
+  F.nz = inv * N.z;
+  F.A = ldexp2(nn, 0.5f);
+  F.V = ddot(pa, N) * sixth();
+  F.c0 = ddot(eab, eac) * inv;
+  F.c1 = -(ddot(eab, ebc) * inv);
+  F.c2 = ddot(eac, ebc) * inv;
+  fd[f] = F;
+}
+
+__global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* __restrict__ fd,
+                                                EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.ne) return;
+  int4 E = t.edge[e];
+  df3 ev = X.at(E.y) - X.at(E.x);
+  df l = df_sqrt(ddot(ev, ev));
+  EdgeDF o;
+  o.l = l;
+  o.th = df_make(0.0f);
+  o.flag = df_make(0.0f);
+  if (E.z >= 0 && E.w >= 0) {
+    const FaceDF& F0 = fd[E.z];
+    const FaceDF& F1 = fd[E.w];
+    df3 n0 = {F0.nx, F0.ny, F0.nz}, n1 = {F1.nx, F1.ny, F1.nz};
+    df3 cr = dcross(n0, n1);
+    df c = ddot(n0, n1);
+    df sn = df_sqrt(ddot(cr, cr));
+    df th;
+    if (!df_atan2_pos(sn, c, &th)) th = df_from(atan2(df_to(sn), df_to(c)));
+    o.th = df_lt0(ddot(cr, ev)) ? -th : th;
+    o.flag = df_make(1.0f);
+  }
+  // flat-bottom edge penalty (src/mesh_tether.h:29-85), FP64 outside the
+  // flat bottom
+  double val = 0.0, fac = 0.0;
+  if (ep.btype == 0) {
+    double ld = df_to(l);
+    int r = ep.r;
+    if (ld > ep.lc0) {
+      val = ipow((double)r, r + 1) * ipow(ld - ep.lc0, r);
+      fac = ipow((double)r, r + 2) * ipow(ld - ep.lc0, r - 1);
+    } else if (ld < ep.lc1) {
+      val = exp(ld / (ld - ep.lc1)) / ipow(ld, r);
+    }
+    if (ld < ep.lc1) {
+      double lmc = ld - ep.lc1;
+      fac -= ep.lc1 / (lmc * lmc) + r / ld;
+      fac /= ipow(ld, r);
+      fac *= exp(ld / lmc);
+    }
+  }
+  o.db = val == 0.0 && fac == 0.0 ? df_make(0.0f) : df_from(fac);
+  ed[e] = o;
+  ebond[e] = val == 0.0 ? df_make(0.0f) : df_from(val);
+}
+
+__global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const FaceDF* __restrict__ fd,
+                                                 const EdgeDF* __restrict__ ed, const df* __restrict__ ebond,
+                                                 const double* __restrict__ reppot, EP ep, EPD epd,
+                                                 df* __restrict__ rho, double* __restrict__ partial, Globals* g) {
+  __shared__ float2 red[6][VB];
+  __shared__ double redd[6][VB];
+  __shared__ bool last;
+  int v = blockIdx.x * VB + threadIdx.x;
+  df pr[6];
+  for (int k = 0; k < 6; ++k) pr[k] = df_make(0.0f);
+  if (v < t.nv) {
+    int d = t.val[v];
+    df A = df_make(0.0f), V = df_make(0.0f), LT = df_make(0.0f), T = df_make(0.0f);
+    for (int m = 0; m < d; ++m) {
+      int4 s = t.slot[(size_t)m * t.nv + v];
+      int f = slot_face(s.y);
+      if (f < 0) continue;
+      df fa = fd[f].A;
+      A += fa;
+      V += fd[f].V;
+      EdgeDF E = ed[s.z];
+      LT += E.l * E.th;
+      if (ep.btype == 0) {
+        T += ebond[s.z];
+      } else {
+        df q = fa * epd.inv_a0 - df_make(1.0f);
+        T += q * q;
+      }
+    }
+    df a = A * third(), c = ldexp2(LT, 0.25f);
+    pr[0] = a;
+    pr[1] = V * third();
+    pr[2] = c;
+    pr[3] = ldexp2(c * c, 2.0f) / a;
+    pr[4] = T * epd.inv_tdiv;
+    double pot = reppot[v];
+    pr[5] = pot == 0.0 ? df_make(0.0f) : df_from(pot);
+    rho[v] = c / a;
+  }
+  // fixed-order double-float tree over the block, FP64 across blocks
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = make_float2(pr[k].hi, pr[k].lo);
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) {
+        float2 x = red[k][threadIdx.x], y = red[k][threadIdx.x + o];
+        df z = df{x.x, x.y} + df{y.x, y.y};
+        red[k][threadIdx.x] = make_float2(z.hi, z.lo);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) partial[8 * (size_t)blockIdx.x + k] = df_to(df{red[k][0].x, red[k][0].y});
+    __threadfence();
+    unsigned int tk = atomicAdd(&g->ticket, 1u);
+    last = (tk == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += VB)
+    for (int k = 0; k < 6; ++k) acc[k] += ((volatile double*)partial)[8 * (size_t)b + k];
+  for (int k = 0; k < 6; ++k) redd[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) redd[k][threadIdx.x] += redd[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) g->props[k] = redd[k][0];
+    assemble(ep, g);
+    g->ticket = 0;
+  }
+}
+
+__device__ __forceinline__ df cot_df(const FaceDF& F, int c) { return c == 0 ? F.c0 : (c == 1 ? F.c1 : F.c2); }
+
+__global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* __restrict__ fd,
+                                                const EdgeDF* __restrict__ ed, const df* __restrict__ rho,
+                                                const double* __restrict__ repg, const Globals* __restrict__ g,
+                                                EP ep, EPD epd, double* __restrict__ grad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.nv) return;
+  const df gA = {g->gdf[0], g->gdf[1]}, gV = {g->gdf[2], g->gdf[3]}, gC = {g->gdf[4], g->gdf[5]};
+  const df hgC = ldexp2(gC, 0.5f);
+  const df gV6 = gV * sixth();
+  const df kb = epd.kb;
+  df3 xi = X.at(i);
+  df ri = rho[i];
+  df3 acc = {df_make(0.0f), df_make(0.0f), df_make(0.0f)};
+  int d = t.val[i];
+  if (d > 0) {
+    const size_t nv = t.nv;
+    int4 sp = t.slot[(size_t)(d - 1) * nv + i];
+    df3 dk = X.at(sp.x) - xi;  // x_k - x_i
+    df rk = rho[sp.x];
+    int4 sc = t.slot[i];
+    df3 dj = X.at(sc.x) - xi;
+    df rj = rho[sc.x];
+    int fcur = slot_face(sc.y);
+    for (int m = 0; m < d; ++m) {
+      int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
+      int fnx = slot_face(sn.y);
+      if (fcur >= 0) {
+        const FaceDF& Fc = fd[fcur];
+        int ci = slot_corner(sc.y);
+        df cj = cot_df(Fc, ci == 2 ? 0 : ci + 1);
+        df ck = cot_df(Fc, ci == 0 ? 2 : ci - 1);
+        df3 n = {Fc.nx, Fc.ny, Fc.nz};
+        // face (i, j, k): area and volume terms
+        df alpha = gA - epd.kb23 * (ri * ri + rj * rj + rk * rk);
+        if (ep.btype == 1) alpha += ldexp2(epd.kt * (Fc.A * epd.inv_a0 - df_make(1.0f)) * epd.inv_a0, 2.0f);
+        df3 dkj = dk - dj;
+        acc += ldexp2(alpha, 0.5f) * dcross(n, dkj);
+        // x_j x x_k = x_i x (d_k - d_j) + d_j x d_k
+        acc += gV6 * (dcross(xi, dkj) + dcross(dj, dk));
+        // edge (i, j): length and dihedral terms
+        const EdgeDF& E = ed[sc.z];
+        df w = hgC + kb * (ri + rj);
+        df cl = w * E.th;
+        if (ep.btype == 0) cl += epd.kt * E.db;
+        acc += (-(cl / E.l)) * dj;
+        if (E.flag.hi != 0.0f) {
+          const FaceDF& Fn = fd[fnx];
+          int cin = slot_corner(sn.y);
+          df cjn = cot_df(Fn, cin == 0 ? 2 : cin - 1);
+          df3 nn = {Fn.nx, Fn.ny, Fn.nz};
+          acc += df3{w * (cj * n.x + cjn * nn.x), w * (cj * n.y + cjn * nn.y), w * (cj * n.z + cjn * nn.z)};
+        }
+        // edge (j, k) opposite i: dihedral term
+        if (ed[sc.w].flag.hi != 0.0f) {
+          df wo = hgC + kb * (rj + rk);
+          acc += (-(wo * (cj + ck))) * n;
+        }
+      }
+      dk = dj;
+      rk = rj;
+      sc = sn;
+      fcur = fnx;
+      dj = X.at(sn.x) - xi;
+      rj = rho[sn.x];
+    }
+  }
+  d3 r = ld3(repg, i);
+  grad[3 * i] = df_to(acc.x) + ep.kr * r.x;
+  grad[3 * i + 1] = df_to(acc.y) + ep.kr * r.y;
+  grad[3 * i + 2] = df_to(acc.z) + ep.kr * r.z;
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+df host_df(double x) {
+  float h = (float)x;
+  return {h, (float)(x - (double)h)};
+}
+
+}  // namespace
+
+void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, double* d_grad, cudaStream_t s,
+                    cudaEvent_t* ev) {
+  e->ensure(m->nv, m->ne, m->nf);
+  size_t nv = std::max(m->nv, 1);
+  e->pos32.ensure(3 * nv);
+  e->poslo.ensure(3 * nv);
+  Topo t = m->topo();
+  EP ep = make_ep(e);
+  EPD epd;
+  epd.kb = host_df(ep.kb);
+  epd.kt = host_df(ep.kt);
+  epd.kr = host_df(ep.kr);
+  epd.kb23 = host_df(ep.kb * (2.0 / 3.0));
+  epd.a0 = host_df(ep.a0);
+  epd.inv_a0 = host_df(1.0 / ep.a0);
+  epd.inv_tdiv = host_df(1.0 / ep.tdiv);
+  PosDF X{e->pos32.get(), e->poslo.get()};
+  FaceDF* fd = reinterpret_cast<FaceDF*>(e->face.get());
+  EdgeDF* ed = reinterpret_cast<EdgeDF*>(e->edge.get());
+  df* eb = reinterpret_cast<df*>(e->ebond.get());
+  df* rho = reinterpret_cast<df*>(e->rho.get());
+  if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
+  if (m->nv) k_split_df<<<nblk(3L * m->nv, 256), 256, 0, s>>>(3 * m->nv, P, e->pos32.get(), e->poslo.get());
+  TM_LAUNCH();
+  if (t.nf) k_face_df<<<nblk(t.nf, 256), 256, 0, s>>>(t, X, fd);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
+  if (t.ne) k_edge_df<<<nblk(t.ne, 256), 256, 0, s>>>(t, X, fd, ed, eb, ep);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
+  repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
+                 e->slow.get() + std::max(m->nv, 1), s);
+  int nb = std::max(1, nblk(t.nv, VB));
+  k_vertex_df<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), ep, epd, rho, e->partials.get(), e->glob.get());
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
+  if (want_grad && t.nv)
+    k_grad_df<<<nblk(t.nv, 256), 256, 0, s>>>(t, X, fd, ed, rho, e->repg.get(), e->glob.get(), ep, epd, d_grad);
+  TM_LAUNCH();
+  if (ev) TM_CUDA(cudaEventRecord(ev[4], s));
+}
+
+}  // namespace tmg

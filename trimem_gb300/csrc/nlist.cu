@@ -146,6 +146,7 @@ __global__ void k_bbox_final(int nb, const double* part, double rlist, NLGeom* G
     double dim = __dadd_rn(__dsub_rn(s[3 + k][0], s[k][0]), box_eps);
     int nk = (int)__ddiv_rn(dim, rlist);
     G->rl[k] = nk > 0 ? __ddiv_rn(dim, (double)nk) : dim;
+    G->inv_rl[k] = 1.0 / G->rl[k];
     G->shape[k] = nk > 0 ? nk : 1;
     G->bmin[k] = s[k][0];
   }

@@ -1,0 +1,117 @@
+// Surface repulsion stage of an evaluation (src/mesh_repulsion.h:28-79 over
+// the neighbour list): per vertex the flat-bottom pair potential
+// sum_j exp(l/(l - lc1)) / l^r over the neighbours closer than lc1 and, for a
+// gradient, 2 sum_j phi'(l) (x_i - x_j) / l.
+//
+// A vertex whose current position still lies in its build-time cell walks
+// the precomputed candidate row of that cell (k_rep_fast); the few that moved
+// to another cell are queued and walk the 27 cells through the cell table in
+// a second kernel (k_rep_slow), so the long table walk never holds a warp of
+// fast vertices.  Both produce the per-vertex values in the reference's pair
+// order; the queue order does not matter because each vertex is written by
+// one thread.
+#include <algorithm>
+
+#include "tm_energy.cuh"
+#include "tm_internal.h"
+#include "tm_math.cuh"
+
+namespace tmg {
+namespace {
+
+struct RepAcc {
+  double lc1;
+  int rr;
+  double pot;
+  d3 gr;
+  bool grad;
+  __device__ void operator()(int, double l, d3 dvec) {
+    double lmc = l - lc1;
+    double ex = exp(l / lmc);
+    pot += ex / ipow(l, rr);
+    if (grad) {
+      double fac = -(lc1 / (lmc * lmc) + rr / l);
+      fac /= ipow(l, rr + 1);
+      fac *= ex;
+      gr += fac * dvec;
+    }
+  }
+};
+
+template <bool GRAD>
+__global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restrict__ P, NLView nl, EP ep,
+                                                 double* __restrict__ pot, double* __restrict__ repg,
+                                                 int* __restrict__ slow, int* __restrict__ nslow) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= t.nv) return;
+  d3 p = ld3(P, v);
+  PairTest pt = make_pair_test(nl, v, ep.rlc1, ep.rT);
+  RepAcc acc{ep.rlc1, ep.rr, 0.0, mk(0, 0, 0), GRAD};
+  TableExcl x{t, nl.excl};
+  if (nl.kind == 0) {
+    int co[3];
+    if (!in_build_cell(nl, v, p, co)) {
+      slow[atomicAdd(nslow, 1)] = v;
+      return;
+    }
+    visit_candidates(pt, nl, P, v, p, x, acc);
+  } else {
+    visit_verlet(pt, nl, P, v, p, x, acc);
+  }
+  pot[v] = acc.pot;
+  if (GRAD) st3(repg, v, 2.0 * acc.gr);
+}
+
+template <bool GRAD>
+__global__ void __launch_bounds__(256) k_rep_slow(Topo t, const double* __restrict__ P, NLView nl, EP ep,
+                                                 double* __restrict__ pot, double* __restrict__ repg,
+                                                 const int* __restrict__ slow, const int* __restrict__ nslow) {
+  int n = *nslow;
+  TableExcl x{t, nl.excl};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int v = slow[i];
+    d3 p = ld3(P, v);
+    PairTest pt = make_pair_test(nl, v, ep.rlc1, ep.rT);
+    RepAcc acc{ep.rlc1, ep.rr, 0.0, mk(0, 0, 0), GRAD};
+    int co[3];
+    in_build_cell(nl, v, p, co);
+    visit_cells(pt, nl, P, v, p, co, x, acc);
+    pot[v] = acc.pot;
+    if (GRAD) st3(repg, v, 2.0 * acc.gr);
+  }
+}
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos32, bool want_grad,
+                    double* pot, double* repg, int* slow, int* nslow, cudaStream_t s) {
+  int nv = m->nv;
+  if (nv == 0) return;
+  EP ep = make_ep(e);
+  if (!(ep.rlc1 > 0)) {  // no pair can be closer than a non-positive cut-off
+    TM_CUDA(cudaMemsetAsync(pot, 0, sizeof(double) * nv, s));
+    if (want_grad) TM_CUDA(cudaMemsetAsync(repg, 0, sizeof(double) * 3 * nv, s));
+    return;
+  }
+  Topo t = m->topo();
+  NLView nlv = e->nl.view;
+  nlv.pos32 = pos32;
+  TM_CUDA(cudaMemsetAsync(nslow, 0, sizeof(int), s));
+  if (want_grad)
+    k_rep_fast<true><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+  else
+    k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+  TM_LAUNCH();
+  if (nlv.kind == 0) {
+    int grid = std::min(nblk(nv, 256), 4 * 152);
+    if (want_grad)
+      k_rep_slow<true><<<grid, 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+    else
+      k_rep_slow<false><<<grid, 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+    TM_LAUNCH();
+  }
+}
+
+}  // namespace tmg

@@ -71,6 +71,18 @@ struct TableExcl {  // exclusion on the current topology tables
   __device__ bool operator()(int v, int j) const { return excluded(t, excl, v, j); }
 };
 
+// Cell coordinate int((p - bmin) / rl) with C truncation
+// (src/nlists/cell_list.h:141), decided without the FP64 division unless
+// the quotient is within 1e-9 of an integer, where the exact quotient is used.
+__device__ __forceinline__ int cell_coord(double p, const NLGeom& G, int k) {
+  double q = __dsub_rn(p, G.bmin[k]);
+  double t = __dmul_rn(q, G.inv_rl[k]);
+  double ti = trunc(t);
+  double fr = fabs(t - ti);
+  if (fr > 1e-9 && fr < 1.0 - 1e-9 && fabs(t) < 1.0e9) return (int)ti;
+  return (int)__ddiv_rn(q, G.rl[k]);
+}
+
 // Distance test of candidate j against the query point p of vertex v:
 // an FP32 prefilter (skips only candidates that are certainly outside,
 // margin from the float rounding of both points) and the exact test
@@ -111,53 +123,76 @@ __device__ __forceinline__ bool pair_within(const PairTest& t, const NLView& nl,
   return s < t.T;
 }
 
-// Calls fn(j, |p - x_j|, p - x_j) for every neighbour j of vertex v (at p)
-// closer than dmax (T = sq_threshold(dmax)), in the reference's order: the
-// 27 cells (x outer, z inner), each cell's members in ascending order; or the
-// Verlet row.
+// The three ways to enumerate the neighbours of vertex v (at p): the
+// candidate row of its build cell, the 27-cell scan through the cell table,
+// and the Verlet row.  Each calls fn(j, |p - x_j|, p - x_j) for the
+// neighbours closer than the cut-off, in the reference's order (cells x
+// outer / z inner, members ascending).
+template <class F, class X>
+__device__ __forceinline__ void visit_pair(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p, int j,
+                                           const X& is_excluded, F& fn) {
+  d3 pj;
+  double s;
+  if (!pair_within(pt, nl, P, p, j, &pj, &s)) return;
+  if (nl.excl > 0 && is_excluded(v, j)) return;
+  fn(j, __dsqrt_rn(s), exact_diff(p, pj));
+}
+__device__ __forceinline__ bool in_build_cell(const NLView& nl, int v, d3 p, int* co) {
+  const NLGeom& G = *nl.geom;
+  const double* pp = &p.x;
+  for (int k = 0; k < 3; ++k) co[k] = cell_coord(pp[k], G, k);
+  return nl.crow && co[0] == nl.bcoord[3 * v] && co[1] == nl.bcoord[3 * v + 1] && co[2] == nl.bcoord[3 * v + 2];
+}
+template <class F, class X>
+__device__ __forceinline__ void visit_candidates(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
+                                                 const X& is_excluded, F& fn) {
+  int lo = nl.crow[v], hi = nl.crow[v + 1];
+  for (int q = lo; q < hi; ++q) visit_pair(pt, nl, P, v, p, nl.ccol[q], is_excluded, fn);
+}
+template <class F, class X>
+__device__ __forceinline__ void visit_cells(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
+                                            const int* co, const X& is_excluded, F& fn) {
+  const NLGeom& G = *nl.geom;
+  for (int a = -1; a < 2; ++a) {
+    int ii = co[0] + a;
+    if (ii < 0 || ii >= G.shape[0]) continue;
+    for (int b = -1; b < 2; ++b) {
+      int jj = co[1] + b;
+      if (jj < 0 || jj >= G.shape[1]) continue;
+      for (int c = -1; c < 2; ++c) {
+        int kk = co[2] + c;
+        if (kk < 0 || kk >= G.shape[2]) continue;
+        long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
+        int st = 0;
+        int cnt = cell_find(nl, cid, &st);
+        for (int q = 0; q < cnt; ++q) {
+          int j = nl.cell_verts[st + q];
+          if (j != v) visit_pair(pt, nl, P, v, p, j, is_excluded, fn);
+        }
+      }
+    }
+  }
+}
+template <class F, class X>
+__device__ __forceinline__ void visit_verlet(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
+                                             const X& is_excluded, F& fn) {
+  int lo = nl.vrow[v], hi = nl.vrow[v + 1];
+  for (int q = lo; q < hi; ++q) visit_pair(pt, nl, P, v, p, nl.vcol[q], is_excluded, fn);
+}
+
+// All neighbours of v closer than dmax (T = sq_threshold(dmax)).
 template <class F, class X>
 __device__ __forceinline__ void for_each_neighbour_x(const NLView& nl, const double* P, int v, d3 p, double dmax,
                                                      double T, const X& is_excluded, F&& fn) {
   PairTest pt = make_pair_test(nl, v, dmax, T);
-  auto visit = [&](int j) {
-    d3 pj;
-    double s;
-    if (!pair_within(pt, nl, P, p, j, &pj, &s)) return;
-    if (nl.excl > 0 && is_excluded(v, j)) return;
-    fn(j, __dsqrt_rn(s), exact_diff(p, pj));
-  };
   if (nl.kind == 0) {
-    const NLGeom& G = *nl.geom;
     int co[3];
-    const double* pp = &p.x;
-    for (int k = 0; k < 3; ++k) co[k] = (int)__ddiv_rn(__dsub_rn(pp[k], G.bmin[k]), G.rl[k]);
-    if (nl.crow && co[0] == nl.bcoord[3 * v] && co[1] == nl.bcoord[3 * v + 1] && co[2] == nl.bcoord[3 * v + 2]) {
-      int lo = nl.crow[v], hi = nl.crow[v + 1];
-      for (int q = lo; q < hi; ++q) visit(nl.ccol[q]);
-      return;
-    }
-    for (int a = -1; a < 2; ++a) {
-      int ii = co[0] + a;
-      if (ii < 0 || ii >= G.shape[0]) continue;
-      for (int b = -1; b < 2; ++b) {
-        int jj = co[1] + b;
-        if (jj < 0 || jj >= G.shape[1]) continue;
-        for (int c = -1; c < 2; ++c) {
-          int kk = co[2] + c;
-          if (kk < 0 || kk >= G.shape[2]) continue;
-          long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
-          int st = 0;
-          int cnt = cell_find(nl, cid, &st);
-          for (int q = 0; q < cnt; ++q) {
-            int j = nl.cell_verts[st + q];
-            if (j != v) visit(j);
-          }
-        }
-      }
-    }
+    if (in_build_cell(nl, v, p, co))
+      visit_candidates(pt, nl, P, v, p, is_excluded, fn);
+    else
+      visit_cells(pt, nl, P, v, p, co, is_excluded, fn);
   } else {
-    int lo = nl.vrow[v], hi = nl.vrow[v + 1];
-    for (int q = lo; q < hi; ++q) visit(nl.vcol[q]);
+    visit_verlet(pt, nl, P, v, p, is_excluded, fn);
   }
 }
 
@@ -191,6 +226,12 @@ __device__ __forceinline__ void assemble(const EP& ep, Globals* g) {
   g->gA = 2.0 * ep.ka / ep.refA * da;
   g->gV = 2.0 * ep.kv / ep.refV * dv;
   g->gC = 2.0 * ep.kc / ep.refC * dc;
+  const double gg[3] = {g->gA, g->gV, g->gC};
+  for (int k = 0; k < 3; ++k) {
+    float h = (float)gg[k];
+    g->gdf[2 * k] = h;
+    g->gdf[2 * k + 1] = (float)(gg[k] - (double)h);
+  }
 }
 
 

@@ -85,7 +85,7 @@ struct CellEntry {
 };
 // Cell geometry, derived on the device from the bounding box.
 struct NLGeom {
-  double bmin[3], rl[3];
+  double bmin[3], rl[3], inv_rl[3];
   int shape[3];
   int pad;
   long long stride[3];
@@ -160,6 +160,7 @@ struct Globals {
   double props[8];  // area, volume, curvature, bending, tethering, repulsion
   double comps[8];  // area, volume, area-diff, bending, tether, repulsion, total
   double gA, gV, gC;
+  float gdf[6];  // gA, gV, gC as double-float (hi, lo) pairs
   unsigned int ticket;
   int status;
 };
@@ -171,8 +172,9 @@ struct tm_energy {
   int stencil = 0;  // 0 FP64, 1 FP32
   tm_nlist nl;
   int nv = 0, ne = 0, nf = 0;
-  tmg::DevBuf<double> face, edge, ebond, rho, repg, vprops, partials, grad, work;
-  tmg::DevBuf<float> pos32;
+  tmg::DevBuf<double> face, edge, ebond, rho, repg, reppot, vprops, partials, grad, work;
+  tmg::DevBuf<int> slow;  // vertices that left their build cell (+ count)
+  tmg::DevBuf<float> pos32, poslo;
   tmg::DevBuf<tmg::Globals> glob;
   cudaStream_t stream = nullptr;
   void ensure(int nv_, int ne_, int nf_);
@@ -186,6 +188,13 @@ void energy_eval(tm_energy* e, tm_mesh* m, const double* d_points, bool want_gra
 // same, recording ev[0..4] around the face, edge, vertex and gradient kernels
 void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, bool want_vprops,
                         double* d_grad, cudaStream_t s, cudaEvent_t* ev);
+// repulsion stage: per-vertex potential (and 2 x its gradient) into pot /
+// repg; slow must hold nv + 1 ints
+void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos32, bool want_grad, double* pot,
+                    double* repg, int* slow, int* nslow, cudaStream_t s);
+// double-float stencil variant (stencil mode 2)
+void energy_eval_df(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, double* d_grad,
+                    cudaStream_t s, cudaEvent_t* ev);
 // FP32-stencil variant (stencil mode 1); per-vertex properties are not
 // produced by it
 void energy_eval32(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, bool want_vprops,
