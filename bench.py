@@ -157,6 +157,65 @@ def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400):
                       f"N(0,1e-4)) of the 163,842-vertex workload, {t:.1f} s, OpenMP {O.get_threads()} threads"}
 
 
+def batch_leg(stream, n_rep=48, n_leapfrog=10, n_steps=20):
+    """Replica batch: n_rep membranes of 642, 2562 and 10242 vertices with
+    their own parameters, sampled together by device-side HMC (one launch per
+    stage for all replicas, each HMC step one CUDA graph replay), against the
+    same replicas evaluated one mesh at a time (FP32 stencil, like the batch)."""
+    import ctypes
+
+    import torch
+
+    from helpers import workload_params
+    from trimem_gb300 import capi, meshgen
+
+    L = capi.lib()
+    reps = []
+    for k in range(n_rep):
+        p, f = meshgen.jittered_icosphere(3 + k % 3, seed=100 + k)
+        reps.append((p, f, workload_params(p, f, kappa_b=10.0 + k, vfrac=0.6 + 0.005 * k)))
+    nvert = sum(len(p) for p, _, _ in reps)
+    b = capi.Batch([(p, f) for p, f, _ in reps], [capi.params(**prm) for _, _, prm in reps])
+    b.hmc(3, n_leapfrog, 1e-6, seed=1)  # warm-up and graph capture
+    t0 = time.perf_counter()
+    acc = b.hmc(n_steps, n_leapfrog, 1e-6, seed=1)
+    t1 = time.perf_counter()
+    evals = n_steps * (n_leapfrog + 1) * n_rep
+    singles = []
+    for p, f, prm in reps:
+        m = capi.Mesh(p, f)
+        e = capi.Energy(m, capi.params(**prm))
+        e.set_stencil_precision(1)
+        x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+        g = torch.empty_like(x)
+        capi.check(L.tm_energy_update_repulsion_device(e.h, m.h, ctypes_ptr(x), ctypes_ptr_s(stream)))
+        singles.append((m, e, x, g))
+
+    def sweep():
+        for m, e, x, g in singles:
+            capi.check(L.tm_energy_eval_device(e.h, m.h, ctypes_ptr(x), ctypes_ptr(g), None, ctypes_ptr_s(stream)))
+
+    for _ in range(3):
+        sweep()
+    torch.cuda.synchronize()
+    n_sweeps = 10
+    s0 = time.perf_counter()
+    for _ in range(n_sweeps):
+        sweep()
+    torch.cuda.synchronize()
+    s1 = time.perf_counter()
+    batch_rate = evals / (t1 - t0)
+    seq_rate = n_sweeps * n_rep / (s1 - s0)
+    return {"replicas": n_rep, "vertices": nvert, "sizes": "642/2562/10242 vertices, 16 replicas each",
+            "hmc": f"{n_steps} steps x {n_leapfrog} leapfrog, dt 1e-6, graph replay",
+            "batch_replica_evals_per_s": round(batch_rate, 1),
+            "batch_vertex_evals_per_s": round(batch_rate * nvert / n_rep, 1),
+            "sequential_replica_evals_per_s": round(seq_rate, 1),
+            "speedup": round(batch_rate / seq_rate, 2),
+            "acceptance": round(float(acc.mean()) / n_steps, 3),
+            "timing": "wall clock around the synchronising call (batch) or sweep loop (sequential)"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -173,6 +232,33 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    """Workload construction, one cell-list rebuild, then --profile-evals
+    device evaluations at --stencil precision; prints nothing measured."""
+    import ctypes
+
+    import torch
+
+    from trimem_gb300 import capi
+
+    p, f, prm = workload()
+    mesh = capi.Mesh(p, f)
+    en = capi.Energy(mesh, capi.params(**prm))
+    L = capi.lib()
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    g = torch.empty_like(x)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    capi.check(L.tm_energy_set_stencil_precision(en.h, args.stencil))
+    capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), None))
+    for _ in range(args.profile_evals):
+        x.add_(torch.randn(x.shape, dtype=torch.float64, device="cuda", generator=gen), alpha=1e-4)
+        capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()),
+                                           ctypes.c_void_p(g.data_ptr()), None, None))
+    torch.cuda.synchronize()
+    print("profile evaluations done:", args.profile_evals)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,9 +267,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--e2e-evals", type=int, default=30)
+    ap.add_argument("--profile-evals", type=int, default=0,
+                    help="only run this many device evaluations (for ncu captures) and exit")
+    ap.add_argument("--stencil", type=int, default=0, help="stencil precision of --profile-evals (0, 1, 2)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_evals:
+        return run_profile(args)
 
     import torch
 
@@ -372,6 +463,11 @@ def main():
            "d2h_bytes_per_step": EVALS_PER_STEP * (24 * V + 8),
            "api": "np.copyto(TriMesh.points(), x); EnergyManager.energy_gradient(mesh); update_repulsion every 10"}
 
+    try:
+        batch = batch_leg(stream)
+    except Exception as exc:  # the headline line is printed either way
+        batch = {"error": f"{type(exc).__name__}: {exc}"}
+
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(p, f, prm)
@@ -384,6 +480,7 @@ def main():
             "config": config({"eval_ms": round(eval_ms, 5), "rebuild_ms": round(rebuild_ms, 5),
                               "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4)}),
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(), "fp32_stencil": fp32, "df64_stencil": df64,
+            "batch_replicas": batch,
             "gpu_launches": launches_per_step * args.steps, "notes": peaks_fp64}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -129,7 +129,7 @@ int tm_energy_eval_timed(tm_energy* e, tm_mesh* m, const double* d_points, doubl
 #define TM_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
 /* tm_energy_eval_device (FP64 stencil) for callers that must not allocate
  * device memory during the evaluation: the scratch lives in one file-scope
- * device array of TM_NOALLOC_SCRATCH_BYTES (about 55,000 vertices; larger
+ * device array of TM_NOALLOC_SCRATCH_BYTES (about 53,000 vertices; larger
  * meshes are rejected with TM_ERR_ARG) instead of the energy manager's
  * buffers.  The first call on a device looks up the array's address and must
  * precede any stream capture; calls that overlap on the GPU share the array
@@ -182,6 +182,29 @@ int tm_fd_gradient(tm_mesh* m, tm_energy* e, double eps, double* grad);
  * The neighbour list is the one of the energy manager (not rebuilt). */
 int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double mass, double dt, int n_steps,
                        double temperature, uint64_t seed, uint64_t step, double u, double* out4, void* stream);
+
+/* ---- batches of replicas (no counterpart in the reference: the reference
+ * runs one membrane per process) -------------------------------------------
+ * n_rep independent meshes with their own parameters evaluated and sampled
+ * together: FP32 stencils, FP64 global sums, one launch per stage for all
+ * replicas.  Positions live on the device in a padded layout: replica r
+ * occupies vertices [offsets[r], offsets[r] + n_points[r]) of
+ * [0, n_total) (see tm_batch_layout); padding vertices are inert. */
+typedef struct tm_batch tm_batch;
+int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_points, const int32_t* const* faces,
+                    const int64_t* n_faces, const tm_params* params, tm_batch** out);
+int tm_batch_destroy(tm_batch* b);
+int tm_batch_layout(tm_batch* b, int64_t* n_total, int64_t* offsets);
+/* direction 0: device -> host_x, 1: host_x -> device; host_x is n_total x 3 */
+int tm_batch_positions(tm_batch* b, double* host_x, int direction);
+/* energy of every replica (n_rep values) and optionally the gradient */
+int tm_batch_energy(tm_batch* b, double* energies, double* grad);
+int tm_batch_update_repulsion(tm_batch* b);
+/* n_steps HMC steps of every replica (n_leapfrog velocity-Verlet steps of
+ * size dt, mass, temperature; per-replica Metropolis); use_graph replays one
+ * captured step as a CUDA graph.  accepted[r] = accepted steps. */
+int tm_batch_hmc(tm_batch* b, int n_steps, int n_leapfrog, double dt, double mass, double temperature, uint64_t seed,
+                 int use_graph, int32_t* accepted);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,60 @@
+"""Batches of replicas: one launch per stage for all replicas must give each
+replica the result of its own single-mesh evaluation (FP32 stencils, FP64
+sums), and the batched HMC must be deterministic with and without graphs."""
+import numpy as np
+import pytest
+
+from helpers import workload_params
+from oracle import oracle as O
+from trimem_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+def _replicas():
+    out = []
+    for k, (level, seed, kb, vf) in enumerate([(2, 1, 10.0, 0.9), (3, 2, 30.0, 0.7), (3, 3, 50.0, 0.95), (4, 4, 20.0, 0.6)]):
+        p, f = meshgen.jittered_icosphere(level, seed=seed)
+        prm = workload_params(p, f, kappa_b=kb, vfrac=vf, excl=1, rep_scale=1.2)
+        out.append((p, f, prm))
+    return out
+
+
+@pytest.fixture(scope="module")
+def C(built):
+    from trimem_gb300 import capi
+    return capi
+
+
+def test_batch_matches_single_meshes(C):
+    reps = _replicas()
+    b = C.Batch([(p, f) for p, f, _ in reps], [C.params(**prm) for _, _, prm in reps])
+    assert b.n_total % 256 == 0 and list(b.offsets[:-1] % 256) == [0] * len(reps)
+    eb, gb = b.energy(with_grad=True)
+    for r, (p, f, prm) in enumerate(reps):
+        m = C.Mesh(p, f)
+        e = C.Energy(m, C.params(**prm))
+        e.set_stencil_precision(1)
+        es, gs = e.gradient(m, with_energy=True)
+        assert abs(eb[r] - es) <= 1e-12 * abs(es), (r, eb[r], es)
+        assert np.linalg.norm(gb[r] - gs) <= 1e-12 * np.linalg.norm(gs), r
+        # and the FP32-stencil error against the FP64 oracle stays small
+        eo = O.Energy(O.Mesh(p, f), O.default_params(**prm)).energy(O.Mesh(p, f))
+        assert abs(eb[r] - eo) <= 1e-5 * abs(eo), r
+
+
+def test_batch_hmc_graph_replay_is_deterministic(C):
+    reps = _replicas()
+    runs = []
+    for use_graph in (False, True):
+        b = C.Batch([(p, f) for p, f, _ in reps], [C.params(**prm) for _, _, prm in reps])
+        acc = b.hmc(6, 5, 1e-6, seed=11, use_graph=use_graph)
+        runs.append((acc, b.positions()))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    for x0, x1 in zip(runs[0][1], runs[1][1]):
+        assert np.array_equal(x0, x1)
+    assert runs[0][0].sum() > 0  # small steps are accepted
+    # the positions moved and stay finite
+    x_init = [p for p, _, _ in reps]
+    assert any(np.abs(x - xi).max() > 0 for x, xi in zip(runs[1][1], x_init))
+    assert all(np.isfinite(x).all() for x in runs[1][1])

@@ -99,6 +99,13 @@ _SIGS = {
     "tm_avg_tri_props": (_i32, [_p, _dp, _dp]),
     "tm_fd_gradient": (_i32, [_p, _p, _d, _dp]),
     "tm_hmc_step_device": (_i32, [_p, _p, _p, _d, _d, _i32, _d, ctypes.c_uint64, ctypes.c_uint64, _d, _dp, _p]),
+    "tm_batch_create": (_i32, [_i32, ctypes.POINTER(_dp), _i64p, ctypes.POINTER(_ip), _i64p, ctypes.POINTER(Params), _pp]),
+    "tm_batch_destroy": (_i32, [_p]),
+    "tm_batch_layout": (_i32, [_p, _i64p, _i64p]),
+    "tm_batch_positions": (_i32, [_p, _dp, _i32]),
+    "tm_batch_energy": (_i32, [_p, _dp, _dp]),
+    "tm_batch_update_repulsion": (_i32, [_p]),
+    "tm_batch_hmc": (_i32, [_p, _i32, _i32, _d, _d, _d, ctypes.c_uint64, _i32, _ip]),
 }
 
 _lib = None
@@ -304,6 +311,65 @@ class NList:
         j = np.empty(n.value, np.int32)
         check(lib().tm_nlist_fetch(self.h, _dptr(d), None, _iptr(j)))
         return d, j
+
+
+class Batch:
+    """tm_batch handle: replicas evaluated and sampled together."""
+
+    def __init__(self, meshes, params_list):
+        R = len(meshes)
+        self._pts = [np.ascontiguousarray(p, dtype=np.float64) for p, _ in meshes]
+        self._fcs = [np.ascontiguousarray(f, dtype=np.int32) for _, f in meshes]
+        pp = (_dp * R)(*[_dptr(a) for a in self._pts])
+        fp = (_ip * R)(*[_iptr(a) for a in self._fcs])
+        npts = (_i64 * R)(*[len(a) for a in self._pts])
+        nfcs = (_i64 * R)(*[len(a) for a in self._fcs])
+        prm = (Params * R)(*params_list)
+        h = ctypes.c_void_p()
+        check(lib().tm_batch_create(R, pp, npts, fp, nfcs, prm, ctypes.byref(h)))
+        self.h = h
+        self.R = R
+        n = _i64()
+        off = (_i64 * (R + 1))()
+        check(lib().tm_batch_layout(self.h, ctypes.byref(n), off))
+        self.n_total = n.value
+        self.offsets = np.array(off[:], dtype=np.int64)
+        self.sizes = [len(a) for a in self._pts]
+
+    def close(self):
+        if self.h:
+            lib().tm_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def positions(self):
+        x = np.empty((self.n_total, 3))
+        check(lib().tm_batch_positions(self.h, _dptr(x), 0))
+        return [x[o:o + n] for o, n in zip(self.offsets[:-1], self.sizes)]
+
+    def set_positions(self, xs):
+        x = np.zeros((self.n_total, 3))
+        for o, n, xi in zip(self.offsets[:-1], self.sizes, xs):
+            x[o:o + n] = xi
+        check(lib().tm_batch_positions(self.h, _dptr(x), 1))
+
+    def energy(self, with_grad=False):
+        e = np.empty(self.R)
+        g = np.empty((self.n_total, 3)) if with_grad else None
+        check(lib().tm_batch_energy(self.h, _dptr(e), _dptr(g) if with_grad else None))
+        if with_grad:
+            return e, [g[o:o + n] for o, n in zip(self.offsets[:-1], self.sizes)]
+        return e
+
+    def update_repulsion(self):
+        check(lib().tm_batch_update_repulsion(self.h))
+
+    def hmc(self, n_steps, n_leapfrog, dt, mass=1.0, temperature=1.0, seed=0, use_graph=True):
+        acc = np.zeros(self.R, np.int32)
+        check(lib().tm_batch_hmc(self.h, int(n_steps), int(n_leapfrog), float(dt), float(mass),
+                                 float(temperature), int(seed), int(bool(use_graph)), _iptr(acc)))
+        return acc
 
 
 def flip(mesh, energy, ratio, seed, mode, batch=256):

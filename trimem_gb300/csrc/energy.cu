@@ -80,7 +80,7 @@ __global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__
 }
 
 __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd, EdgeD* __restrict__ ed,
-                       double* __restrict__ ebond, EP ep) {
+                       double* __restrict__ ebond, EP ep, int* __restrict__ blist, int* __restrict__ bcnt) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= t.ne) return;
   int4 E = t.edge[e];
@@ -99,26 +99,28 @@ __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __rest
     o.th = dot(cross(n0, n1), ev) >= 0.0 ? a : -a;
     o.flag = 1.0;
   }
-  // flat-bottom edge penalty and its derivative (src/mesh_tether.h:29-85)
+  // flat-bottom edge penalty: above the flat bottom inline (products only);
+  // edges below it (exp and divisions in FP64) go to a list handled by
+  // k_bond_short so that whole warps do not wait on a few lanes
   double val = 0.0, fac = 0.0;
-  if (ep.btype == 0) {
-    int r = ep.r;
-    if (l > ep.lc0) {
-      val = ipow((double)r, r + 1) * ipow(l - ep.lc0, r);
-      fac = ipow((double)r, r + 2) * ipow(l - ep.lc0, r - 1);
-    } else if (l < ep.lc1) {
-      val = exp(l / (l - ep.lc1)) / ipow(l, r);
-    }
-    if (l < ep.lc1) {
-      double lmc = l - ep.lc1;
-      fac -= ep.lc1 / (lmc * lmc) + r / l;
-      fac /= ipow(l, r);
-      fac *= exp(l / lmc);
-    }
-  }
-  o.db = fac;
+  bool shortb = ep.btype == 0 && l < ep.lc1;
+  if (ep.btype == 0 && !shortb && l > ep.lc0) edge_bond(ep, l, &val, &fac);
+  warp_append(shortb, e, blist, bcnt);  o.db = fac;
   ed[e] = o;
   ebond[e] = val;
+}
+
+__global__ void k_bond_short(const double* __restrict__ P, Topo t, EdgeD* __restrict__ ed,
+                             double* __restrict__ ebond, EP ep, const int* __restrict__ blist,
+                             const int* __restrict__ bcnt) {
+  int n = *bcnt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int e = blist[i];
+    double val, fac;
+    edge_bond(ep, ed[e].l, &val, &fac);
+    ed[e].db = fac;
+    ebond[e] = val;
+  }
 }
 
 template <bool VPROPS>
@@ -149,14 +151,15 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__
         T += q * q;
       }
     }
-    double a = A / 3, c = 0.25 * LT;
+    double a = A * (1.0 / 3.0), c = 0.25 * LT;
+    double ia = 1.0 / a;
     pr[0] = a;
-    pr[1] = V / 3;
+    pr[1] = V * (1.0 / 3.0);
     pr[2] = c;
-    pr[3] = 2 * c * c / a;
-    pr[4] = T / ep.tdiv;
+    pr[3] = 2 * c * c * ia;
+    pr[4] = T * (1.0 / ep.tdiv);
     pr[5] = reppot[v];
-    rho[v] = c / a;
+    rho[v] = c * ia;
     if (VPROPS)
       for (int k = 0; k < 6; ++k) vprops[6 * (size_t)v + k] = pr[k];
   }
@@ -323,7 +326,12 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
   k_face<<<nfb, 256, 0, s>>>(t, P, fd, e->pos32.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
-  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep);
+  int* blist = e->slow.get() + std::max(m->nv, 1) + 1;
+  int* bcnt = blist + std::max(m->ne, 1);
+  TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
+  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep, blist, bcnt);
+  TM_LAUNCH();
+  if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(P, t, ed, e->ebond.get(), ep, blist, bcnt);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
   repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
@@ -362,7 +370,8 @@ void tm_energy::ensure(int nv_, int ne_, int nf_) {
   rho.ensure(std::max(nv, 1));
   repg.ensure(3 * (size_t)std::max(nv, 1));
   reppot.ensure(std::max(nv, 1));
-  slow.ensure((size_t)std::max(nv, 1) + 1);
+  // repulsion slow list (nv + 1) and short-bond edge list (ne + 1)
+  slow.ensure((size_t)std::max(nv, 1) + 1 + (size_t)std::max(ne, 1) + 1);
   vprops.ensure(6 * (size_t)std::max(nv, 1));
   pos32.ensure(3 * (size_t)std::max(nv, 1));
   int nb = std::max(1, (nv + tmg::VB - 1) / tmg::VB);
@@ -637,13 +646,14 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   size_t off_pos32 = off_repg + align256(3 * sizeof(double) * nv);
   size_t off_pot = off_pos32 + align256(3 * sizeof(float) * nv);
   size_t off_slow = off_pot + align256(sizeof(double) * nv);
-  size_t off_part = off_slow + align256(sizeof(int) * (nv + 1));
+  size_t off_blist = off_slow + align256(sizeof(int) * (nv + 1));
+  size_t off_part = off_blist + align256(sizeof(int) * (ne + 1));
   size_t off_glob = off_part + align256(8 * sizeof(double) * nb);
   size_t need = off_glob + align256(sizeof(Globals));
   if (need > (size_t)TM_NOALLOC_SCRATCH_BYTES)
     fail(TM_ERR_ARG, "mesh needs " + std::to_string(need) + " bytes of scratch, more than the " +
                          std::to_string((size_t)TM_NOALLOC_SCRATCH_BYTES) +
-                         " bytes of tm_energy_eval_device_noalloc (about 55,000 vertices)");
+                         " bytes of tm_energy_eval_device_noalloc (about 53,000 vertices)");
   unsigned char* base = noalloc_scratch_for_current_device();
   cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
   FaceD* fd = reinterpret_cast<FaceD*>(base + off_face);
@@ -654,6 +664,8 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   float* pos32 = reinterpret_cast<float*>(base + off_pos32);
   double* reppot = reinterpret_cast<double*>(base + off_pot);
   int* slow = reinterpret_cast<int*>(base + off_slow);
+  int* blist = reinterpret_cast<int*>(base + off_blist);
+  int* bcnt = blist + ne;
   double* part = reinterpret_cast<double*>(base + off_part);
   Globals* g = reinterpret_cast<Globals*>(base + off_glob);
   // the block ticket of the reduction must start at zero
@@ -665,7 +677,10 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   int nfb = std::max(nblk(std::max(t.nf, t.nv), 256), 1);
   k_face<<<nfb, 256, 0, s>>>(t, d_points, fd, pos32);
   TM_LAUNCH();
-  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, d_points, fd, ed, ebond, ep);
+  TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
+  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, d_points, fd, ed, ebond, ep, blist, bcnt);
+  TM_LAUNCH();
+  if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(d_points, t, ed, ebond, ep, blist, bcnt);
   TM_LAUNCH();
   repulsion_eval(e, m, d_points, pos32, true, reppot, repg, slow, slow + nv, s);
   k_vertex<false><<<nb, VB, 0, s>>>(t, fd, ed, ebond, reppot, ep, rho, nullptr, part, g);

@@ -275,6 +275,202 @@ __global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __
   grad[3 * i + 2] = acc.z;
 }
 
+// ---- batch of replicas (disjoint-union mesh, replica-aligned blocks) -----
+// Same arithmetic as the single-mesh FP32 kernels; the parameters and the
+// global sums are per replica (vrep: vertex -> replica, -1 for padding).
+
+__global__ void k_edge32b(Topo t, Split S, const FaceF* __restrict__ fd, EdgeF* __restrict__ ed,
+                          float* __restrict__ ebond, const EP* __restrict__ eps, const int* __restrict__ vrep) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.ne) return;
+  int4 E = t.edge[e];
+  const EP& ep = eps[vrep[E.x]];
+  f3 ev = S.diff(E.y, E.x);
+  float l = fnorm(ev);
+  EdgeF o;
+  o.l = l;
+  o.th = 0.0f;
+  o.flag = 0.0f;
+  if (E.z >= 0 && E.w >= 0) {
+    FaceF F0 = fd[E.z], F1 = fd[E.w];
+    f3 n0 = {F0.nx, F0.ny, F0.nz}, n1 = {F1.nx, F1.ny, F1.nz};
+    f3 cr = fcross(n0, n1);
+    float a = atan2f(fnorm(cr), fdot(n0, n1));
+    o.th = fdot(cr, ev) >= 0.0f ? a : -a;
+    o.flag = 1.0f;
+  }
+  float val = 0.0f, fac = 0.0f;
+  if (ep.btype == 0) {
+    int r = ep.r;
+    float lc0 = (float)ep.lc0, lc1 = (float)ep.lc1;
+    if (l > lc0) {
+      val = fipow((float)r, r + 1) * fipow(l - lc0, r);
+      fac = fipow((float)r, r + 2) * fipow(l - lc0, r - 1);
+    } else if (l < lc1) {
+      val = expf(l / (l - lc1)) / fipow(l, r);
+    }
+    if (l < lc1) {
+      float lmc = l - lc1;
+      fac -= lc1 / (lmc * lmc) + r / l;
+      fac /= fipow(l, r);
+      fac *= expf(l / lmc);
+    }
+  }
+  o.db = fac;
+  ed[e] = o;
+  ebond[e] = val;
+}
+
+__global__ void __launch_bounds__(VB) k_vertex32b(Topo t, const FaceF* __restrict__ fd, const EdgeF* __restrict__ ed,
+                                                 const float* __restrict__ ebond, const double* __restrict__ reppot,
+                                                 const EP* __restrict__ eps, const int* __restrict__ vrep,
+                                                 const int2* __restrict__ rblocks, float* __restrict__ rho,
+                                                 double* __restrict__ partial, Globals* gs) {
+  __shared__ double red[6][VB];
+  __shared__ bool last;
+  const int rep = vrep[blockIdx.x * VB];  // blocks never straddle replicas
+  const EP& ep = eps[rep];
+  int v = blockIdx.x * VB + threadIdx.x;
+  double pr[6] = {0, 0, 0, 0, 0, 0};
+  if (v < t.nv && vrep[v] >= 0) {
+    int d = t.val[v];
+    float A = 0, V = 0, LT = 0, T = 0;
+    for (int m = 0; m < d; ++m) {
+      int4 s = t.slot[(size_t)m * t.nv + v];
+      int f = slot_face(s.y);
+      if (f < 0) continue;
+      float fa = fd[f].A;
+      A += fa;
+      V += fd[f].V;
+      EdgeF E = ed[s.z];
+      LT += E.l * E.th;
+      if (ep.btype == 0) {
+        T += ebond[s.z];
+      } else {
+        float q = fa / (float)ep.a0 - 1.0f;
+        T += q * q;
+      }
+    }
+    float a = A / 3, c = 0.25f * LT;
+    pr[0] = a;
+    pr[1] = V / 3;
+    pr[2] = c;
+    pr[3] = 2 * c * c / a;
+    pr[4] = T / (float)ep.tdiv;
+    pr[5] = reppot[v];
+    rho[v] = c / a;
+  }
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = pr[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  Globals* g = gs + rep;
+  const int2 rb = rblocks[rep];
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) partial[8 * (size_t)blockIdx.x + k] = red[k][0];
+    __threadfence();
+    unsigned int tk = atomicAdd(&g->ticket, 1u);
+    last = (tk == (unsigned)(rb.y - rb.x - 1));
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = rb.x + threadIdx.x; b < rb.y; b += VB)
+    for (int k = 0; k < 6; ++k) acc[k] += ((volatile double*)partial)[8 * (size_t)b + k];
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 6; ++k) g->props[k] = red[k][0];
+    assemble(ep, g);
+    g->ticket = 0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_grad32b(Topo t, Split S, const FaceF* __restrict__ fd,
+                                                const EdgeF* __restrict__ ed, const float* __restrict__ rho,
+                                                const double* __restrict__ repg, const Globals* __restrict__ gs,
+                                                const EP* __restrict__ eps, const int* __restrict__ vrep,
+                                                double* __restrict__ grad) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.nv) return;
+  int rep = vrep[i];
+  if (rep < 0) {
+    grad[3 * i] = grad[3 * i + 1] = grad[3 * i + 2] = 0.0;
+    return;
+  }
+  const EP& ep = eps[rep];
+  const Globals* g = gs + rep;
+  const float gA = (float)g->gA, gV = (float)g->gV, gC = (float)g->gC;
+  const float kb = (float)ep.kb, kt = (float)ep.kt, a0 = (float)ep.a0;
+  const float hgC = 0.5f * gC;
+  const float kb23 = kb * (2.0f / 3.0f);
+  float ri = rho[i];
+  f3 acc = (float)ep.kr * f3{(float)repg[3 * i], (float)repg[3 * i + 1], (float)repg[3 * i + 2]};
+  int d = t.val[i];
+  if (d > 0) {
+    const size_t nv = t.nv;
+    int4 sp = t.slot[(size_t)(d - 1) * nv + i];
+    f3 xk = S.diff(sp.x, i);
+    float rk = rho[sp.x];
+    int4 sc = t.slot[i];
+    f3 xj = S.diff(sc.x, i);
+    float rj = rho[sc.x];
+    FaceF Fc;
+    int fcur = slot_face(sc.y);
+    if (fcur >= 0) Fc = fd[fcur];
+    f3 xi_abs = S.h(i);
+    for (int m = 0; m < d; ++m) {
+      int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
+      int fnx = slot_face(sn.y);
+      FaceF Fn;
+      if (fnx >= 0) Fn = fd[fnx];
+      if (fcur >= 0) {
+        int ci = slot_corner(sc.y);
+        float cj = cotf_at(Fc, ci == 2 ? 0 : ci + 1);
+        float ck = cotf_at(Fc, ci == 0 ? 2 : ci - 1);
+        f3 n = {Fc.nx, Fc.ny, Fc.nz};
+        float alpha = gA - kb23 * (ri * ri + rj * rj + rk * rk);
+        if (ep.btype == 1) alpha += kt * 2.0f * (Fc.A / a0 - 1.0f) / a0;
+        acc += (0.5f * alpha) * fcross(n, xk - xj);
+        f3 vj = fcross(xi_abs, xk - xj) + fcross(xj, xk);
+        acc += (gV * (1.0f / 6.0f)) * vj;
+        EdgeF E = ed[sc.z];
+        float w = hgC + kb * (ri + rj);
+        float cl = w * E.th + (ep.btype == 0 ? kt * E.db : 0.0f);
+        acc += (-cl / E.l) * xj;
+        if (E.flag != 0.0f) {
+          int cin = slot_corner(sn.y);
+          float cjn = cotf_at(Fn, cin == 0 ? 2 : cin - 1);
+          acc += w * (cj * n + cjn * f3{Fn.nx, Fn.ny, Fn.nz});
+        }
+        if (ed[sc.w].flag != 0.0f) {
+          float wo = hgC + kb * (rj + rk);
+          acc += (-wo * (cj + ck)) * n;
+        }
+      }
+      xk = xj;
+      rk = rj;
+      sc = sn;
+      fcur = fnx;
+      Fc = Fn;
+      xj = S.diff(sn.x, i);
+      rj = rho[sn.x];
+    }
+  }
+  grad[3 * i] = acc.x;
+  grad[3 * i + 1] = acc.y;
+  grad[3 * i + 2] = acc.z;
+}
+
 inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
@@ -315,6 +511,34 @@ void energy_eval32(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bo
   if (want_grad && t.nv) k_grad32<<<nblk(t.nv, 256), 256, 0, s>>>(t, S, fd, ed, rho, repg, e->glob.get(), ep, d_grad);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[4], s));
+}
+
+void energy_eval_batch32(tm_energy* e, tm_mesh* m, const double* P, double* d_grad, const EP* eps,
+                         const int* vrep, const int2* rblocks, Globals* gs, const int* blk, cudaStream_t s) {
+  e->ensure(m->nv, m->ne, m->nf);
+  size_t nv = std::max(m->nv, 1);
+  Topo t = m->topo();
+  e->pos32.ensure(3 * nv);
+  e->poslo.ensure(3 * nv);
+  Split S{e->pos32.get(), e->poslo.get()};
+  FaceF* fd = reinterpret_cast<FaceF*>(e->face.get());
+  EdgeF* ed = reinterpret_cast<EdgeF*>(e->edge.get());
+  float* eb = reinterpret_cast<float*>(e->ebond.get());
+  float* rho = reinterpret_cast<float*>(e->rho.get());
+  // blk: tuned block sizes of the element kernels {split, face, edge, grad}
+  if (m->nv) k_split<<<nblk(3L * m->nv, blk[0]), blk[0], 0, s>>>(m->nv, P, e->pos32.get(), e->poslo.get());
+  TM_LAUNCH();
+  if (t.nf) k_face32<<<nblk(t.nf, blk[1]), blk[1], 0, s>>>(t, S, fd);
+  TM_LAUNCH();
+  if (t.ne) k_edge32b<<<nblk(t.ne, blk[2]), blk[2], 0, s>>>(t, S, fd, ed, eb, eps, vrep);
+  TM_LAUNCH();
+  repulsion_eval(e, m, P, e->pos32.get(), true, e->reppot.get(), e->repg.get(), e->slow.get(),
+                 e->slow.get() + std::max(m->nv, 1), s, eps);
+  int nb = std::max(1, nblk(t.nv, VB));
+  k_vertex32b<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), eps, vrep, rblocks, rho, e->partials.get(), gs);
+  TM_LAUNCH();
+  if (t.nv) k_grad32b<<<nblk(t.nv, blk[3]), blk[3], 0, s>>>(t, S, fd, ed, rho, e->repg.get(), gs, eps, vrep, d_grad);
+  TM_LAUNCH();
 }
 
 }  // namespace tmg

@@ -49,8 +49,14 @@ struct PosDF {
 
 // double-float parameters (hi/lo from the host)
 struct EPD {
-  df kb, kt, kr, kb23, a0, inv_a0, inv_tdiv;
+  df kb, kt, kr, kb23, a0, inv_a0, inv_tdiv, lc0, lc1;
 };
+__device__ __forceinline__ bool df_less(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ df df_ipow(df x, int n) {
+  df r = df_make(1.0f);
+  for (int k = 0; k < n; ++k) r = r * x;
+  return r;
+}
 
 __global__ void k_split_df(int n3, const double* __restrict__ P, float* __restrict__ hi, float* __restrict__ lo) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -83,7 +89,8 @@ __global__ void __launch_bounds__(256) k_face_df(Topo t, PosDF X, FaceDF* __rest
 }
 
 __global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* __restrict__ fd,
-                                                EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep) {
+                                                EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep, EPD epd,
+                                                int* __restrict__ blist, int* __restrict__ bcnt) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= t.ne) return;
   int4 E = t.edge[e];
@@ -105,28 +112,34 @@ __global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* 
     o.th = df_lt0(ddot(cr, ev)) ? -th : th;
     o.flag = df_make(1.0f);
   }
-  // flat-bottom edge penalty (src/mesh_tether.h:29-85), FP64 outside the
-  // flat bottom
-  double val = 0.0, fac = 0.0;
-  if (ep.btype == 0) {
-    double ld = df_to(l);
+  // flat-bottom edge penalty: above the flat bottom inline in double-float
+  // (products only), below it (exp, FP64) through the short-edge list
+  df val = df_make(0.0f);
+  o.db = df_make(0.0f);
+  bool shortb = ep.btype == 0 && df_less(l, epd.lc1);
+  if (ep.btype == 0 && !shortb && df_less(epd.lc0, l) && ep.r >= 1) {
     int r = ep.r;
-    if (ld > ep.lc0) {
-      val = ipow((double)r, r + 1) * ipow(ld - ep.lc0, r);
-      fac = ipow((double)r, r + 2) * ipow(ld - ep.lc0, r - 1);
-    } else if (ld < ep.lc1) {
-      val = exp(ld / (ld - ep.lc1)) / ipow(ld, r);
-    }
-    if (ld < ep.lc1) {
-      double lmc = ld - ep.lc1;
-      fac -= ep.lc1 / (lmc * lmc) + r / ld;
-      fac /= ipow(ld, r);
-      fac *= exp(ld / lmc);
-    }
+    df d = l - epd.lc0;
+    df dr1 = df_ipow(d, r - 1);
+    float rr = (float)r;
+    val = df_ipow(df_make(rr), r + 1) * (dr1 * d);
+    o.db = df_ipow(df_make(rr), r + 2) * dr1;
   }
-  o.db = val == 0.0 && fac == 0.0 ? df_make(0.0f) : df_from(fac);
+  warp_append(shortb, e, blist, bcnt);
   ed[e] = o;
-  ebond[e] = val == 0.0 ? df_make(0.0f) : df_from(val);
+  ebond[e] = val;
+}
+
+__global__ void k_bond_short_df(EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep,
+                                const int* __restrict__ blist, const int* __restrict__ bcnt) {
+  int n = *bcnt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int e = blist[i];
+    double val, fac;
+    edge_bond(ep, df_to(ed[e].l), &val, &fac);
+    ed[e].db = df_from(fac);
+    ebond[e] = df_from(val);
+  }
 }
 
 __global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const FaceDF* __restrict__ fd,
@@ -142,6 +155,7 @@ __global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const FaceDF* __restri
   if (v < t.nv) {
     int d = t.val[v];
     df A = df_make(0.0f), V = df_make(0.0f), LT = df_make(0.0f), T = df_make(0.0f);
+#pragma unroll 4
     for (int m = 0; m < d; ++m) {
       int4 s = t.slot[(size_t)m * t.nv + v];
       int f = slot_face(s.y);
@@ -221,6 +235,10 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
   df3 xi = X.at(i);
   df ri = rho[i];
   df3 acc = {df_make(0.0f), df_make(0.0f), df_make(0.0f)};
+  // volume term sum_f (x_j x x_k)/6 with x = x_i + d: the x_i x (d_k - d_j)
+  // parts telescope around the fan, so only sum d_j x d_k and, for open
+  // fans, x_i x sum (d_k - d_j) remain
+  df3 vcr = acc, vtel = acc;
   int d = t.val[i];
   if (d > 0) {
     const size_t nv = t.nv;
@@ -245,8 +263,8 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
         if (ep.btype == 1) alpha += ldexp2(epd.kt * (Fc.A * epd.inv_a0 - df_make(1.0f)) * epd.inv_a0, 2.0f);
         df3 dkj = dk - dj;
         acc += ldexp2(alpha, 0.5f) * dcross(n, dkj);
-        // x_j x x_k = x_i x (d_k - d_j) + d_j x d_k
-        acc += gV6 * (dcross(xi, dkj) + dcross(dj, dk));
+        vcr += dcross(dj, dk);
+        vtel += dkj;
         // edge (i, j): length and dihedral terms
         const EdgeDF& E = ed[sc.z];
         df w = hgC + kb * (ri + rj);
@@ -274,6 +292,7 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
       rj = rho[sn.x];
     }
   }
+  if (d > 0) acc += gV6 * (vcr + dcross(xi, vtel));
   d3 r = ld3(repg, i);
   grad[3 * i] = df_to(acc.x) + ep.kr * r.x;
   grad[3 * i + 1] = df_to(acc.y) + ep.kr * r.y;
@@ -305,6 +324,8 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   epd.a0 = host_df(ep.a0);
   epd.inv_a0 = host_df(1.0 / ep.a0);
   epd.inv_tdiv = host_df(1.0 / ep.tdiv);
+  epd.lc0 = host_df(ep.lc0);
+  epd.lc1 = host_df(ep.lc1);
   PosDF X{e->pos32.get(), e->poslo.get()};
   FaceDF* fd = reinterpret_cast<FaceDF*>(e->face.get());
   EdgeDF* ed = reinterpret_cast<EdgeDF*>(e->edge.get());
@@ -316,7 +337,12 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   if (t.nf) k_face_df<<<nblk(t.nf, 256), 256, 0, s>>>(t, X, fd);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
-  if (t.ne) k_edge_df<<<nblk(t.ne, 256), 256, 0, s>>>(t, X, fd, ed, eb, ep);
+  int* blist = e->slow.get() + std::max(m->nv, 1) + 1;
+  int* bcnt = blist + std::max(m->ne, 1);
+  TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
+  if (t.ne) k_edge_df<<<nblk(t.ne, 256), 256, 0, s>>>(t, X, fd, ed, eb, ep, epd, blist, bcnt);
+  TM_LAUNCH();
+  if (t.ne) k_bond_short_df<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(ed, eb, ep, blist, bcnt);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
   repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),

@@ -116,7 +116,11 @@ __global__ void k_bbox(int nv, const double* P, double* part) {
 // Bounding box with the reference's initial values, then r_list, shape and
 // strides exactly like src/nlists/cell_list.h:56-65.  One block reduces the
 // block partials (min/max are exact, so the order does not matter).
+__device__ void k_bbox_final_body(int nb, const double* part, double rlist, NLGeom* G);
 __global__ void k_bbox_final(int nb, const double* part, double rlist, NLGeom* G) {
+  k_bbox_final_body(nb, part, rlist, G);
+}
+__device__ void k_bbox_final_body(int nb, const double* part, double rlist, NLGeom* G) {
   __shared__ double s[6][BB];
   double lo[3] = {DBL_MAX, 0.0, 0.0}, hi[3] = {-1.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < nb; b += BB)
@@ -147,12 +151,51 @@ __global__ void k_bbox_final(int nb, const double* part, double rlist, NLGeom* G
     int nk = (int)__ddiv_rn(dim, rlist);
     G->rl[k] = nk > 0 ? __ddiv_rn(dim, (double)nk) : dim;
     G->inv_rl[k] = 1.0 / G->rl[k];
+    G->inv_rlf[k] = (float)G->inv_rl[k];
+    G->bminf[k] = (float)s[k][0];
     G->shape[k] = nk > 0 ? nk : 1;
     G->bmin[k] = s[k][0];
   }
   G->stride[0] = 1;
   G->stride[1] = G->shape[0];
   G->stride[2] = (long long)G->shape[0] * G->shape[1];
+}
+
+// batch: one partial box per 256-vertex block (blocks never straddle
+// replicas), then one block per replica reduces its blocks
+__global__ void k_bbox_blocks(int nv, const double* P, const int* vrep, double* part) {
+  __shared__ double s[6][BB];
+  double lo[3] = {DBL_MAX, 0.0, 0.0}, hi[3] = {-1.0, 0.0, 0.0};
+  int i = blockIdx.x * BB + threadIdx.x;
+  if (i < nv && vrep[i] >= 0)
+    for (int k = 0; k < 3; ++k) {
+      double x = P[3 * i + k];
+      if (x < lo[k]) lo[k] = x;
+      if (x > hi[k]) hi[k] = x;
+    }
+  for (int k = 0; k < 3; ++k) {
+    s[k][threadIdx.x] = lo[k];
+    s[3 + k][threadIdx.x] = hi[k];
+  }
+  __syncthreads();
+  for (int o = BB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 3; ++k) {
+        double a = s[k][threadIdx.x + o];
+        if (a < s[k][threadIdx.x]) s[k][threadIdx.x] = a;
+        double b = s[3 + k][threadIdx.x + o];
+        if (b > s[3 + k][threadIdx.x]) s[3 + k][threadIdx.x] = b;
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) part[6 * blockIdx.x + k] = s[k][0];
+}
+
+__global__ void k_bbox_final_batch(const int2* rblocks, const double* part, const double* rlist, NLGeom* geoms) {
+  int r = blockIdx.x;
+  int2 rb = rblocks[r];
+  k_bbox_final_body(rb.y - rb.x, part + 6 * rb.x, rlist[r], geoms + r);
 }
 
 __global__ void k_table_init(CellEntry* T, size_t n) {
@@ -168,7 +211,14 @@ __global__ void k_cell_insert(int nv, const double* P, NLView nl, CellEntry* T, 
                               int* vslot, int* status) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
-  const NLGeom& G = *nl.geom;
+  int rep = rep_of(nl, v);
+  if (rep < 0) {  // padding vertex of a batch: in no cell
+    vslot[v] = -1;
+    vcid[v] = -1;
+    vcoord[3 * v] = vcoord[3 * v + 1] = vcoord[3 * v + 2] = -1000000;
+    return;
+  }
+  const NLGeom& G = nl.geom[rep];
   long long id = 0;
   for (int k = 0; k < 3; ++k) {
     int c = (int)__ddiv_rn(__dsub_rn(P[3 * v + k], G.bmin[k]), G.rl[k]);
@@ -176,6 +226,7 @@ __global__ void k_cell_insert(int nv, const double* P, NLView nl, CellEntry* T, 
     id += (long long)c * G.stride[k];
   }
   vcid[v] = id;
+  id = cell_key(id, rep);
   unsigned long long h = cell_hash2(id) & nl.tmask;
   int slot = -1;
   for (unsigned long long p = 0; p <= nl.tmask; ++p) {
@@ -208,6 +259,7 @@ __global__ void k_scatter(int nv, const int* vslot, const CellEntry* T, int* fil
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   int s = vslot[v];
+  if (s < 0) return;
   int pos = T[s].start + atomicAdd(&fill[s], 1);
   cell_verts[pos] = v;
 }
@@ -340,7 +392,12 @@ __global__ void k_cell_pairs(int nv, const double* P, NLView nl, Topo t, const i
 __global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt, const int* off, int* out) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nv) return;
-  const NLGeom& G = *nl.geom;
+  int rep = rep_of(nl, a);
+  if (rep < 0) {
+    if (!pass) cnt[a] = 0;
+    return;
+  }
+  const NLGeom& G = nl.geom[rep];
   int n = 0;
   int base = pass ? off[a] : 0;
   for (int x = -1; x < 2; ++x) {
@@ -354,7 +411,7 @@ __global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt,
         if (kk < 0 || kk >= G.shape[2]) continue;
         long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
         int st = 0;
-        int c = cell_lookup(nl, cid, &st);
+        int c = cell_lookup(nl, cell_key(cid, rep), &st);
         for (int q = 0; q < c; ++q) {
           int b = nl.cell_verts[st + q];
           if (b == a) continue;
@@ -449,27 +506,9 @@ inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
 
-void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, cudaStream_t s) {
-  if (p.n_search != 0 && p.n_search != 1) fail(TM_ERR_ARG, "Unknown neighbour search algorithm.");
-  if (p.exclusion_level < 0 || p.exclusion_level > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
-  nl->prm = p;
-  int nv = m->nv;
-  nl->nv = nv;
-  NLView& V = nl->view;
-  V = NLView{};
-  V.kind = 0;
-  V.excl = p.exclusion_level;
-  // 1. box and cell geometry (device only, no host round trip)
-  int nb = std::max(1, std::min(1024, nblk(nv, BB)));
-  nl->bbox.ensure(6 * (size_t)nb + 6);
-  nl->geom.ensure(1);
-  V.geom = nl->geom.get();
-  if (nv > 0) {
-    k_bbox<<<nb, BB, 0, s>>>(nv, P, nl->bbox.get());
-    TM_LAUNCH();
-  }
-  k_bbox_final<<<1, BB, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
-  TM_LAUNCH();
+// Steps 2-4 of the cell-list build and the candidate rows (shared by single
+// meshes and batches; V.geom and V.vrep are set by the caller).
+static void build_cells(tm_nlist* nl, NLView& V, int nv, const double* P, cudaStream_t s, bool candidates) {
   // 2. hash table of the non-empty cells: 2x the vertex count, power of two
   size_t tsize = 64;
   while (tsize < 2 * (size_t)std::max(nv, 1)) tsize <<= 1;
@@ -506,7 +545,7 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
                                                         nl->vrank.get());
     TM_LAUNCH();
   }
-  if (p.n_search == 0 && nv > 0) {
+  if (candidates && nv > 0) {
     // candidate rows for the queries of points that stay in their build cell
     nl->crow.ensure((size_t)nv + 1);
     nl->cnt.ensure((size_t)nv + 1);
@@ -526,6 +565,30 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
       V.bcoord = nl->vcoord.get();
     }
   }
+}
+
+void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, cudaStream_t s) {
+  if (p.n_search != 0 && p.n_search != 1) fail(TM_ERR_ARG, "Unknown neighbour search algorithm.");
+  if (p.exclusion_level < 0 || p.exclusion_level > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
+  nl->prm = p;
+  int nv = m->nv;
+  nl->nv = nv;
+  NLView& V = nl->view;
+  V = NLView{};
+  V.kind = 0;
+  V.excl = p.exclusion_level;
+  // 1. box and cell geometry (device only, no host round trip)
+  int nb = std::max(1, std::min(1024, nblk(nv, BB)));
+  nl->bbox.ensure(6 * (size_t)nb + 6);
+  nl->geom.ensure(1);
+  V.geom = nl->geom.get();
+  if (nv > 0) {
+    k_bbox<<<nb, BB, 0, s>>>(nv, P, nl->bbox.get());
+    TM_LAUNCH();
+  }
+  k_bbox_final<<<1, BB, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
+  TM_LAUNCH();
+  build_cells(nl, V, nv, P, s, p.n_search == 0);
   if (p.n_search == 1) {
     // Verlet CSR from the cell list at cut-off rlist, rows in the reference's
     // insertion order
@@ -555,6 +618,31 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
     V.vrow = nl->vrow.get();
     V.vcol = nl->vcol.get();
   }
+}
+
+void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
+                      const double* d_rlist, int excl, const double* P, cudaStream_t s) {
+  if (excl < 0 || excl > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
+  int nv = m->nv;
+  nl->nv = nv;
+  nl->prm.n_search = 0;
+  nl->prm.exclusion_level = excl;
+  NLView& V = nl->view;
+  V = NLView{};
+  V.kind = 0;
+  V.excl = excl;
+  V.vrep = d_vrep;
+  int nb = std::max(1, nblk(nv, BB));
+  nl->bbox.ensure(6 * (size_t)nb);
+  nl->geom.ensure(R);
+  V.geom = nl->geom.get();
+  if (nv > 0) {
+    k_bbox_blocks<<<nb, BB, 0, s>>>(nv, P, d_vrep, nl->bbox.get());
+    TM_LAUNCH();
+  }
+  k_bbox_final_batch<<<R, BB, 0, s>>>(d_rblocks, nl->bbox.get(), d_rlist, nl->geom.get());
+  TM_LAUNCH();
+  build_cells(nl, V, nv, P, s, true);
 }
 
 int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* P, double rd, cudaStream_t s) {

@@ -41,19 +41,28 @@ struct RepAcc {
 template <bool GRAD>
 __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restrict__ P, NLView nl, EP ep,
                                                  double* __restrict__ pot, double* __restrict__ repg,
-                                                 int* __restrict__ slow, int* __restrict__ nslow) {
+                                                 int* __restrict__ slow, int* __restrict__ nslow,
+                                                 const EP* __restrict__ eps) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= t.nv) return;
+  if (nl.vrep) {  // batch: per-replica cut-off, padding vertices have none
+    int r = nl.vrep[v];
+    if (r < 0) {
+      pot[v] = 0.0;
+      if (GRAD) st3(repg, v, mk(0, 0, 0));
+      return;
+    }
+    ep = eps[r];
+  }
   d3 p = ld3(P, v);
   PairTest pt = make_pair_test(nl, v, ep.rlc1, ep.rT);
   RepAcc acc{ep.rlc1, ep.rr, 0.0, mk(0, 0, 0), GRAD};
   TableExcl x{t, nl.excl};
   if (nl.kind == 0) {
     int co[3];
-    if (!in_build_cell(nl, v, p, co)) {
-      slow[atomicAdd(nslow, 1)] = v;
-      return;
-    }
+    bool fast = in_build_cell(nl, v, p, co);
+    warp_append(!fast, v, slow, nslow);
+    if (!fast) return;
     visit_candidates(pt, nl, P, v, p, x, acc);
   } else {
     visit_verlet(pt, nl, P, v, p, x, acc);
@@ -62,22 +71,55 @@ __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restri
   if (GRAD) st3(repg, v, 2.0 * acc.gr);
 }
 
+// One warp per queued vertex: lane l < 27 scans neighbour cell l (the
+// reference's x-outer / z-inner order), then the lanes' sums are combined by
+// a fixed shuffle tree, so the result does not depend on timing.
 template <bool GRAD>
-__global__ void __launch_bounds__(256) k_rep_slow(Topo t, const double* __restrict__ P, NLView nl, EP ep,
+__global__ void __launch_bounds__(256) k_rep_slow(Topo t, const double* __restrict__ P, NLView nl, EP ep0,
                                                  double* __restrict__ pot, double* __restrict__ repg,
-                                                 const int* __restrict__ slow, const int* __restrict__ nslow) {
+                                                 const int* __restrict__ slow, const int* __restrict__ nslow,
+                                                 const EP* __restrict__ eps) {
   int n = *nslow;
+  int lane = threadIdx.x & 31;
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int nwarps = (gridDim.x * blockDim.x) >> 5;
   TableExcl x{t, nl.excl};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  for (int i = warp; i < n; i += nwarps) {
     int v = slow[i];
+    const NLGeom& G = geom_of(nl, v);
+    const int rep = rep_of(nl, v);
+    const EP& ep = nl.vrep ? eps[rep] : ep0;
     d3 p = ld3(P, v);
     PairTest pt = make_pair_test(nl, v, ep.rlc1, ep.rT);
     RepAcc acc{ep.rlc1, ep.rr, 0.0, mk(0, 0, 0), GRAD};
     int co[3];
     in_build_cell(nl, v, p, co);
-    visit_cells(pt, nl, P, v, p, co, x, acc);
-    pot[v] = acc.pot;
-    if (GRAD) st3(repg, v, 2.0 * acc.gr);
+    if (lane < 27) {
+      int ii = co[0] + lane / 9 - 1, jj = co[1] + (lane / 3) % 3 - 1, kk = co[2] + lane % 3 - 1;
+      if (ii >= 0 && ii < G.shape[0] && jj >= 0 && jj < G.shape[1] && kk >= 0 && kk < G.shape[2]) {
+        long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
+        int st = 0;
+        int cnt = cell_find(nl, cell_key(cid, rep), &st);
+        for (int q = 0; q < cnt; ++q) {
+          int j = nl.cell_verts[st + q];
+          if (j != v) visit_pair(pt, nl, P, v, p, j, x, acc);
+        }
+      }
+    }
+    double s = acc.pot, gx = acc.gr.x, gy = acc.gr.y, gz = acc.gr.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_down_sync(0xffffffffu, s, o);
+      if (GRAD) {
+        gx += __shfl_down_sync(0xffffffffu, gx, o);
+        gy += __shfl_down_sync(0xffffffffu, gy, o);
+        gz += __shfl_down_sync(0xffffffffu, gz, o);
+      }
+    }
+    if (lane == 0) {
+      pot[v] = s;
+      if (GRAD) st3(repg, v, 2.0 * mk(gx, gy, gz));
+    }
   }
 }
 
@@ -86,11 +128,11 @@ inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 }  // namespace
 
 void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos32, bool want_grad,
-                    double* pot, double* repg, int* slow, int* nslow, cudaStream_t s) {
+                    double* pot, double* repg, int* slow, int* nslow, cudaStream_t s, const EP* eps) {
   int nv = m->nv;
   if (nv == 0) return;
   EP ep = make_ep(e);
-  if (!(ep.rlc1 > 0)) {  // no pair can be closer than a non-positive cut-off
+  if (!eps && !(ep.rlc1 > 0)) {  // no pair can be closer than a non-positive cut-off
     TM_CUDA(cudaMemsetAsync(pot, 0, sizeof(double) * nv, s));
     if (want_grad) TM_CUDA(cudaMemsetAsync(repg, 0, sizeof(double) * 3 * nv, s));
     return;
@@ -100,16 +142,16 @@ void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos3
   nlv.pos32 = pos32;
   TM_CUDA(cudaMemsetAsync(nslow, 0, sizeof(int), s));
   if (want_grad)
-    k_rep_fast<true><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+    k_rep_fast<true><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps);
   else
-    k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+    k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps);
   TM_LAUNCH();
   if (nlv.kind == 0) {
-    int grid = std::min(nblk(nv, 256), 4 * 152);
+    int grid = 8 * 152;  // 8 warps per block, one warp per queued vertex
     if (want_grad)
-      k_rep_slow<true><<<grid, 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+      k_rep_slow<true><<<grid, 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps);
     else
-      k_rep_slow<false><<<grid, 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow);
+      k_rep_slow<false><<<grid, 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps);
     TM_LAUNCH();
   }
 }

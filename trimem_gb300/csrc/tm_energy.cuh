@@ -137,10 +137,27 @@ __device__ __forceinline__ void visit_pair(const PairTest& pt, const NLView& nl,
   if (nl.excl > 0 && is_excluded(v, j)) return;
   fn(j, __dsqrt_rn(s), exact_diff(p, pj));
 }
+// Cell coordinate from the float copy of the position when the float
+// quotient is clearly away from an integer: its error is bounded by
+// 2^-23 (|p| + |bmin| + |p - bmin|) / rl + 2^-23 |t| (four times the
+// rounding bound); otherwise the exact FP64 coordinate.
+__device__ __forceinline__ int cell_coord_f(float pf, double p, const NLGeom& G, int k) {
+  float q = pf - G.bminf[k];
+  float t = q * G.inv_rlf[k];
+  float ti = truncf(t);
+  float fr = fabsf(t - ti);
+  float margin = 1.1920929e-07f * ((fabsf(pf) + fabsf(G.bminf[k]) + fabsf(q)) * G.inv_rlf[k] + fabsf(t) + 1.0f);
+  if (fr > margin && fr < 1.0f - margin && fabsf(t) < 1.0e6f) return (int)ti;
+  return cell_coord(p, G, k);
+}
 __device__ __forceinline__ bool in_build_cell(const NLView& nl, int v, d3 p, int* co) {
-  const NLGeom& G = *nl.geom;
+  const NLGeom& G = geom_of(nl, v);
   const double* pp = &p.x;
-  for (int k = 0; k < 3; ++k) co[k] = cell_coord(pp[k], G, k);
+  if (nl.pos32) {
+    for (int k = 0; k < 3; ++k) co[k] = cell_coord_f(nl.pos32[3 * v + k], pp[k], G, k);
+  } else {
+    for (int k = 0; k < 3; ++k) co[k] = cell_coord(pp[k], G, k);
+  }
   return nl.crow && co[0] == nl.bcoord[3 * v] && co[1] == nl.bcoord[3 * v + 1] && co[2] == nl.bcoord[3 * v + 2];
 }
 template <class F, class X>
@@ -152,7 +169,8 @@ __device__ __forceinline__ void visit_candidates(const PairTest& pt, const NLVie
 template <class F, class X>
 __device__ __forceinline__ void visit_cells(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
                                             const int* co, const X& is_excluded, F& fn) {
-  const NLGeom& G = *nl.geom;
+  const NLGeom& G = geom_of(nl, v);
+  const int rep = rep_of(nl, v);
   for (int a = -1; a < 2; ++a) {
     int ii = co[0] + a;
     if (ii < 0 || ii >= G.shape[0]) continue;
@@ -164,7 +182,7 @@ __device__ __forceinline__ void visit_cells(const PairTest& pt, const NLView& nl
         if (kk < 0 || kk >= G.shape[2]) continue;
         long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
         int st = 0;
-        int cnt = cell_find(nl, cid, &st);
+        int cnt = cell_find(nl, cell_key(cid, rep), &st);
         for (int q = 0; q < cnt; ++q) {
           int j = nl.cell_verts[st + q];
           if (j != v) visit_pair(pt, nl, P, v, p, j, is_excluded, fn);
@@ -250,5 +268,39 @@ __device__ __forceinline__ double energy_of(const EP& ep, const double* p) {
 }
 
 EP make_ep(const tm_energy* e);
+
+// Appends idx to list (count in *cnt) with one atomic per warp.
+__device__ __forceinline__ void warp_append(bool need, int idx, int* list, int* cnt) {
+  unsigned mask = __ballot_sync(__activemask(), need);
+  if (!need) return;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(mask) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(cnt, __popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  list[base + __popc(mask & ((1u << lane) - 1u))] = idx;
+}
+
+// Flat-bottom edge penalty and its derivative dB/dl
+// (src/mesh_tether.h:29-85) for an edge of length l.
+__device__ __forceinline__ void edge_bond(const EP& ep, double l, double* val, double* fac) {
+  int r = ep.r;
+  double v = 0.0, f = 0.0;
+  if (l > ep.lc0) {
+    v = ipow((double)r, r + 1) * ipow(l - ep.lc0, r);
+    f = ipow((double)r, r + 2) * ipow(l - ep.lc0, r - 1);
+  }
+  if (l < ep.lc1) {
+    double lmc = l - ep.lc1;
+    double ex = exp(l / lmc);
+    double ilr = 1.0 / ipow(l, r);
+    if (!(l > ep.lc0)) v = ex * ilr;
+    f -= ep.lc1 / (lmc * lmc) + r / l;
+    f *= ilr;
+    f *= ex;
+  }
+  *val = v;
+  *fac = f;
+}
 
 }  // namespace tmg

@@ -86,6 +86,7 @@ struct CellEntry {
 // Cell geometry, derived on the device from the bounding box.
 struct NLGeom {
   double bmin[3], rl[3], inv_rl[3];
+  float bminf[3], inv_rlf[3];  // float copies for the fast binning test
   int shape[3];
   int pad;
   long long stride[3];
@@ -93,7 +94,10 @@ struct NLGeom {
 struct NLView {
   int kind;  // 0 cell list, 1 Verlet list
   int excl;
+  // cell geometry; for a batch of replicas one entry per replica selected by
+  // vrep (vertex -> replica), and hash keys carry the replica in bits 44+
   const NLGeom* geom;
+  const int* vrep;
   const CellEntry* table;
   unsigned long long tmask;
   const int* cell_verts;
@@ -107,6 +111,12 @@ struct NLView {
   const int* bcoord;   // build-time cell coordinates, 3 per vertex
   const float* pos32;  // positions rounded to float (prefilter), may be NULL
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ int rep_of(const NLView& nl, int v) { return nl.vrep ? nl.vrep[v] : 0; }
+__device__ __forceinline__ const NLGeom& geom_of(const NLView& nl, int v) { return nl.geom[rep_of(nl, v)]; }
+__device__ __forceinline__ long long cell_key(long long cid, int rep) { return cid + ((long long)rep << 44); }
+#endif
 
 struct TopoW;
 
@@ -155,6 +165,7 @@ struct tm_nlist {
 };
 
 namespace tmg {
+struct EP;
 // device-side scalar state of an energy manager
 struct Globals {
   double props[8];  // area, volume, curvature, bending, tethering, repulsion
@@ -191,7 +202,10 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* d_points, bool w
 // repulsion stage: per-vertex potential (and 2 x its gradient) into pot /
 // repg; slow must hold nv + 1 ints
 void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos32, bool want_grad, double* pot,
-                    double* repg, int* slow, int* nslow, cudaStream_t s);
+                    double* repg, int* slow, int* nslow, cudaStream_t s, const EP* eps = nullptr);
+// batch of replicas, FP32 stencils and FP64 sums per replica
+void energy_eval_batch32(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, const EP* eps,
+                         const int* vrep, const int2* rblocks, Globals* gs, const int* blk, cudaStream_t s);
 // double-float stencil variant (stencil mode 2)
 void energy_eval_df(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, double* d_grad,
                     cudaStream_t s, cudaEvent_t* ev);
@@ -203,6 +217,10 @@ void energy_from_props_device(tm_energy* e, const double* d_props6, double* d_ou
 // nlist.cu
 void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* d_points, cudaStream_t s);
 int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* d_points, double rdist, cudaStream_t s);
+// cell list over a batch of replicas (disjoint-union mesh with replica-aligned
+// 256-vertex blocks): per-replica boxes and cut-offs, replica-tagged cells
+void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
+                      const double* d_rlist, int excl, const double* d_points, cudaStream_t s);
 int64_t nlist_point_distances(tm_nlist* nl, tm_mesh* m, const double* d_points, int pid, double rdist,
                               cudaStream_t s);
 // smallest double T with sqrt(T) >= d (IEEE round-to-nearest sqrt), so that
