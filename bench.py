@@ -42,7 +42,7 @@ UNIT = "evals/s"
 
 
 def workload():
-    from helpers import workload_params
+    from trimem_gb300.workloads import workload_params
     from trimem_gb300 import meshgen
 
     p, f = meshgen.jittered_icosphere(LEVEL, seed=0)
@@ -166,7 +166,7 @@ def batch_leg(stream, n_rep=48, n_leapfrog=10, n_steps=20):
 
     import torch
 
-    from helpers import workload_params
+    from trimem_gb300.workloads import workload_params
     from trimem_gb300 import capi, meshgen
 
     L = capi.lib()
@@ -214,6 +214,44 @@ def batch_leg(stream, n_rep=48, n_leapfrog=10, n_steps=20):
             "speedup": round(batch_rate / seq_rate, 2),
             "acceptance": round(float(acc.mean()) / n_steps, 3),
             "timing": "wall clock around the synchronising call (batch) or sweep loop (sequential)"}
+
+
+def chain_leg(stream, stencil, n_burn=30, n_steps=150, weights=None):
+    """ESS/s of the bending energy of a device chain on the 163,842-vertex
+    mesh: per step one HMC move (20 velocity-Verlet steps, dt 5e-5, m 1, T 1)
+    and one flip sweep (ratio 0.2, 98,304 attempts), neighbour list rebuilt
+    every step.  The area and volume targets are the initial ones
+    (continuation lambda 0), so the chain samples around its start instead
+    of collapsing towards the 0.65 reduced volume, which an ESS needs."""
+    import torch
+
+    from trimem_gb300 import capi
+    from trimem_gb300.mc.device import DeviceChain
+    from trimem_gb300.mc.ess import ess
+
+    p, f, prm = workload()
+    prm = dict(prm, cont_lambda=0.0)
+    mesh = capi.Mesh(p, f)
+    en = capi.Energy(mesh, capi.params(**prm))
+    en.set_stencil_precision(stencil)
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    sg = capi.Surrogate(mesh, weights) if weights is not None else None
+    ch = DeviceChain(mesh, en, x, dt=5e-5, n_leapfrog=20, flip_ratio=0.2, seed=11, stream=stream, force=sg)
+    ch.run(n_burn)
+    torch.cuda.synchronize()
+    a0, f0 = ch.accepted, ch.flips
+    t0 = time.perf_counter()
+    trace = ch.run(n_steps)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    bend = prm["kappa_b"] * trace[:, 3]
+    e = ess(bend)
+    return {"steps": n_steps, "burn_in": n_burn, "seconds": round(t1 - t0, 3),
+            "ms_per_step": round((t1 - t0) * 1e3 / n_steps, 3),
+            "acceptance": round((ch.accepted - a0) / n_steps, 3),
+            "flips_accepted_per_sweep": round((ch.flips - f0) / n_steps, 1),
+            "ess_bending": round(e, 2), "ess_per_s": round(e / (t1 - t0), 3),
+            "bending_mean": float(bend.mean()), "bending_sd": float(bend.std())}
 
 
 def run_reference(args):
@@ -468,6 +506,18 @@ def main():
     except Exception as exc:  # the headline line is printed either way
         batch = {"error": f"{type(exc).__name__}: {exc}"}
 
+    chain = {}
+    for name, kw in [("plain_fp64", dict(stencil=0)), ("plain_df64", dict(stencil=2)),
+                     ("surrogate", dict(stencil=0, weights="L7"))]:
+        try:
+            if kw.get("weights") == "L7":
+                from trimem_gb300 import surrogate as S
+
+                kw["weights"] = np.load(S.WEIGHTS_L7)
+            chain[name] = chain_leg(stream, **kw)
+        except Exception as exc:
+            chain[name] = {"error": f"{type(exc).__name__}: {exc}"}
+
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(p, f, prm)
@@ -481,6 +531,7 @@ def main():
                               "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4)}),
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(), "fp32_stencil": fp32, "df64_stencil": df64,
             "batch_replicas": batch,
+            "hmc_chain": chain,
             "gpu_launches": launches_per_step * args.steps, "notes": peaks_fp64}
     if rank == 0:
         print(json.dumps(line), flush=True)

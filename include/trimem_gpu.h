@@ -178,10 +178,43 @@ int tm_fd_gradient(tm_mesh* m, tm_energy* e, double eps, double* grad);
  * (seed, step), n_steps velocity-Verlet steps of size dt with mass m, then
  * accept with probability min(1, exp(-dH/T)) using the uniform u.
  * d_x (n_vertices*3) is updated in place when accepted.  out[0] = accepted,
- * out[1] = H(start), out[2] = H(end), out[3] = energy of the returned state.
+ * out[1] = H(start), out[2] = H(end), out[3] = energy of the returned state;
+ * props6 (may be NULL) receives the six global properties of the returned
+ * state (area, volume, curvature, bending, tethering, repulsion).
  * The neighbour list is the one of the energy manager (not rebuilt). */
 int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double mass, double dt, int n_steps,
-                       double temperature, uint64_t seed, uint64_t step, double u, double* out4, void* stream);
+                       double temperature, uint64_t seed, uint64_t step, double u, double* out4, double* props6,
+                       void* stream);
+
+/* ---- learned surrogate force (no counterpart in the reference) ---------------
+ * A message-passing network (3 rounds, width 64, bf16 dense layers on the
+ * tensor cores) that stands in for the bending and repulsion forces; the
+ * local penalty forces stay exact (FP32 stencils).  weights: the float32 blob
+ * written by trimem_gb300.surrogate (26,442 values).  The surrogate drives
+ * the leapfrog of tm_surrogate_hmc_step_device; acceptance uses the exact
+ * FP64 Hamiltonian of the energy manager. */
+typedef struct tm_surrogate tm_surrogate;
+int tm_surrogate_create(tm_mesh* m, const float* weights, int64_t n_weights, tm_surrogate** out);
+int tm_surrogate_destroy(tm_surrogate* s);
+/* surrogate gradient (the force is its negative), device arrays n_vertices*3 */
+int tm_surrogate_gradient_device(tm_surrogate* s, tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
+                                 void* stream);
+/* network inputs for training, device arrays: d_u (nv x 8), d_normals (nv x 4),
+ * slot-major [max_valence][nv] neighbours (-1 past the valence), edge
+ * features (x 4) and unit edge directions (x 3), and the exact gradient of
+ * the local terms (nv x 3 doubles) */
+int tm_surrogate_inputs_device(tm_surrogate* s, tm_energy* e, tm_mesh* m, const double* d_points, int32_t max_valence,
+                               float* d_u, float* d_normals, int32_t* d_nbr, float* d_edge_feat, float* d_dirs,
+                               double* d_grad_local, void* stream);
+/* HMC step of tm_hmc_step_device with surrogate forces in the leapfrog */
+int tm_surrogate_hmc_step_device(tm_surrogate* s, tm_energy* e, tm_mesh* m, double* d_x, double mass, double dt,
+                                 int n_steps, double temperature, uint64_t seed, uint64_t step, double u, double* out4,
+                                 double* props6, void* stream);
+/* One dense layer of the network on the tensor cores: out = h + SiLU([h | m] W^T + b)
+ * with h, m, out bf16 (rows x 64, row-major, 16-byte aligned), W bf16 (64 x 128)
+ * and b float (64). */
+int tm_dense_silu_bf16(const void* d_h, const void* d_m, const void* d_w, const float* d_bias, void* d_out,
+                       int64_t rows, void* stream);
 
 /* ---- batches of replicas (no counterpart in the reference: the reference
  * runs one membrane per process) -------------------------------------------

@@ -42,3 +42,26 @@ def test_device_hmc_step_conserves_energy_and_is_reversible(built):
     acc, h0, h1, e = estore.hmc_step_device(mesh, xs.data_ptr(), 1.0, 1e-3, 5, 1.0, 7, 0, 1.0 - 1e-16)
     if not acc:
         assert torch.equal(xs, x)
+
+
+def test_device_chain_records_the_returned_states(built):
+    """The chain driver: properties recorded per step are those of the state
+    the HMC move returned; with flip sweeps the mesh stays valid."""
+    import torch
+
+    from trimem_gb300 import capi
+    from trimem_gb300.mc.device import DeviceChain
+
+    p, f = meshgen.jittered_icosphere(3, seed=2)
+    prm = dict(workload_params(p, f), cont_lambda=0.0)
+    m = capi.Mesh(p, f)
+    e = capi.Energy(m, capi.params(**prm))
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    ch = DeviceChain(m, e, x, dt=2e-6, n_leapfrog=5, flip_ratio=0.0, seed=3, refresh=0)
+    trace = ch.run(6)
+    assert ch.accepted > 0
+    m.points()[:] = x.cpu().numpy()
+    np.testing.assert_allclose(trace[-1], e.properties(m)[:6], rtol=1e-12)
+    ch2 = DeviceChain(m, e, x, dt=2e-6, n_leapfrog=5, flip_ratio=0.2, seed=4, refresh=1)
+    ch2.run(4)
+    assert ch2.flips > 0 and m.check() == 0

@@ -200,8 +200,39 @@ def test_flip_on_jittered_mesh_with_repulsion(C):
     ag = C.flip(mg, eg, 0.2, 21, 1, 512)
     assert ag == ao
     assert np.array_equal(mg.fv_indices(), mo.fv_indices())
-    # energies on the flipped meshes agree as well
+    # energies on the flipped meshes agree as well (the repulsion re-tests
+    # exclusions on the new topology), also after a small displacement
     assert abs(eg.energy(mg) - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+    d = np.random.default_rng(2).normal(0, 1e-3 * meshgen.mean_edge_length(p, f), size=p.shape)
+    mo.points()[:] += d
+    mg.points()[:] += d
+    for stencil in (0, 2):
+        eg.set_stencil_precision(stencil)
+        eng, gg = eg.gradient(mg, with_energy=True)
+        assert abs(eng - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+        assert rel(gg, eo.gradient(mo)) < RTOL
+
+
+def test_repulsion_after_a_large_move(C):
+    """One vertex moved by more than half the repulsion cut-off since the
+    cell-list build: the evaluation leaves the near rows for the full
+    candidate rows and still matches the oracle on the same cells."""
+    p, f = meshgen.jittered_icosphere(3, seed=5)
+    prm = workload_params(p, f, excl=1, rep_scale=1.3)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    rng = np.random.default_rng(3)
+    d = rng.normal(0, 1e-3 * meshgen.mean_edge_length(p, f), size=p.shape)
+    d[17, 0] += 0.7 * prm["rep_lc1"]
+    mo.points()[:] += d
+    mg.points()[:] += d
+    assert eo.properties(mo)[5] > 0  # pairs inside the cut-off exist
+    for stencil in (0, 1, 2):
+        eg.set_stencil_precision(stencil)
+        tol = 1e-5 if stencil == 1 else RTOL
+        eng, gg = eg.gradient(mg, with_energy=True)
+        assert abs(eng - eo.energy(mo)) <= tol * abs(eo.energy(mo)), stencil
+        assert rel(gg, eo.gradient(mo)) < tol * 10, stencil
+        assert abs(eg.properties(mg)[5] - eo.properties(mo)[5]) <= RTOL * eo.properties(mo)[5], stencil
 
 
 def test_flip_ratio_errors(C):

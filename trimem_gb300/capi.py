@@ -98,7 +98,7 @@ _SIGS = {
     "tm_edges_length": (_i32, [_p, _dp]),
     "tm_avg_tri_props": (_i32, [_p, _dp, _dp]),
     "tm_fd_gradient": (_i32, [_p, _p, _d, _dp]),
-    "tm_hmc_step_device": (_i32, [_p, _p, _p, _d, _d, _i32, _d, ctypes.c_uint64, ctypes.c_uint64, _d, _dp, _p]),
+    "tm_hmc_step_device": (_i32, [_p, _p, _p, _d, _d, _i32, _d, ctypes.c_uint64, ctypes.c_uint64, _d, _dp, _dp, _p]),
     "tm_batch_create": (_i32, [_i32, ctypes.POINTER(_dp), _i64p, ctypes.POINTER(_ip), _i64p, ctypes.POINTER(Params), _pp]),
     "tm_batch_destroy": (_i32, [_p]),
     "tm_batch_layout": (_i32, [_p, _i64p, _i64p]),
@@ -106,6 +106,13 @@ _SIGS = {
     "tm_batch_energy": (_i32, [_p, _dp, _dp]),
     "tm_batch_update_repulsion": (_i32, [_p]),
     "tm_batch_hmc": (_i32, [_p, _i32, _i32, _d, _d, _d, ctypes.c_uint64, _i32, _ip]),
+    "tm_surrogate_create": (_i32, [_p, ctypes.POINTER(ctypes.c_float), _i64, _pp]),
+    "tm_surrogate_destroy": (_i32, [_p]),
+    "tm_surrogate_gradient_device": (_i32, [_p, _p, _p, _p, _p, _p]),
+    "tm_surrogate_inputs_device": (_i32, [_p, _p, _p, _p, _i32, _p, _p, _p, _p, _p, _p, _p]),
+    "tm_surrogate_hmc_step_device": (_i32, [_p, _p, _p, _p, _d, _d, _i32, _d, ctypes.c_uint64, ctypes.c_uint64, _d,
+                                            _dp, _dp, _p]),
+    "tm_dense_silu_bf16": (_i32, [_p, _p, _p, _p, _p, _i64, _p]),
 }
 
 _lib = None
@@ -370,6 +377,25 @@ class Batch:
         check(lib().tm_batch_hmc(self.h, int(n_steps), int(n_leapfrog), float(dt), float(mass),
                                  float(temperature), int(seed), int(bool(use_graph)), _iptr(acc)))
         return acc
+
+
+class Surrogate:
+    """tm_surrogate handle: the learned force model of a mesh (weights: the
+    float32 blob of trimem_gb300.surrogate)."""
+
+    def __init__(self, mesh, weights):
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        h = ctypes.c_void_p()
+        check(lib().tm_surrogate_create(mesh.h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(w),
+                                        ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().tm_surrogate_destroy(self.h)
+            self.h = None
+
+    __del__ = close
 
 
 def flip(mesh, energy, ratio, seed, mode, batch=256):

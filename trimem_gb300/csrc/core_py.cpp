@@ -594,7 +594,7 @@ PYBIND11_MODULE(core, m) {
           [](EnergyManager& e, TriMesh& t, uintptr_t x, double mass, double dt, int n_steps, double temp,
              uint64_t seed, uint64_t step, double u, uintptr_t stream) {
             double out[4];
-            check(tm_hmc_step_device(e.h, t.h, (double*)x, mass, dt, n_steps, temp, seed, step, u, out,
+            check(tm_hmc_step_device(e.h, t.h, (double*)x, mass, dt, n_steps, temp, seed, step, u, out, nullptr,
                                      (void*)stream));
             return py::make_tuple(out[0] != 0.0, out[1], out[2], out[3]);
           },

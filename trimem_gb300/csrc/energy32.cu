@@ -17,52 +17,13 @@
 #include "tm_energy.cuh"
 #include "tm_internal.h"
 #include "tm_math.cuh"
+#include "tm_fp32.cuh"
 
 namespace tmg {
 
-struct __align__(16) FaceF {
-  float nx, ny, nz, A, V, c0, c1, c2;
-};
-struct __align__(16) EdgeF {
-  float l, th, db, flag;
-};
-
 namespace {
 
-struct f3 {
-  float x, y, z;
-};
-__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ f3 operator*(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ f3& operator+=(f3& a, f3 b) {
-  a.x += b.x;
-  a.y += b.y;
-  a.z += b.z;
-  return a;
-}
-__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ f3 fcross(f3 a, f3 b) {
-  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-__device__ __forceinline__ float fnorm(f3 a) { return sqrtf(fdot(a, a)); }
-__device__ __forceinline__ float fipow(float x, int n) {
-  int a = n < 0 ? -n : n;
-  float r = 1.0f;
-  for (int k = 0; k < a; ++k) r *= x;
-  return n < 0 ? 1.0f / r : r;
-}
-
-struct Split {
-  const float* hi;
-  const float* lo;
-  __device__ f3 h(int v) const { return {hi[3 * v], hi[3 * v + 1], hi[3 * v + 2]}; }
-  // x_b - x_a with FP32 relative accuracy
-  __device__ f3 diff(int b, int a) const {
-    return {(hi[3 * b] - hi[3 * a]) + (lo[3 * b] - lo[3 * a]), (hi[3 * b + 1] - hi[3 * a + 1]) + (lo[3 * b + 1] - lo[3 * a + 1]),
-            (hi[3 * b + 2] - hi[3 * a + 2]) + (lo[3 * b + 2] - lo[3 * a + 2])};
-  }
-};
+using namespace fp32;
 
 __global__ void k_split(int nv, const double* __restrict__ P, float* __restrict__ hi, float* __restrict__ lo) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -511,6 +472,39 @@ void energy_eval32(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bo
   if (want_grad && t.nv) k_grad32<<<nblk(t.nv, 256), 256, 0, s>>>(t, S, fd, ed, rho, repg, e->glob.get(), ep, d_grad);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[4], s));
+}
+
+// The local terms of the energy only (bending and repulsion weights set to
+// zero, no neighbour pass) with FP32 stencils: the exact part of the
+// surrogate force.  Leaves the FP32 face / edge records, rho = c/a per vertex
+// and the split positions (e->pos32, e->poslo) filled for the caller.
+void energy_eval32_local(tm_energy* e, tm_mesh* m, const double* P, double* d_grad, cudaStream_t s) {
+  e->ensure(m->nv, m->ne, m->nf);
+  size_t nv = std::max(m->nv, 1);
+  Topo t = m->topo();
+  EP ep = make_ep(e);
+  ep.kb = 0.0;
+  ep.kr = 0.0;
+  e->pos32.ensure(3 * nv);
+  e->poslo.ensure(3 * nv);
+  Split S{e->pos32.get(), e->poslo.get()};
+  FaceF* fd = reinterpret_cast<FaceF*>(e->face.get());
+  EdgeF* ed = reinterpret_cast<EdgeF*>(e->edge.get());
+  float* eb = reinterpret_cast<float*>(e->ebond.get());
+  float* rho = reinterpret_cast<float*>(e->rho.get());
+  TM_CUDA(cudaMemsetAsync(e->reppot.get(), 0, sizeof(double) * nv, s));
+  TM_CUDA(cudaMemsetAsync(e->repg.get(), 0, sizeof(double) * 3 * nv, s));
+  if (m->nv) k_split<<<nblk(3L * m->nv, 256), 256, 0, s>>>(m->nv, P, e->pos32.get(), e->poslo.get());
+  TM_LAUNCH();
+  if (t.nf) k_face32<<<nblk(t.nf, 256), 256, 0, s>>>(t, S, fd);
+  TM_LAUNCH();
+  if (t.ne) k_edge32<<<nblk(t.ne, 256), 256, 0, s>>>(t, S, fd, ed, eb, ep);
+  TM_LAUNCH();
+  int nb = std::max(1, nblk(t.nv, VB));
+  k_vertex32<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), ep, rho, e->partials.get(), e->glob.get());
+  TM_LAUNCH();
+  if (t.nv) k_grad32<<<nblk(t.nv, 256), 256, 0, s>>>(t, S, fd, ed, rho, e->repg.get(), e->glob.get(), ep, d_grad);
+  TM_LAUNCH();
 }
 
 void energy_eval_batch32(tm_energy* e, tm_mesh* m, const double* P, double* d_grad, const EP* eps,

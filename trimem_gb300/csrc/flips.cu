@@ -488,6 +488,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     // least one proposal and the loop ends
   }
   m->host_topo_stale = true;
+  if (hs.acc > 0) ++m->topo_version;
   return hs.acc;
 }
 

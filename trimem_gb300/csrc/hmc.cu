@@ -96,8 +96,9 @@ __global__ void k_dot_final(int nb, const double* part, double* out) {
   if (threadIdx.x == 0) *out = s[0];
 }
 
-// out4 = {accepted, H0, H1, E(returned)}; sc = {E0, pp0, E1, pp1}
-__global__ void k_accept(const double* sc, double m, double T, double u, double* out4, int* flag) {
+// out4 = {accepted, H0, H1, E(returned)}; sc = {E0, pp0, E1, pp1};
+// props: 8 properties at the start, 8 at the end, 8 of the returned state
+__global__ void k_accept(const double* sc, double m, double T, double u, double* out4, int* flag, double* props) {
   if (threadIdx.x || blockIdx.x) return;
   double H0 = sc[0] + 0.5 * sc[1] / m;
   double H1 = sc[2] + 0.5 * sc[3] / m;
@@ -109,6 +110,7 @@ __global__ void k_accept(const double* sc, double m, double T, double u, double*
   out4[2] = H1;
   out4[3] = acc ? sc[2] : sc[0];
   *flag = acc;
+  for (int k = 0; k < 8; ++k) props[16 + k] = acc ? props[8 + k] : props[k];
 }
 __global__ void k_copy_if(int n, const int* flag, const double* a, double* b) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -119,17 +121,18 @@ inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
 
-extern "C" int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double mass, double dt, int n_steps,
-                                  double temperature, uint64_t seed, uint64_t step, double u, double* out4,
-                                  void* stream) {
-  TM_API_BEGIN
-  if (!e || !m || !d_x || !out4) fail(TM_ERR_ARG, "NULL argument");
+// One HMC step; the leapfrog forces come from the energy manager (exact,
+// at its stencil precision) or, when sg is given, from the surrogate, in
+// which case the start and end energies are separate exact evaluations.
+static void hmc_step(tm_surrogate* sg, tm_energy* e, tm_mesh* m, double* d_x, double mass, double dt, int n_steps,
+                     double temperature, uint64_t seed, uint64_t step, double u, double* out4, double* props6,
+                     cudaStream_t s) {
+  if (!d_x || !out4) fail(TM_ERR_ARG, "NULL argument");
   if (n_steps < 0 || !(mass > 0) || !(temperature > 0)) fail(TM_ERR_ARG, "invalid HMC parameters");
-  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
   int n3 = 3 * m->nv;
   // work: x, p, g0, g1, partials, scalars
   int nb = std::max(1, std::min(1024, nblk(n3, 256)));
-  e->work.ensure(4 * (size_t)n3 + nb + 16 + 8);
+  e->work.ensure(4 * (size_t)n3 + nb + 16 + 8 + 24);
   double* x = e->work.get();
   double* p = x + n3;
   double* g0 = p + n3;
@@ -138,6 +141,8 @@ extern "C" int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double 
   double* sc = part + nb;  // 4 scalars
   double* o4 = sc + 8;
   int* flag = reinterpret_cast<int*>(o4 + 4);
+  double* props = o4 + 8;  // 24: start, end, returned
+  const Globals* G = e->glob.get();
   int b = 256;
   k_copy<<<nblk(n3, b), b, 0, s>>>(n3, d_x, x);
   TM_LAUNCH();
@@ -146,25 +151,62 @@ extern "C" int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double 
   k_dot_partial<<<nb, 256, 0, s>>>(n3, p, part);
   k_dot_final<<<1, 256, 0, s>>>(nb, part, sc + 1);
   TM_LAUNCH();
-  energy_eval(e, m, x, true, false, g0, s);
-  TM_CUDA(cudaMemcpyAsync(sc + 0, &e->glob.get()->comps[6], sizeof(double), cudaMemcpyDeviceToDevice, s));
+  auto force = [&](double* g) {
+    if (sg)
+      surrogate_grad(sg, e, m, x, g, s);
+    else
+      energy_eval(e, m, x, true, false, g, s);
+  };
+  auto record = [&](double* E, double* pr) {
+    TM_CUDA(cudaMemcpyAsync(E, &G->comps[6], sizeof(double), cudaMemcpyDeviceToDevice, s));
+    TM_CUDA(cudaMemcpyAsync(pr, G->props, sizeof(double) * 8, cudaMemcpyDeviceToDevice, s));
+  };
+  if (sg) {
+    energy_eval(e, m, x, false, false, nullptr, s);
+    record(sc + 0, props);
+    force(g0);
+  } else {
+    force(g0);
+    record(sc + 0, props);
+  }
   for (int i = 0; i < n_steps; ++i) {
     k_drift<<<nblk(n3, b), b, 0, s>>>(n3, dt, mass, p, g0, x);
     TM_LAUNCH();
-    energy_eval(e, m, x, true, false, g1, s);
+    force(g1);
     k_kick<<<nblk(n3, b), b, 0, s>>>(n3, dt, g0, g1, p);
     TM_LAUNCH();
     std::swap(g0, g1);
   }
-  TM_CUDA(cudaMemcpyAsync(sc + 2, &e->glob.get()->comps[6], sizeof(double), cudaMemcpyDeviceToDevice, s));
+  if (sg) energy_eval(e, m, x, false, false, nullptr, s);
+  record(sc + 2, props + 8);
   k_dot_partial<<<nb, 256, 0, s>>>(n3, p, part);
   k_dot_final<<<1, 256, 0, s>>>(nb, part, sc + 3);
   TM_LAUNCH();
-  k_accept<<<1, 1, 0, s>>>(sc, mass, temperature, u, o4, flag);
+  k_accept<<<1, 1, 0, s>>>(sc, mass, temperature, u, o4, flag, props);
   TM_LAUNCH();
   k_copy_if<<<nblk(n3, b), b, 0, s>>>(n3, flag, x, d_x);
   TM_LAUNCH();
   TM_CUDA(cudaMemcpyAsync(out4, o4, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  if (props6) TM_CUDA(cudaMemcpyAsync(props6, props + 16, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
   TM_CUDA(cudaStreamSynchronize(s));
+}
+
+extern "C" int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double mass, double dt, int n_steps,
+                                  double temperature, uint64_t seed, uint64_t step, double u, double* out4,
+                                  double* props6, void* stream) {
+  TM_API_BEGIN
+  if (!e || !m) fail(TM_ERR_ARG, "NULL argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  hmc_step(nullptr, e, m, d_x, mass, dt, n_steps, temperature, seed, step, u, out4, props6, s);
+  TM_API_END
+}
+
+extern "C" int tm_surrogate_hmc_step_device(tm_surrogate* sg, tm_energy* e, tm_mesh* m, double* d_x, double mass,
+                                            double dt, int n_steps, double temperature, uint64_t seed, uint64_t step,
+                                            double u, double* out4, double* props6, void* stream) {
+  TM_API_BEGIN
+  if (!sg || !e || !m) fail(TM_ERR_ARG, "NULL argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  hmc_step(sg, e, m, d_x, mass, dt, n_steps, temperature, seed, step, u, out4, props6, s);
   TM_API_END
 }

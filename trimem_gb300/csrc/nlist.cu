@@ -424,6 +424,27 @@ __global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt,
   if (!pass) cnt[a] = n;
 }
 
+// Near rows: the candidates of each vertex whose build-time distance is
+// below rn (squared threshold rn2, rounded up), in candidate order; bit 31
+// marks pairs excluded on the build topology.
+__global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, double rn2, int pass, int* cnt,
+                       const int* off, int* out) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nv) return;
+  d3 pa = ld3(P, a);
+  int n = 0;
+  int base = pass ? off[a] : 0;
+  for (int q = nl.crow[a]; q < nl.crow[a + 1]; ++q) {
+    int b = nl.ccol[q];
+    d3 pb = ld3(P, b);
+    double dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+    if (dx * dx + dy * dy + dz * dz >= rn2) continue;
+    if (pass) out[base + n] = nl_excluded(t, excl, a, b) ? (int)(0x80000000u | (unsigned)b) : b;
+    ++n;
+  }
+  if (!pass) cnt[a] = n;
+}
+
 // distance_matrix of the Verlet list: rows in vertex order, d < rd
 __global__ void k_verlet_dm(int nv, const double* P, const int* vrow, const int* vcol, double rd, int pass, int* cnt,
                             const int* off, double* od, int* oi, int* oj) {
@@ -567,6 +588,36 @@ static void build_cells(tm_nlist* nl, NLView& V, int nv, const double* P, cudaSt
   }
 }
 
+// Near rows for repulsion queries at cut-off lc1 (skin lc1): a pair closer
+// than lc1 at query time whose vertices both moved less than lc1/2 since the
+// build was closer than 2 lc1 at the build, so the near row of a vertex that
+// is still in its build cell holds every candidate the query can accept.
+static void build_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, double lc1, cudaStream_t s) {
+  int nv = nl->nv;
+  Topo t = m->topo();
+  double rn = 2.0 * lc1;
+  nl->nrow.ensure((size_t)nv + 1);
+  nl->cnt.ensure((size_t)nv + 1);
+  k_near<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, V.excl, rn * rn * (1.0 + 1e-12), 0, nl->cnt.get(), nullptr,
+                                       nullptr);
+  TM_LAUNCH();
+  TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
+  int total = 0;
+  exclusive_scan_int(nl->cnt.get(), nl->nrow.get(), nv + 1, &total, nl->tmp, s);
+  nl->ncol.ensure(std::max(total, 1));
+  k_near<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, V.excl, rn * rn * (1.0 + 1e-12), 1, nullptr, nl->nrow.get(),
+                                       nl->ncol.get());
+  TM_LAUNCH();
+  nl->xb.ensure(3 * (size_t)nv);
+  TM_CUDA(cudaMemcpyAsync(nl->xb.get(), P, sizeof(double) * 3 * nv, cudaMemcpyDeviceToDevice, s));
+  nl->moved.ensure(1);
+  nl->near_lc1 = lc1;
+  nl->near_move2 = 0.25 * lc1 * lc1 * (1.0 - 1e-12);
+  nl->topo_version = m->topo_version;
+  V.nrow = nl->nrow.get();
+  V.ncol = nl->ncol.get();
+}
+
 void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, cudaStream_t s) {
   if (p.n_search != 0 && p.n_search != 1) fail(TM_ERR_ARG, "Unknown neighbour search algorithm.");
   if (p.exclusion_level < 0 || p.exclusion_level > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
@@ -589,6 +640,7 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
   k_bbox_final<<<1, BB, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
   TM_LAUNCH();
   build_cells(nl, V, nv, P, s, p.n_search == 0);
+  if (p.n_search == 0 && V.crow && p.rep_lc1 > 0) build_near(nl, m, V, P, p.rep_lc1, s);
   if (p.n_search == 1) {
     // Verlet CSR from the cell list at cut-off rlist, rows in the reference's
     // insertion order

@@ -4,7 +4,9 @@
 // gradient, 2 sum_j phi'(l) (x_i - x_j) / l.
 //
 // A vertex whose current position still lies in its build-time cell walks
-// the precomputed candidate row of that cell (k_rep_fast); the few that moved
+// the precomputed candidate row of that cell (k_rep_fast), or only its near
+// row while no vertex has moved lc1/2 since the build (k_moved decides this
+// for the whole mesh before the pass); the few that moved
 // to another cell are queued and walk the 27 cells through the cell table in
 // a second kernel (k_rep_slow), so the long table walk never holds a warp of
 // fast vertices.  Both produce the per-vertex values in the reference's pair
@@ -42,9 +44,11 @@ template <bool GRAD>
 __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restrict__ P, NLView nl, EP ep,
                                                  double* __restrict__ pot, double* __restrict__ repg,
                                                  int* __restrict__ slow, int* __restrict__ nslow,
-                                                 const EP* __restrict__ eps) {
+                                                 const EP* __restrict__ eps, int near_mode,
+                                                 const int* __restrict__ moved) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= t.nv) return;
+  if (near_mode && *moved) near_mode = 0;
   if (nl.vrep) {  // batch: per-replica cut-off, padding vertices have none
     int r = nl.vrep[v];
     if (r < 0) {
@@ -63,7 +67,10 @@ __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restri
     bool fast = in_build_cell(nl, v, p, co);
     warp_append(!fast, v, slow, nslow);
     if (!fast) return;
-    visit_candidates(pt, nl, P, v, p, x, acc);
+    if (near_mode)
+      visit_near(pt, nl, P, v, p, near_mode, x, acc);
+    else
+      visit_candidates(pt, nl, P, v, p, x, acc);
   } else {
     visit_verlet(pt, nl, P, v, p, x, acc);
   }
@@ -123,6 +130,16 @@ __global__ void __launch_bounds__(256) k_rep_slow(Topo t, const double* __restri
   }
 }
 
+// *moved = 1 when some vertex is lc1/2 or farther from its build position
+// (squared threshold thr2, rounded down); NaN counts as moved
+__global__ void k_moved(int nv, const double* __restrict__ P, const double* __restrict__ xb, double thr2,
+                        int* moved) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double dx = P[3 * v] - xb[3 * v], dy = P[3 * v + 1] - xb[3 * v + 1], dz = P[3 * v + 2] - xb[3 * v + 2];
+  if (!(dx * dx + dy * dy + dz * dz < thr2)) atomicOr(moved, 1);
+}
+
 inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
@@ -141,10 +158,19 @@ void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos3
   NLView nlv = e->nl.view;
   nlv.pos32 = pos32;
   TM_CUDA(cudaMemsetAsync(nslow, 0, sizeof(int), s));
+  int near_mode = 0;
+  int* moved = nullptr;
+  if (nlv.kind == 0 && nlv.nrow && !eps && e->nl.near_lc1 == ep.rlc1 && e->nl.nv == nv) {
+    near_mode = m->topo_version == e->nl.topo_version ? 1 : 2;
+    moved = e->nl.moved.get();
+    TM_CUDA(cudaMemsetAsync(moved, 0, sizeof(int), s));
+    k_moved<<<nblk(nv, 256), 256, 0, s>>>(nv, P, e->nl.xb.get(), e->nl.near_move2, moved);
+    TM_LAUNCH();
+  }
   if (want_grad)
-    k_rep_fast<true><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps);
+    k_rep_fast<true><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps, near_mode, moved);
   else
-    k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps);
+    k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps, near_mode, moved);
   TM_LAUNCH();
   if (nlv.kind == 0) {
     int grid = 8 * 152;  // 8 warps per block, one warp per queued vertex

@@ -1,0 +1,548 @@
+// Learned surrogate force for hybrid HMC: the leapfrog integrates
+//   -grad E(x)  ~  -(g_local(x) - F_nn(x)),
+// where g_local is the exact gradient of the local penalty terms (area,
+// volume, area difference, tether; FP32 stencils, one pass without the
+// neighbour list) and F_nn is a message-passing network that stands in for
+// the bending and repulsion forces.  Acceptance always uses the exact FP64
+// Hamiltonian, so the chain samples the exact distribution; the surrogate
+// only changes how often proposals are accepted.
+//
+// Network (width H = 64, SiLU, three rounds), per vertex i with ring j:
+//   u_i   = 8 rotation-invariant vertex features (area, curvature, valence,
+//           dihedral and edge-length statistics of the ring)
+//   e_ij  = 4 edge features (length, dihedral, curvature difference / mean)
+//   h_i   = SiLU(W_in u_i + b_in)
+//   round r:  m_i = sum_j (W_e^r e_ij + b_e^r) * h_j          (gather, CUDA cores)
+//             h_i = h_i + SiLU(W^r [h_i ; m_i] + b^r)          (tcgen05 BF16 GEMM)
+//   F_i   = s ( sum_j c_ij (x_j - x_i)/|x_j - x_i| + c_i N_i ),
+//           c_ij = sum_c w_o,c h_i,c h_j,c + b_o,  c_i = w_n . h_i + b_n,
+//           N_i the area-weighted vertex normal.
+// F is equivariant by construction (invariant coefficients on the edge
+// directions and the normal).  Activations h, m are stored as bf16, the
+// dense weights W^r are bf16 with FP32 accumulation in tensor memory; the
+// small layers are FP32.
+//
+// The dense layer is one CTA per 128 vertices: TMA loads [h | m] (two
+// 128 x 64 bf16 boxes) and W^r (two 64 x 64 boxes) into 128-byte-swizzled
+// shared memory, one thread issues 8 tcgen05.mma (M 128, N 64, K 16), the
+// accumulator (128 lanes x 64 FP32 columns) is read back by four warps and
+// the epilogue adds bias, SiLU and the residual h (from the swizzled tile).
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "tm_energy.cuh"
+#include "tm_fp32.cuh"
+#include "tm_internal.h"
+#include "tm_math.cuh"
+#include "tm_tc.cuh"
+
+using namespace tmg;
+
+#define TM_API_BEGIN try {
+#define TM_API_END                  \
+  }                                 \
+  catch (const tmg::Error& e) {     \
+    tmg::set_last_error(e.what());  \
+    return e.code;                  \
+  }                                 \
+  catch (const std::exception& e) { \
+    tmg::set_last_error(e.what());  \
+    return TM_ERR_ARG;              \
+  }                                 \
+  return TM_OK;
+
+namespace {
+
+constexpr int H = 64, FV = 8, FE = 4, NR = 3, BM = 128;
+constexpr int BLOB_HEADER = 8;
+constexpr int BLOB_SIZE = BLOB_HEADER + H * FV + H + NR * (H * FE + H + H * 2 * H + H) + H + 1 + H + 1;
+
+// FP32 parameters of the small layers (device copy)
+struct SurW {
+  float win[H * FV], bin[H];
+  float we[NR][H * FE], be[NR][H], b[NR][H];
+  float wo[H], wn[H];
+  float bo, bn, lbar, abar, fscale;
+};
+
+}  // namespace
+
+struct tm_surrogate {
+  int nv = 0;
+  SurW hw{};
+  DevBuf<SurW> w;
+  DevBuf<__nv_bfloat16> wd;  // dense weights [NR][H][2H] (row n, column k)
+  DevBuf<float> u, nrm;
+  DevBuf<__nv_bfloat16> hb[2], mb;
+  DevBuf<double> gloc;
+  DevBuf<int> status;
+  alignas(64) CUtensorMap map_h[2];
+  alignas(64) CUtensorMap map_m;
+  alignas(64) CUtensorMap map_w[NR];
+};
+
+namespace {
+
+using namespace tmg::fp32;
+using tmg::tc::smem_u32;
+
+inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+
+__device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x)); }
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// vertex features, normal and embedding (one thread per vertex)
+__global__ void k_sfeat(Topo t, const FaceF* __restrict__ fd, const EdgeF* __restrict__ ed,
+                        const float* __restrict__ rho, const SurW* __restrict__ W, float* __restrict__ u,
+                        float* __restrict__ nrm, __nv_bfloat16* __restrict__ h) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.nv) return;
+  const float lbar = W->lbar, abar = W->abar;
+  int d = t.val[i];
+  float A = 0.f, ls = 0.f, l2 = 0.f, ths = 0.f, th2 = 0.f;
+  f3 N = {0.f, 0.f, 0.f};
+  for (int m = 0; m < d; ++m) {
+    int4 s = t.slot[(size_t)m * t.nv + i];
+    int f = slot_face(s.y);
+    if (f >= 0) {
+      FaceF F = fd[f];
+      A += F.A;
+      N += F.A * f3{F.nx, F.ny, F.nz};
+    }
+    EdgeF E = ed[s.z];
+    float lr = E.l / lbar;
+    ls += lr;
+    l2 += lr * lr;
+    ths += E.th;
+    th2 += E.th * E.th;
+  }
+  float inv_d = d > 0 ? 1.0f / d : 0.0f;
+  float x[FV];
+  float rl = rho[i] * lbar;
+  x[0] = (A / 3.0f) / abar - 1.0f;
+  x[1] = rl;
+  x[2] = rl * rl;
+  x[3] = (d - 6) * (1.0f / 6.0f);
+  x[4] = ths * inv_d;
+  x[5] = sqrtf(th2 * inv_d);
+  x[6] = ls * inv_d - 1.0f;
+  x[7] = sqrtf(fmaxf(l2 * inv_d - (ls * inv_d) * (ls * inv_d), 0.0f));
+  for (int k = 0; k < FV; ++k) u[(size_t)FV * i + k] = x[k];
+  float nn = fnorm(N);
+  float in = nn > 0.f ? 1.0f / nn : 0.0f;
+  nrm[4 * (size_t)i] = N.x * in;
+  nrm[4 * (size_t)i + 1] = N.y * in;
+  nrm[4 * (size_t)i + 2] = N.z * in;
+  nrm[4 * (size_t)i + 3] = 0.f;
+  __nv_bfloat162* h2 = reinterpret_cast<__nv_bfloat162*>(h + (size_t)H * i);
+  for (int c = 0; c < H; c += 2) {
+    float y0 = W->bin[c], y1 = W->bin[c + 1];
+    for (int k = 0; k < FV; ++k) {
+      y0 += W->win[c * FV + k] * x[k];
+      y1 += W->win[(c + 1) * FV + k] * x[k];
+    }
+    h2[c / 2] = __floats2bfloat162_rn(silu(y0), silu(y1));
+  }
+}
+
+__device__ __forceinline__ void edge_feat(const EdgeF& E, float ri, float rj, float lbar, float* ef) {
+  ef[0] = E.l / lbar - 1.0f;
+  ef[1] = E.th;
+  ef[2] = (rj - ri) * lbar;
+  ef[3] = 0.5f * (rj + ri) * lbar;
+}
+
+// m_i = sum_j (W_e e_ij + b_e) * h_j (one warp per vertex, two channels per lane)
+__global__ void k_agg(Topo t, const EdgeF* __restrict__ ed, const float* __restrict__ rho,
+                      const SurW* __restrict__ W, int r, const __nv_bfloat16* __restrict__ h,
+                      __nv_bfloat16* __restrict__ mout) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= t.nv) return;
+  const int c0 = 2 * lane, c1 = c0 + 1;
+  float w0[FE], w1[FE];
+  for (int k = 0; k < FE; ++k) {
+    w0[k] = W->we[r][c0 * FE + k];
+    w1[k] = W->we[r][c1 * FE + k];
+  }
+  const float b0 = W->be[r][c0], b1 = W->be[r][c1], lbar = W->lbar;
+  const float ri = rho[i];
+  const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(h);
+  float a0 = 0.f, a1 = 0.f;
+  int d = t.val[i];
+  for (int m = 0; m < d; ++m) {
+    int4 s = t.slot[(size_t)m * t.nv + i];
+    int j = s.x;
+    float ef[FE];
+    edge_feat(ed[s.z], ri, rho[j], lbar, ef);
+    float g0 = b0, g1 = b1;
+    for (int k = 0; k < FE; ++k) {
+      g0 += w0[k] * ef[k];
+      g1 += w1[k] * ef[k];
+    }
+    float2 hj = __bfloat1622float2(h2[(size_t)j * (H / 2) + lane]);
+    a0 += g0 * hj.x;
+    a1 += g1 * hj.y;
+  }
+  reinterpret_cast<__nv_bfloat162*>(mout)[(size_t)i * (H / 2) + lane] = __floats2bfloat162_rn(a0, a1);
+}
+
+// h_out = h + SiLU([h | m] W^T + b) for 128 vertices per CTA on the tensor cores
+constexpr int DENSE_SMEM = 1024 + 49152 + 64;
+
+__global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorMap mh,
+                                               const __grid_constant__ CUtensorMap mm,
+                                               const __grid_constant__ CUtensorMap mw, const float* __restrict__ bias,
+                                               __nv_bfloat16* __restrict__ out, int M, int* status) {
+  using namespace tmg::tc;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* A0 = base;           // h tile, 128 rows x 128 B
+  uint8_t* A1 = base + 16384;   // m tile
+  uint8_t* B0 = base + 32768;   // W[:, 0:64], 64 rows x 128 B
+  uint8_t* B1 = base + 40960;   // W[:, 64:128]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(base + 49152);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(base + 49152 + 16);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM;
+  if (threadIdx.x == 0) {
+    tma_prefetch_desc(&mh);
+    tma_prefetch_desc(&mm);
+    tma_prefetch_desc(&mw);
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tslot, 64);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&bars[0], 49152);
+    tma_load_2d(A0, &mh, &bars[0], 0, m0);
+    tma_load_2d(A1, &mm, &bars[0], 0, m0);
+    tma_load_2d(B0, &mw, &bars[0], 0, 0);
+    tma_load_2d(B1, &mw, &bars[0], 64, 0);
+    if (mbar_wait(&bars[0], 0)) {
+      tc_fence_after();
+      constexpr uint32_t idesc = idesc_bf16_f32(BM, H);
+#pragma unroll
+      for (int kc = 0; kc < 2; ++kc) {
+        const uint32_t a = smem_u32(kc ? A1 : A0), b = smem_u32(kc ? B1 : B0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          mma_bf16(tmem, sdesc_sw128(a + 32 * k, 1024), sdesc_sw128(b + 32 * k, 1024), idesc, (kc | k) != 0);
+      }
+      mma_commit(&bars[1]);
+    } else {
+      atomicExch(status, 1);  // tile loads did not arrive
+    }
+  }
+  __syncwarp();
+  bool done = __all_sync(0xffffffffu, mbar_wait(&bars[1], 0));
+  tc_fence_after();
+  if (done) {
+    const int r = warp * 32 + lane;
+    float acc[H];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    tmem_ld32(taddr, acc);
+    tmem_ld32(taddr + 32, acc + 32);
+    if (m0 + r < M) {
+      const uint8_t* rowp = A0 + (r >> 3) * 1024 + (r & 7) * 128;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        uint4 hv = *reinterpret_cast<const uint4*>(rowp + ((c ^ (r & 7)) * 16));
+        const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(&hv);
+        uint4 ov;
+        __nv_bfloat162* o2 = reinterpret_cast<__nv_bfloat162*>(&ov);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int n = c * 8 + 2 * q;
+          float2 hf = __bfloat1622float2(h2[q]);
+          o2[q] = __floats2bfloat162_rn(hf.x + silu(acc[n] + bias[n]), hf.y + silu(acc[n + 1] + bias[n + 1]));
+        }
+        *reinterpret_cast<uint4*>(out + (size_t)(m0 + r) * H + c * 8) = ov;
+      }
+    }
+  } else if (lane == 0) {
+    atomicExch(status, 2);  // the MMA completion did not arrive
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
+// output head: g = g_local - s (sum_j c_ij t_ij + c_i N_i) (one warp per vertex)
+__global__ void k_out(Topo t, Split S, const float* __restrict__ nrm, const SurW* __restrict__ W,
+                      const __nv_bfloat16* __restrict__ h, const double* __restrict__ gloc, double* __restrict__ g) {
+  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (i >= t.nv) return;
+  const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(h);
+  float2 hi = __bfloat1622float2(h2[(size_t)i * (H / 2) + lane]);
+  const float wo0 = W->wo[2 * lane], wo1 = W->wo[2 * lane + 1];
+  const float pi0 = wo0 * hi.x, pi1 = wo1 * hi.y;
+  float cn = warp_sum(W->wn[2 * lane] * hi.x + W->wn[2 * lane + 1] * hi.y) + W->bn;
+  f3 F = cn * f3{nrm[4 * (size_t)i], nrm[4 * (size_t)i + 1], nrm[4 * (size_t)i + 2]};
+  int d = t.val[i];
+  for (int m = 0; m < d; ++m) {
+    int j = t.nbr[(size_t)m * t.nv + i];
+    float2 hj = __bfloat1622float2(h2[(size_t)j * (H / 2) + lane]);
+    float c = warp_sum(pi0 * hj.x + pi1 * hj.y) + W->bo;
+    f3 e = S.diff(j, i);
+    float l = fnorm(e);
+    F += (c / l) * e;
+  }
+  if (lane == 0) {
+    const float s = W->fscale;
+    g[3 * (size_t)i] = gloc[3 * (size_t)i] - (double)(s * F.x);
+    g[3 * (size_t)i + 1] = gloc[3 * (size_t)i + 1] - (double)(s * F.y);
+    g[3 * (size_t)i + 2] = gloc[3 * (size_t)i + 2] - (double)(s * F.z);
+  }
+}
+
+// training inputs: ring neighbours, edge features and unit edge directions,
+// slot-major [D][nv] (neighbour -1 and zeros past the valence)
+__global__ void k_export(Topo t, Split S, const EdgeF* __restrict__ ed, const float* __restrict__ rho,
+                         const SurW* __restrict__ W, int D, int* __restrict__ nbr, float* __restrict__ ef,
+                         float* __restrict__ tv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= t.nv) return;
+  int d = t.val[i];
+  for (int m = 0; m < D; ++m) {
+    size_t o = (size_t)m * t.nv + i;
+    float f[FE] = {0.f, 0.f, 0.f, 0.f};
+    f3 dir = {0.f, 0.f, 0.f};
+    int j = -1;
+    if (m < d) {
+      int4 s = t.slot[o];
+      j = s.x;
+      edge_feat(ed[s.z], rho[i], rho[j], W->lbar, f);
+      f3 e = S.diff(j, i);
+      dir = (1.0f / fnorm(e)) * e;
+    }
+    nbr[o] = j;
+    for (int k = 0; k < FE; ++k) ef[FE * o + k] = f[k];
+    tv[3 * o] = dir.x;
+    tv[3 * o + 1] = dir.y;
+    tv[3 * o + 2] = dir.z;
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    TM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) fail(TM_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// bf16 row-major [rows][cols] matrix, boxes of 64 columns x box_rows rows,
+// 128-byte swizzle
+void make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+  if ((reinterpret_cast<uintptr_t>(ptr) & 15) != 0) fail(TM_ERR_ARG, "tensor base not 16-byte aligned");
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * sizeof(__nv_bfloat16)};
+  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(TM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+}
+
+void dense_launch(const CUtensorMap& mh, const CUtensorMap& mm, const CUtensorMap& mw, const float* bias,
+                  __nv_bfloat16* out, int M, int* status, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    TM_CUDA(cudaFuncSetAttribute(k_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, DENSE_SMEM));
+    attr = true;
+  }
+  if (M > 0) k_dense<<<nblk(M, BM), BM, DENSE_SMEM, s>>>(mh, mm, mw, bias, out, M, status);
+  TM_LAUNCH();
+}
+
+void parse_blob(const float* b, int64_t n, SurW& w, std::vector<__nv_bfloat16>& wd) {
+  if (n != BLOB_SIZE) fail(TM_ERR_ARG, "surrogate weights: expected " + std::to_string(BLOB_SIZE) + " floats");
+  if (b[0] != 1.0f || b[1] != FV || b[2] != FE || b[3] != H || b[4] != NR)
+    fail(TM_ERR_ARG, "surrogate weights: unsupported layout");
+  w.lbar = b[5];
+  w.abar = b[6];
+  w.fscale = b[7];
+  if (!(w.lbar > 0) || !(w.abar > 0)) fail(TM_ERR_ARG, "surrogate weights: non-positive length or area scale");
+  const float* q = b + BLOB_HEADER;
+  auto take = [&](float* dst, int k) {
+    std::memcpy(dst, q, sizeof(float) * k);
+    q += k;
+  };
+  take(w.win, H * FV);
+  take(w.bin, H);
+  wd.resize((size_t)NR * H * 2 * H);
+  for (int r = 0; r < NR; ++r) {
+    take(w.we[r], H * FE);
+    take(w.be[r], H);
+    for (int k = 0; k < H * 2 * H; ++k) wd[(size_t)r * H * 2 * H + k] = __float2bfloat16_rn(q[k]);
+    q += H * 2 * H;
+    take(w.b[r], H);
+  }
+  take(w.wo, H);
+  take(&w.bo, 1);
+  take(w.wn, H);
+  take(&w.bn, 1);
+}
+
+}  // namespace
+
+namespace tmg {
+
+// surrogate gradient at positions P into g (device arrays of 3 nv doubles)
+void surrogate_grad(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* P, double* g, cudaStream_t s) {
+  if (m->nv != sg->nv) fail(TM_ERR_ARG, "surrogate built for another mesh size");
+  int nv = m->nv;
+  if (nv == 0) return;
+  energy_eval32_local(e, m, P, sg->gloc.get(), s);
+  Topo t = m->topo();
+  const FaceF* fd = reinterpret_cast<const FaceF*>(e->face.get());
+  const EdgeF* ed = reinterpret_cast<const EdgeF*>(e->edge.get());
+  const float* rho = reinterpret_cast<const float*>(e->rho.get());
+  Split S{e->pos32.get(), e->poslo.get()};
+  SurW* W = sg->w.get();
+  k_sfeat<<<nblk(nv, 128), 128, 0, s>>>(t, fd, ed, rho, W, sg->u.get(), sg->nrm.get(), sg->hb[0].get());
+  TM_LAUNCH();
+  int cur = 0;
+  for (int r = 0; r < NR; ++r) {
+    k_agg<<<nblk(32L * nv, 256), 256, 0, s>>>(t, ed, rho, W, r, sg->hb[cur].get(), sg->mb.get());
+    TM_LAUNCH();
+    dense_launch(sg->map_h[cur], sg->map_m, sg->map_w[r], W->b[r], sg->hb[cur ^ 1].get(), nv, sg->status.get(), s);
+    cur ^= 1;
+  }
+  k_out<<<nblk(32L * nv, 256), 256, 0, s>>>(t, S, sg->nrm.get(), W, sg->hb[cur].get(), sg->gloc.get(), g);
+  TM_LAUNCH();
+}
+
+}  // namespace tmg
+
+extern "C" {
+
+int tm_surrogate_create(tm_mesh* m, const float* weights, int64_t n_weights, tm_surrogate** out) {
+  TM_API_BEGIN
+  if (!m || !weights || !out) fail(TM_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  std::unique_ptr<tm_surrogate> sg(new tm_surrogate());
+  std::vector<__nv_bfloat16> wd;
+  parse_blob(weights, n_weights, sg->hw, wd);
+  int nv = m->nv;
+  sg->nv = nv;
+  size_t n = std::max(nv, 1);
+  sg->w.ensure(1);
+  sg->wd.ensure(wd.size());
+  sg->u.ensure(FV * n);
+  sg->nrm.ensure(4 * n);
+  sg->hb[0].ensure(H * n);
+  sg->hb[1].ensure(H * n);
+  sg->mb.ensure(H * n);
+  sg->gloc.ensure(3 * n);
+  sg->status.ensure(1);
+  TM_CUDA(cudaMemcpy(sg->w.get(), &sg->hw, sizeof(SurW), cudaMemcpyHostToDevice));
+  TM_CUDA(cudaMemcpy(sg->wd.get(), wd.data(), sizeof(__nv_bfloat16) * wd.size(), cudaMemcpyHostToDevice));
+  TM_CUDA(cudaMemset(sg->status.get(), 0, sizeof(int)));
+  if (nv > 0) {
+    for (int k = 0; k < 2; ++k) make_map(&sg->map_h[k], sg->hb[k].get(), nv, H, BM);
+    make_map(&sg->map_m, sg->mb.get(), nv, H, BM);
+  }
+  for (int r = 0; r < NR; ++r) make_map(&sg->map_w[r], sg->wd.get() + (size_t)r * H * 2 * H, H, 2 * H, H);
+  *out = sg.release();
+  TM_API_END
+}
+
+int tm_surrogate_destroy(tm_surrogate* sg) {
+  delete sg;
+  return TM_OK;
+}
+
+int tm_surrogate_gradient_device(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
+                                 void* stream) {
+  TM_API_BEGIN
+  if (!sg || !e || !m || !d_points || !d_grad) fail(TM_ERR_ARG, "NULL argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  surrogate_grad(sg, e, m, d_points, d_grad, s);
+  int st = 0;
+  TM_CUDA(cudaMemcpyAsync(&st, sg->status.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  TM_CUDA(cudaStreamSynchronize(s));
+  if (st) fail(TM_ERR_TIMEOUT, "tensor-core layer wait timed out (" + std::to_string(st) + ")");
+  TM_API_END
+}
+
+int tm_surrogate_inputs_device(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* d_points, int32_t max_valence,
+                               float* d_u, float* d_normals, int32_t* d_nbr, float* d_edge_feat, float* d_dirs,
+                               double* d_grad_local, void* stream) {
+  TM_API_BEGIN
+  if (!sg || !e || !m || !d_points || !d_u || !d_normals || !d_nbr || !d_edge_feat || !d_dirs || !d_grad_local)
+    fail(TM_ERR_ARG, "NULL argument");
+  if (m->nv != sg->nv) fail(TM_ERR_ARG, "surrogate built for another mesh size");
+  if (max_valence < 1 || max_valence > TM_MAXVAL) fail(TM_ERR_ARG, "max_valence out of range");
+  cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
+  int nv = m->nv;
+  if (nv == 0) return TM_OK;
+  std::vector<int> val(nv);
+  TM_CUDA(cudaMemcpyAsync(val.data(), m->d_val.get(), sizeof(int) * nv, cudaMemcpyDeviceToHost, s));
+  TM_CUDA(cudaStreamSynchronize(s));
+  int dmax = *std::max_element(val.begin(), val.end());
+  if (dmax > max_valence) fail(TM_ERR_ARG, "a vertex valence exceeds max_valence (" + std::to_string(dmax) + ")");
+  energy_eval32_local(e, m, d_points, d_grad_local, s);
+  Topo t = m->topo();
+  const FaceF* fd = reinterpret_cast<const FaceF*>(e->face.get());
+  const EdgeF* ed = reinterpret_cast<const EdgeF*>(e->edge.get());
+  const float* rho = reinterpret_cast<const float*>(e->rho.get());
+  Split S{e->pos32.get(), e->poslo.get()};
+  k_sfeat<<<nblk(nv, 128), 128, 0, s>>>(t, fd, ed, rho, sg->w.get(), d_u, sg->nrm.get(), sg->hb[0].get());
+  TM_LAUNCH();
+  TM_CUDA(cudaMemcpyAsync(d_normals, sg->nrm.get(), sizeof(float) * 4 * nv, cudaMemcpyDeviceToDevice, s));
+  k_export<<<nblk(nv, 128), 128, 0, s>>>(t, S, ed, rho, sg->w.get(), max_valence, d_nbr, d_edge_feat, d_dirs);
+  TM_LAUNCH();
+  TM_CUDA(cudaStreamSynchronize(s));
+  TM_API_END
+}
+
+int tm_dense_silu_bf16(const void* d_h, const void* d_m, const void* d_w, const float* d_bias, void* d_out,
+                       int64_t rows, void* stream) {
+  TM_API_BEGIN
+  if (!d_h || !d_m || !d_w || !d_bias || !d_out) fail(TM_ERR_ARG, "NULL argument");
+  if (rows < 0 || rows > (1LL << 30)) fail(TM_ERR_ARG, "rows out of range");
+  cudaStream_t s = (cudaStream_t)stream;
+  alignas(64) CUtensorMap mh, mm, mw;
+  if (rows == 0) return TM_OK;
+  make_map(&mh, d_h, rows, H, BM);
+  make_map(&mm, d_m, rows, H, BM);
+  make_map(&mw, d_w, H, 2 * H, H);
+  DevBuf<int> st;
+  st.ensure(1);
+  TM_CUDA(cudaMemsetAsync(st.get(), 0, sizeof(int), s));
+  dense_launch(mh, mm, mw, d_bias, static_cast<__nv_bfloat16*>(d_out), (int)rows, st.get(), s);
+  int hs = 0;
+  TM_CUDA(cudaMemcpyAsync(&hs, st.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
+  TM_CUDA(cudaStreamSynchronize(s));
+  if (hs) fail(TM_ERR_TIMEOUT, "tensor-core layer wait timed out (" + std::to_string(hs) + ")");
+  TM_API_END
+}
+
+}  // extern "C"

@@ -166,6 +166,24 @@ __device__ __forceinline__ void visit_candidates(const PairTest& pt, const NLVie
   int lo = nl.crow[v], hi = nl.crow[v + 1];
   for (int q = lo; q < hi; ++q) visit_pair(pt, nl, P, v, p, nl.ccol[q], is_excluded, fn);
 }
+// The near row of v (a subsequence of its candidate row, so the same order).
+// mode 1: topology unchanged since the build, entries flagged excluded are
+// skipped without a test; mode 2: exclusion tested on the current topology.
+template <class F, class X>
+__device__ __forceinline__ void visit_near(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
+                                           int mode, const X& is_excluded, F& fn) {
+  int lo = nl.nrow[v], hi = nl.nrow[v + 1];
+  for (int q = lo; q < hi; ++q) {
+    int c = nl.ncol[q];
+    if (c < 0 && mode == 1) continue;
+    int j = c & 0x7fffffff;
+    d3 pj;
+    double s;
+    if (!pair_within(pt, nl, P, p, j, &pj, &s)) continue;
+    if (mode == 2 && nl.excl > 0 && is_excluded(v, j)) continue;
+    fn(j, __dsqrt_rn(s), exact_diff(p, pj));
+  }
+}
 template <class F, class X>
 __device__ __forceinline__ void visit_cells(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
                                             const int* co, const X& is_excluded, F& fn) {

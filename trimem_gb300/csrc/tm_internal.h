@@ -110,6 +110,11 @@ struct NLView {
   const int* ccol;
   const int* bcoord;   // build-time cell coordinates, 3 per vertex
   const float* pos32;  // positions rounded to float (prefilter), may be NULL
+  // near rows: the entries of each candidate row closer than 2 lc1 at build
+  // time (same order; bit 31 set when the pair was excluded on the build
+  // topology).  Valid while no vertex moved lc1/2 or more since the build.
+  const int* nrow;
+  const int* ncol;
 };
 
 #ifdef __CUDACC__
@@ -125,6 +130,8 @@ struct TopoW;
 // --------------------------------------------------------------------------
 // Handles (opaque in the C ABI)
 // --------------------------------------------------------------------------
+struct tm_surrogate;  // surrogate.cu
+
 struct tm_mesh {
   int nv = 0, ne = 0, nf = 0;
   bool closed = true;
@@ -139,6 +146,7 @@ struct tm_mesh {
   tmg::DevBuf<double> d_scratch;  // primitives / utilities
   tmg::DevBuf<int> d_status;
   cudaStream_t stream = nullptr;
+  unsigned long long topo_version = 0;  // advanced by every flip sweep that flips
   tmg::Topo topo() const;
   tmg::TopoW topo_w();
   void rebuild_tables(cudaStream_t s);  // faces, edges, rings from halfedges
@@ -156,6 +164,11 @@ struct tm_nlist {
   tmg::DevBuf<tmg::NLGeom> geom;
   tmg::DevBuf<long long> vcid;
   tmg::DevBuf<double> bbox;
+  // near rows (see NLView) and what they were built for
+  tmg::DevBuf<int> nrow, ncol, moved;
+  tmg::DevBuf<double> xb;  // positions at the build
+  double near_lc1 = 0.0, near_move2 = 0.0;
+  unsigned long long topo_version = 0;
   // last query result
   std::vector<double> res_d;
   std::vector<int> res_i, res_j;
@@ -203,6 +216,11 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* d_points, bool w
 // repg; slow must hold nv + 1 ints
 void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos32, bool want_grad, double* pot,
                     double* repg, int* slow, int* nslow, cudaStream_t s, const EP* eps = nullptr);
+// learned surrogate gradient (surrogate.cu)
+void surrogate_grad(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
+                    cudaStream_t s);
+// local terms only (bending and repulsion weights zero), FP32 stencils
+void energy_eval32_local(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, cudaStream_t s);
 // batch of replicas, FP32 stencils and FP64 sums per replica
 void energy_eval_batch32(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, const EP* eps,
                          const int* vrep, const int2* rblocks, Globals* gs, const int* blk, cudaStream_t s);

@@ -1,0 +1,78 @@
+"""Device-resident Markov chains over the C ABI.
+
+Each step is one HMC move (velocity Verlet on the GPU, exact Metropolis on
+the FP64 Hamiltonian, src/trimem/mc/hmc.py:14-26,129-158) followed by one
+edge-flip sweep (src/flips.cpp:22-165); the neighbour list is rebuilt every
+``refresh`` steps like the reference's evaluator callback
+(src/trimem/mc/evaluators.py).  The reference mixes the two moves by a coin
+flip per step (src/trimem/mc/hmc.py:325-372); running both every step keeps
+the schedule of the large-mesh runs (L velocity-Verlet steps + one sweep).
+Positions never leave the device; the six global properties of every
+returned state are recorded so that observables such as the bending energy
+can be traced without a host copy of the mesh.
+"""
+import ctypes
+
+import numpy as np
+
+
+class DeviceChain:
+    """Chain on the device positions ``x`` (a contiguous CUDA float64 tensor
+    of shape (n_vertices, 3)) of ``mesh``/``energy`` (capi handles)."""
+
+    def __init__(self, mesh, energy, x, mass=1.0, dt=5e-5, n_leapfrog=20, temperature=1.0, flip_ratio=0.2,
+                 flip_mode=1, flip_batch=1024, refresh=1, seed=0, stream=None, force=None):
+        from .. import capi
+
+        self.capi = capi
+        self.lib = capi.lib()
+        self.mesh, self.energy, self.x = mesh, energy, x
+        self.mass, self.dt, self.L, self.T = float(mass), float(dt), int(n_leapfrog), float(temperature)
+        self.flip_ratio, self.flip_mode, self.flip_batch = float(flip_ratio), int(flip_mode), int(flip_batch)
+        self.refresh = int(refresh)
+        self.seed = int(seed)
+        self.stream = ctypes.c_void_p(stream or 0)
+        self.force = force  # None: exact gradient; else a surrogate handle
+        self.rng = np.random.default_rng(seed)
+        self.step_index = 0
+        self.accepted = 0
+        self.flips = 0
+
+    def _ptr(self):
+        return ctypes.c_void_p(self.x.data_ptr())
+
+    def step(self):
+        """One HMC move and one flip sweep; returns (accepted, props6, energy)."""
+        out4 = (ctypes.c_double * 4)()
+        props = (ctypes.c_double * 6)()
+        u = float(self.rng.uniform())
+        if self.force is None:
+            self.capi.check(self.lib.tm_hmc_step_device(
+                self.energy.h, self.mesh.h, self._ptr(), self.mass, self.dt, self.L, self.T, self.seed,
+                self.step_index, u, out4, props, self.stream))
+        else:
+            self.capi.check(self.lib.tm_surrogate_hmc_step_device(
+                self.force.h, self.energy.h, self.mesh.h, self._ptr(), self.mass, self.dt, self.L, self.T,
+                self.seed, self.step_index, u, out4, props, self.stream))
+        acc = out4[0] != 0.0
+        self.accepted += int(acc)
+        if self.flip_ratio > 0.0:
+            nacc = ctypes.c_int32()
+            self.capi.check(self.lib.tm_flip_device(
+                self.mesh.h, self.energy.h, self._ptr(), self.flip_ratio,
+                (self.seed * 1000003 + self.step_index) & 0xFFFFFFFFFFFFFFFF, self.flip_mode, self.flip_batch,
+                ctypes.byref(nacc), self.stream))
+            self.flips += nacc.value
+        self.step_index += 1
+        if self.refresh and self.step_index % self.refresh == 0:
+            self.capi.check(self.lib.tm_energy_update_repulsion_device(self.energy.h, self.mesh.h, self._ptr(),
+                                                                       self.stream))
+        return acc, np.array(props[:]), out4[3]
+
+    def run(self, n):
+        """n steps; returns an (n, 6) array of the global properties after
+        each HMC move (before that step's sweep)."""
+        trace = np.empty((n, 6))
+        for i in range(n):
+            _, trace[i], _ = self.step()
+        return trace
