@@ -168,7 +168,7 @@ class Mesh:
         self.h = h
 
     def close(self):
-        if self.h:
+        if getattr(self, "h", None):
             lib().tm_mesh_destroy(self.h)
             self.h = None
 
@@ -231,7 +231,7 @@ class Energy:
         self.h = h
 
     def close(self):
-        if self.h:
+        if getattr(self, "h", None):
             lib().tm_energy_destroy(self.h)
             self.h = None
 
@@ -296,7 +296,7 @@ class NList:
         self.h = h
 
     def close(self):
-        if self.h:
+        if getattr(self, "h", None):
             lib().tm_nlist_destroy(self.h)
             self.h = None
 
@@ -344,7 +344,7 @@ class Batch:
         self.sizes = [len(a) for a in self._pts]
 
     def close(self):
-        if self.h:
+        if getattr(self, "h", None):
             lib().tm_batch_destroy(self.h)
             self.h = None
 
@@ -391,7 +391,7 @@ class Surrogate:
         self.h = h
 
     def close(self):
-        if self.h:
+        if getattr(self, "h", None):
             lib().tm_surrogate_destroy(self.h)
             self.h = None
 
