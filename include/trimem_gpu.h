@@ -186,6 +186,16 @@ int tm_hmc_step_device(tm_energy* e, tm_mesh* m, double* d_x, double mass, doubl
                        double temperature, uint64_t seed, uint64_t step, double u, double* out4, double* props6,
                        void* stream);
 
+/* ---- minimisation (src/trimem/mc/util.py:240-306) --------------------------
+ * Energy minimisation of the device positions d_x (n_vertices*3, updated in
+ * place) by L-BFGS with `history` correction pairs and an Armijo
+ * backtracking line search; the cell list is rebuilt at every evaluation
+ * like the reference's refresh = 1.  Stops when max |gradient| <= gtol, the
+ * relative energy decrease of a step is <= ftol, no decrease is found, or
+ * after maxiter iterations. */
+int tm_minimize_device(tm_energy* e, tm_mesh* m, double* d_x, int maxiter, int history, double gtol, double ftol,
+                       int32_t* iterations, double* energy, void* stream);
+
 /* ---- learned surrogate force (no counterpart in the reference) ---------------
  * A message-passing network (3 rounds, width 64, bf16 dense layers on the
  * tensor cores) that stands in for the bending and repulsion forces; the

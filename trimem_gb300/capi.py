@@ -106,6 +106,7 @@ _SIGS = {
     "tm_batch_energy": (_i32, [_p, _dp, _dp]),
     "tm_batch_update_repulsion": (_i32, [_p]),
     "tm_batch_hmc": (_i32, [_p, _i32, _i32, _d, _d, _d, ctypes.c_uint64, _i32, _ip]),
+    "tm_minimize_device": (_i32, [_p, _p, _p, _i32, _i32, _d, _d, _ip, _dp, _p]),
     "tm_surrogate_create": (_i32, [_p, ctypes.POINTER(ctypes.c_float), _i64, _pp]),
     "tm_surrogate_destroy": (_i32, [_p]),
     "tm_surrogate_gradient_device": (_i32, [_p, _p, _p, _p, _p, _p]),
