@@ -120,6 +120,33 @@ __device__ __forceinline__ void df_sincos_small(float t, df* s, df* c) {
   *c = pc;
 }
 
+// e^x for x <= 0 to double-word accuracy (0 below -80, where e^x < 2e-35):
+// x = k ln2 + r with a three-part Cody-Waite split of ln2 (the first part
+// has 16 significant bits, so k * part is exact), e^r = (e^(r/16))^16 with
+// e^(r/16) from its Taylor polynomial of degree 8 (|r/16| < 0.022,
+// truncation < 3e-21), then the exact scaling by 2^k.
+__device__ __forceinline__ df df_exp_nonpos(df x) {
+  if (!(x.hi >= -80.0f)) return df_make(0.0f);
+  const float L2H = 0.693145751953125f, L2M = 1.428606765e-06f, L2L = 5.497923148e-14f;
+  const float k = rintf(__fmul_rn(x.hi, 1.44269504f));
+  df r = x + df_make(__fmul_rn(-k, L2H));
+  r = r - two_prod(k, L2M);
+  r = r - df_make(__fmul_rn(k, L2L));
+  r = ldexp2(r, 0.0625f);
+  const df c[9] = {{1.000000000e+00f, 0.000000000e+00f}, {1.000000000e+00f, 0.000000000e+00f},
+                   {5.000000000e-01f, 0.000000000e+00f}, {1.666666716e-01f, -4.967053879e-09f},
+                   {4.166666791e-02f, -1.241763470e-09f}, {8.333333768e-03f, -4.346172033e-10f},
+                   {1.388888923e-03f, -3.363109444e-11f}, {1.984127011e-04f, -2.725596875e-12f},
+                   {2.480158764e-05f, -3.406996094e-13f}};
+  df p = c[8];
+#pragma unroll
+  for (int n = 7; n >= 0; --n) p = p * r + c[n];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) p = p * p;
+  const float s = __int_as_float((127 + (int)k) << 23);  // 2^k, -116 <= k <= 0
+  return {p.hi * s, p.lo * s};
+}
+
 // atan2(y, x) for y >= 0 (so the result is in [0, pi]) to double-word
 // accuracy: a float estimate t0 refined by one step
 // t = t0 + (y cos t0 - x sin t0) / (x cos t0 + y sin t0); valid while

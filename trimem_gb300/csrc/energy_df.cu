@@ -130,15 +130,45 @@ __global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* 
   ebond[e] = val;
 }
 
-__global__ void k_bond_short_df(EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep,
+// Flat-bottom bond of an edge shorter than lc1 (src/mesh_tether.h:29-85)
+// in double-word arithmetic: value e^(l/(l-lc1)) / l^r, derivative
+// -(lc1/(l-lc1)^2 + r/l) e^(l/(l-lc1)) / l^r (plus the l > lc0 branch when
+// lc1 > lc0).
+__device__ __forceinline__ void edge_bond_short_df(const EP& ep, const EPD& epd, df l, df* val, df* fac) {
+  const int r = ep.r;
+  df v = df_make(0.0f), f = df_make(0.0f);
+  const bool above = df_less(epd.lc0, l);
+  if (above) {
+    const df fr = df_make((float)r), d = l - epd.lc0;
+    v = df_ipow(fr, r + 1) * df_ipow(d, r);
+    f = df_ipow(fr, r + 2) * df_ipow(d, r - 1);
+  }
+  const df lmc = l - epd.lc1;
+  const df ilmc = df_make(1.0f) / lmc, il = df_make(1.0f) / l;
+  const df ex = df_exp_nonpos(l * ilmc);
+  const df ilr = df_ipow(il, r);
+  if (!above) v = ex * ilr;
+  f = f - (epd.lc1 * ilmc * ilmc + il * (float)r);
+  *val = v;
+  *fac = (f * ilr) * ex;
+}
+
+__global__ void k_bond_short_df(EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep, EPD epd,
                                 const int* __restrict__ blist, const int* __restrict__ bcnt) {
   int n = *bcnt;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int e = blist[i];
-    double val, fac;
-    edge_bond(ep, df_to(ed[e].l), &val, &fac);
-    ed[e].db = df_from(fac);
-    ebond[e] = df_from(val);
+    if (ep.r >= 1) {
+      df val, fac;
+      edge_bond_short_df(ep, epd, ed[e].l, &val, &fac);
+      ed[e].db = fac;
+      ebond[e] = val;
+    } else {  // non-positive exponents: FP64
+      double val, fac;
+      edge_bond(ep, df_to(ed[e].l), &val, &fac);
+      ed[e].db = df_from(fac);
+      ebond[e] = df_from(val);
+    }
   }
 }
 
@@ -342,7 +372,7 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
   if (t.ne) k_edge_df<<<nblk(t.ne, 256), 256, 0, s>>>(t, X, fd, ed, eb, ep, epd, blist, bcnt);
   TM_LAUNCH();
-  if (t.ne) k_bond_short_df<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(ed, eb, ep, blist, bcnt);
+  if (t.ne) k_bond_short_df<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(ed, eb, ep, epd, blist, bcnt);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
   repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
