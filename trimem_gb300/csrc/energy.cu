@@ -90,14 +90,14 @@ __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __rest
   EdgeD o;
   o.l = l;
   o.th = 0.0;
-  o.flag = 0.0;
+  o.il = -1.0 / l;
   if (E.z >= 0 && E.w >= 0) {
     FaceD F0 = fd[E.z], F1 = fd[E.w];
     d3 n0 = mk(F0.nx, F0.ny, F0.nz), n1 = mk(F1.nx, F1.ny, F1.nz);
     double c = fmin(1.0, fmax(-1.0, dot(n0, n1)));
     double a = acos(c);
     o.th = dot(cross(n0, n1), ev) >= 0.0 ? a : -a;
-    o.flag = 1.0;
+    o.il = -o.il;
   }
   // flat-bottom edge penalty: above the flat bottom inline (products only);
   // edges below it (exp and divisions in FP64) go to a list handled by
@@ -248,14 +248,14 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
         EdgeD E = ed[sc.z];
         double w = hgC + kb * (ri + rj);
         double cl = w * E.th + (ep.btype == 0 ? ep.kt * E.db : 0.0);
-        acc += (-cl / E.l) * (xj - xi);
-        if (E.flag != 0.0) {
+        acc += (-cl * fabs(E.il)) * (xj - xi);
+        if (E.il > 0.0) {
           int cin = slot_corner(sn.y);
           double cjn = cot_at(Fn, cin == 0 ? 2 : cin - 1);
           acc += w * (cj * n + cjn * mk(Fn.nx, Fn.ny, Fn.nz));
         }
         // edge (j, k) opposite i: dihedral term
-        if (ed[sc.w].flag != 0.0) {
+        if (ed[sc.w].il > 0.0) {
           double wo = hgC + kb * (rj + rk);
           acc += (-wo * (cj + ck)) * n;
         }

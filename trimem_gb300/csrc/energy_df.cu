@@ -29,8 +29,9 @@ namespace tmg {
 struct __align__(16) FaceDF {
   df nx, ny, nz, A, V, c0, c1, c2;
 };
+// il: 1/l on interior edges, -1/l on boundary edges (sign = interior flag)
 struct __align__(16) EdgeDF {
-  df l, th, db, flag;
+  df l, th, db, il;
 };
 
 namespace {
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* 
   EdgeDF o;
   o.l = l;
   o.th = df_make(0.0f);
-  o.flag = df_make(0.0f);
+  o.il = -(df_make(1.0f) / l);
   if (E.z >= 0 && E.w >= 0) {
     const FaceDF& F0 = fd[E.z];
     const FaceDF& F1 = fd[E.w];
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* 
     df th;
     if (!df_atan2_pos(sn, c, &th)) th = df_from(atan2(df_to(sn), df_to(c)));
     o.th = df_lt0(ddot(cr, ev)) ? -th : th;
-    o.flag = df_make(1.0f);
+    o.il = -o.il;
   }
   // flat-bottom edge penalty: above the flat bottom inline in double-float
   // (products only), below it (exp, FP64) through the short-edge list
@@ -300,8 +301,9 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
         df w = hgC + kb * (ri + rj);
         df cl = w * E.th;
         if (ep.btype == 0) cl += epd.kt * E.db;
-        acc += (-(cl / E.l)) * dj;
-        if (E.flag.hi != 0.0f) {
+        const df il = E.il.hi < 0.0f ? -E.il : E.il;
+        acc += (-(cl * il)) * dj;
+        if (E.il.hi > 0.0f) {
           const FaceDF& Fn = fd[fnx];
           int cin = slot_corner(sn.y);
           df cjn = cot_df(Fn, cin == 0 ? 2 : cin - 1);
@@ -309,7 +311,7 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
           acc += df3{w * (cj * n.x + cjn * nn.x), w * (cj * n.y + cjn * nn.y), w * (cj * n.z + cjn * nn.z)};
         }
         // edge (j, k) opposite i: dihedral term
-        if (ed[sc.w].flag.hi != 0.0f) {
+        if (ed[sc.w].il.hi > 0.0f) {
           df wo = hgC + kb * (rj + rk);
           acc += (-(wo * (cj + ck))) * n;
         }

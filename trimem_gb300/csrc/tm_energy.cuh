@@ -20,8 +20,10 @@ struct EP {
 struct __align__(16) FaceD {
   double nx, ny, nz, A, V, c0, c1, c2;
 };
+// il: 1/l on interior edges, -1/l on boundary edges (the sign is the
+// interior flag; the gradient multiplies by |il| instead of dividing by l)
 struct __align__(16) EdgeD {
-  double l, th, db, flag;
+  double l, th, db, il;
 };
 
 constexpr int VB = 256;  // threads per block of k_vertex (fixed: it sets the reduction order)
