@@ -135,20 +135,37 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__
   if (v < t.nv) {
     int d = t.val[v];
     double A = 0, V = 0, LT = 0, T = 0;
-    for (int m = 0; m < d; ++m) {
-      int4 s = t.slot[(size_t)m * t.nv + v];
-      int f = slot_face(s.y);
-      if (f < 0) continue;
-      double fa = fd[f].A;
-      A += fa;
-      V += fd[f].V;
-      EdgeD E = ed[s.z];
-      LT += E.l * E.th;
-      if (ep.btype == 0) {
-        T += ebond[s.z];
-      } else {
-        double q = fa / ep.a0 - 1.0;
-        T += q * q;
+    // slots in groups of four: all loads of a group are issued before the
+    // sums, which keep the slot order
+    for (int m0 = 0; m0 < d; m0 += 4) {
+      int4 s[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s[k] = m0 + k < d ? t.slot[(size_t)(m0 + k) * t.nv + v] : make_int4(0, -1, 0, 0);
+      double fa[4], fv[4], lt[4], tb[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        int f = slot_face(s[k].y);
+        fa[k] = fv[k] = lt[k] = tb[k] = 0.0;
+        if (f >= 0) {
+          fa[k] = fd[f].A;
+          fv[k] = fd[f].V;
+          EdgeD E = ed[s[k].z];
+          lt[k] = E.l * E.th;
+          if (ep.btype == 0) tb[k] = ebond[s[k].z];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (slot_face(s[k].y) < 0) continue;
+        A += fa[k];
+        V += fv[k];
+        LT += lt[k];
+        if (ep.btype == 0) {
+          T += tb[k];
+        } else {
+          double q = fa[k] / ep.a0 - 1.0;
+          T += q * q;
+        }
       }
     }
     double a = A * (1.0 / 3.0), c = 0.25 * LT;

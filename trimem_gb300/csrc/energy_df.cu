@@ -186,21 +186,37 @@ __global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const FaceDF* __restri
   if (v < t.nv) {
     int d = t.val[v];
     df A = df_make(0.0f), V = df_make(0.0f), LT = df_make(0.0f), T = df_make(0.0f);
-#pragma unroll 4
-    for (int m = 0; m < d; ++m) {
-      int4 s = t.slot[(size_t)m * t.nv + v];
-      int f = slot_face(s.y);
-      if (f < 0) continue;
-      df fa = fd[f].A;
-      A += fa;
-      V += fd[f].V;
-      EdgeDF E = ed[s.z];
-      LT += E.l * E.th;
-      if (ep.btype == 0) {
-        T += ebond[s.z];
-      } else {
-        df q = fa * epd.inv_a0 - df_make(1.0f);
-        T += q * q;
+    // slots in groups of four: all loads of a group are issued before the
+    // sums, which keep the slot order
+    for (int m0 = 0; m0 < d; m0 += 4) {
+      int4 s[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s[k] = m0 + k < d ? t.slot[(size_t)(m0 + k) * t.nv + v] : make_int4(0, -1, 0, 0);
+      df fa[4], fv[4], el[4], eth[4], tb[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        int f = slot_face(s[k].y);
+        fa[k] = fv[k] = el[k] = eth[k] = tb[k] = df_make(0.0f);
+        if (f >= 0) {
+          fa[k] = fd[f].A;
+          fv[k] = fd[f].V;
+          el[k] = ed[s[k].z].l;
+          eth[k] = ed[s[k].z].th;
+          if (ep.btype == 0) tb[k] = ebond[s[k].z];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (slot_face(s[k].y) < 0) continue;
+        A += fa[k];
+        V += fv[k];
+        LT += el[k] * eth[k];
+        if (ep.btype == 0) {
+          T += tb[k];
+        } else {
+          df q = fa[k] * epd.inv_a0 - df_make(1.0f);
+          T += q * q;
+        }
       }
     }
     df a = A * third(), c = ldexp2(LT, 0.25f);
