@@ -216,40 +216,59 @@ def batch_leg(stream, n_rep=48, n_leapfrog=10, n_steps=20):
             "timing": "wall clock around the synchronising call (batch) or sweep loop (sequential)"}
 
 
-def chain_leg(stream, stencil, n_burn=30, n_steps=150, weights=None):
-    """ESS/s of the bending energy of a device chain on the 163,842-vertex
-    mesh: per step one HMC move (20 velocity-Verlet steps, dt 5e-5, m 1, T 1)
-    and one flip sweep (ratio 0.2, 98,304 attempts), neighbour list rebuilt
-    every step.  The area and volume targets are the initial ones
-    (continuation lambda 0), so the chain samples around its start instead
-    of collapsing towards the 0.65 reduced volume, which an ESS needs."""
-    import torch
-
-    from trimem_gb300 import capi
-    from trimem_gb300.mc.device import DeviceChain
-    from trimem_gb300.mc.ess import ess
+def chain_start():
+    """The chains' workload: the 163,842-vertex membrane with area and volume
+    targets at the initial state (continuation lambda 0, so the chain samples
+    around its start instead of collapsing towards the 0.65 reduced volume,
+    which an ESS needs), relaxed to a local energy minimum by the device
+    L-BFGS (the jittered input is far from equilibrium: its short edges give
+    forces no time step survives)."""
+    from trimem_gb300.mc.device import relaxed_state
 
     p, f, prm = workload()
     prm = dict(prm, cont_lambda=0.0)
-    mesh = capi.Mesh(p, f)
+    x0, info = relaxed_state(p, f, prm)
+    return x0, f, prm, info
+
+
+def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=100, weights=None):
+    """ESS/s of the bending energy of a device chain: per step one HMC move
+    (20 velocity-Verlet steps, m 1, T 1) and one flip sweep (ratio 0.2,
+    98,304 attempts), neighbour list rebuilt every step.  dt: the largest of
+    5e-5 (the large-mesh runs' step), 2e-5, 1e-5, ... with pilot acceptance
+    >= 0.5 unless given."""
+    import torch
+
+    from trimem_gb300 import capi
+    from trimem_gb300.mc.device import DeviceChain, tune_dt
+    from trimem_gb300.mc.ess import ess
+
+    x0, f, prm, _ = start
+    mesh = capi.Mesh(x0, f)
     en = capi.Energy(mesh, capi.params(**prm))
     en.set_stencil_precision(stencil)
-    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
     sg = capi.Surrogate(mesh, weights) if weights is not None else None
-    ch = DeviceChain(mesh, en, x, dt=5e-5, n_leapfrog=20, flip_ratio=0.2, seed=11, stream=stream, force=sg)
+    pilot = None
+    if dt is None:
+        dt, pilot = tune_dt(mesh, en, x, stream=stream, force=sg)
+    ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=11, stream=stream, force=sg)
     ch.run(n_burn)
     torch.cuda.synchronize()
     a0, f0 = ch.accepted, ch.flips
+    sec0 = dict(ch.seconds)
     t0 = time.perf_counter()
     trace = ch.run(n_steps)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     bend = prm["kappa_b"] * trace[:, 3]
     e = ess(bend)
-    return {"steps": n_steps, "burn_in": n_burn, "seconds": round(t1 - t0, 3),
-            "ms_per_step": round((t1 - t0) * 1e3 / n_steps, 3),
+    return {"dt": dt, "pilot_acceptance": pilot, "steps": n_steps, "burn_in": n_burn,
+            "seconds": round(t1 - t0, 3), "ms_per_step": round((t1 - t0) * 1e3 / n_steps, 3),
             "acceptance": round((ch.accepted - a0) / n_steps, 3),
             "flips_accepted_per_sweep": round((ch.flips - f0) / n_steps, 1),
+            "ms_per_move": {k: round((ch.seconds[k] - sec0[k]) * 1e3 / n_steps, 3) for k in sec0},
+            "flip_attempts_per_s": round(int(0.2 * mesh.counts()[1]) * n_steps / max(ch.seconds["flip"] - sec0["flip"], 1e-9), 1),
             "ess_bending": round(e, 2), "ess_per_s": round(e / (t1 - t0), 3),
             "bending_mean": float(bend.mean()), "bending_sd": float(bend.std())}
 
@@ -507,16 +526,20 @@ def main():
         batch = {"error": f"{type(exc).__name__}: {exc}"}
 
     chain = {}
-    for name, kw in [("plain_fp64", dict(stencil=0)), ("plain_df64", dict(stencil=2)),
-                     ("surrogate", dict(stencil=0, weights="L7"))]:
-        try:
-            if kw.get("weights") == "L7":
-                from trimem_gb300 import surrogate as S
+    try:
+        start = chain_start()
+        chain["start"] = start[3]
+        plain = chain_leg(stream, start, 0)
+        chain["plain_fp64"] = plain
+        chain["plain_df64"] = chain_leg(stream, start, 2, dt=plain["dt"])
+        from trimem_gb300 import surrogate as S
 
-                kw["weights"] = np.load(S.WEIGHTS_L7)
-            chain[name] = chain_leg(stream, **kw)
-        except Exception as exc:
-            chain[name] = {"error": f"{type(exc).__name__}: {exc}"}
+        if os.path.exists(S.WEIGHTS_L7):
+            chain["surrogate"] = chain_leg(stream, start, 0, dt=plain["dt"], weights=np.load(S.WEIGHTS_L7))
+        else:
+            chain["surrogate"] = {"error": "no trained weights"}
+    except Exception as exc:
+        chain["error"] = f"{type(exc).__name__}: {exc}"
 
     cb = None
     if rank == 0 and not args.no_cpu:

@@ -312,17 +312,23 @@ int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_poi
   TM_CUDA(cudaMemsetAsync(b->gs.get(), 0, sizeof(Globals) * n_rep, s));
   TM_CUDA(cudaMemsetAsync(b->acc.get(), 0, sizeof(int) * n_rep, s));
   TM_CUDA(cudaMemsetAsync(b->counter.get(), 0, sizeof(unsigned long long), s));
+  // initial properties per replica (the reference state of the penalties):
+  // an FP64 evaluation of each replica on its own, as an energy manager of
+  // that mesh computes them at construction (src/energy.cpp:13-28)
   b->initial.assign(6 * (size_t)n_rep, 0.0);
+  for (int r = 0; r < n_rep; ++r) {
+    tm_mesh* mr = nullptr;
+    tm_energy* er = nullptr;
+    rc = tm_mesh_create(points[r], n_points[r], faces[r], n_faces[r], &mr);
+    if (rc) return rc;
+    std::unique_ptr<tm_mesh> hold_m(mr);
+    rc = tm_energy_create(mr, &params[r], &er);
+    if (rc) return rc;
+    std::unique_ptr<tm_energy> hold_e(er);
+    std::memcpy(&b->initial[6 * r], er->initial, sizeof(double) * 6);
+  }
   upload_eps(b.get());
   rebuild_nlist(b.get());
-  // initial properties per replica: the reference properties of each replica
-  batch_eval(b.get(), b->x.get(), b->g0.get(), s);
-  std::vector<Globals> g(n_rep);
-  TM_CUDA(cudaMemcpyAsync(g.data(), b->gs.get(), sizeof(Globals) * n_rep, cudaMemcpyDeviceToHost, s));
-  TM_CUDA(cudaStreamSynchronize(s));
-  for (int r = 0; r < n_rep; ++r)
-    for (int k = 0; k < 6; ++k) b->initial[6 * r + k] = g[r].props[k];
-  upload_eps(b.get());
   autotune(b.get());
   *out = b.release();
   TM_API_END

@@ -12,6 +12,7 @@ returned state are recorded so that observables such as the bending energy
 can be traced without a host copy of the mesh.
 """
 import ctypes
+import time
 
 import numpy as np
 
@@ -37,6 +38,7 @@ class DeviceChain:
         self.step_index = 0
         self.accepted = 0
         self.flips = 0
+        self.seconds = {"hmc": 0.0, "flip": 0.0, "refresh": 0.0}  # wall time per move (each call synchronises)
 
     def _ptr(self):
         return ctypes.c_void_p(self.x.data_ptr())
@@ -46,6 +48,7 @@ class DeviceChain:
         out4 = (ctypes.c_double * 4)()
         props = (ctypes.c_double * 6)()
         u = float(self.rng.uniform())
+        t0 = time.perf_counter()
         if self.force is None:
             self.capi.check(self.lib.tm_hmc_step_device(
                 self.energy.h, self.mesh.h, self._ptr(), self.mass, self.dt, self.L, self.T, self.seed,
@@ -56,6 +59,8 @@ class DeviceChain:
                 self.seed, self.step_index, u, out4, props, self.stream))
         acc = out4[0] != 0.0
         self.accepted += int(acc)
+        t1 = time.perf_counter()
+        self.seconds["hmc"] += t1 - t0
         if self.flip_ratio > 0.0:
             nacc = ctypes.c_int32()
             self.capi.check(self.lib.tm_flip_device(
@@ -63,10 +68,13 @@ class DeviceChain:
                 (self.seed * 1000003 + self.step_index) & 0xFFFFFFFFFFFFFFFF, self.flip_mode, self.flip_batch,
                 ctypes.byref(nacc), self.stream))
             self.flips += nacc.value
+        t2 = time.perf_counter()
+        self.seconds["flip"] += t2 - t1
         self.step_index += 1
         if self.refresh and self.step_index % self.refresh == 0:
             self.capi.check(self.lib.tm_energy_update_repulsion_device(self.energy.h, self.mesh.h, self._ptr(),
                                                                        self.stream))
+        self.seconds["refresh"] += time.perf_counter() - t2
         return acc, np.array(props[:]), out4[3]
 
     def run(self, n):
@@ -76,3 +84,42 @@ class DeviceChain:
         for i in range(n):
             _, trace[i], _ = self.step()
         return trace
+
+
+def relaxed_state(p, f, prm, maxiter=3000, stream=None):
+    """Positions of a local energy minimum reached from (p, f) by the device
+    L-BFGS (neighbour list refreshed every evaluation): a start for chains
+    that would otherwise begin far from equilibrium.  Returns (x, info)."""
+    import time
+
+    import torch
+
+    from .. import capi
+    from .minim import minimize_device
+
+    mesh = capi.Mesh(p, f)
+    en = capi.Energy(mesh, capi.params(**prm))
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    e0 = en.energy(mesh)
+    t0 = time.perf_counter()
+    it, e1 = minimize_device(en, mesh, x, maxiter=maxiter, stream=stream)
+    torch.cuda.synchronize()
+    return x.cpu().numpy(), {"iterations": it, "energy_start": e0, "energy_min": e1,
+                             "seconds": round(time.perf_counter() - t0, 3)}
+
+
+def tune_dt(mesh, energy, x, candidates=(5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6), n_leapfrog=20, target=0.5,
+            pilot=6, seed=99, stream=None, force=None):
+    """Largest time step whose pilot acceptance (pilot HMC steps without
+    flips, from a copy of x) reaches target; the smallest candidate if none
+    does.  Returns (dt, pilot acceptances)."""
+    seen = {}
+    for dt in candidates:
+        xc = x.clone()
+        ch = DeviceChain(mesh, energy, xc, dt=dt, n_leapfrog=n_leapfrog, flip_ratio=0.0, refresh=0, seed=seed,
+                         stream=stream, force=force)
+        ch.run(pilot)
+        seen[dt] = ch.accepted / pilot
+        if seen[dt] >= target:
+            return dt, seen
+    return candidates[-1], seen

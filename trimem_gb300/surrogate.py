@@ -167,26 +167,31 @@ class Inputs:
         self.dirs = self.dirs[:d].contiguous()
 
 
-def generate(n_snap, every=2, burn=10, level=7, seed=5, max_valence=16, stencil=2, log=print):
-    """States of a device chain on the benchmark membrane (HMC 20 x 5e-5 +
-    flip sweep 0.2 per step, initial area / volume targets) with inputs and
-    the training target g_local - g_exact."""
+def generate(n_snap, every=2, burn=10, level=7, seed=5, max_valence=16, log=print):
+    """States of the benchmark chain (the 163,842-vertex membrane relaxed by
+    L-BFGS, initial area / volume targets; HMC with 20 velocity-Verlet steps
+    at the tuned time step + a flip sweep of ratio 0.2 per step) with the
+    network inputs and the training target g_local - g_exact."""
     torch = _torch()
     from . import capi, meshgen
-    from .mc.device import DeviceChain
+    from .mc.device import DeviceChain, relaxed_state, tune_dt
     from .workloads import workload_params
 
     p, f = meshgen.jittered_icosphere(level, seed=0)
     prm = dict(workload_params(p, f, kappa_b=20.0, vfrac=0.65), cont_lambda=0.0)
-    mesh = capi.Mesh(p, f)
+    x0, info = relaxed_state(p, f, prm)
+    log(f"relaxed start: {info}")
+    mesh = capi.Mesh(x0, f)
     en = capi.Energy(mesh, capi.params(**prm))
-    en.set_stencil_precision(stencil)
-    lbar, abar = mesh_scales(p, f)
+    lbar, abar = mesh_scales(x0, f)
     net = make_net()
-    net.scales.copy_(torch.tensor([lbar, abar, 1.0]))
+    with torch.no_grad():
+        net.scales.copy_(torch.tensor([lbar, abar, 1.0]))
     sg = capi.Surrogate(mesh, to_blob(net))
-    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
-    ch = DeviceChain(mesh, en, x, dt=5e-5, n_leapfrog=20, flip_ratio=0.2, seed=seed)
+    x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
+    dt, pilot = tune_dt(mesh, en, x)
+    log(f"time step {dt} (pilot acceptance {pilot})")
+    ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=seed)
     ch.run(burn)
     L = capi.lib()
     data = []
@@ -202,10 +207,10 @@ def generate(n_snap, every=2, burn=10, level=7, seed=5, max_valence=16, stencil=
         data.append(inp)
         if log and (k + 1) % 10 == 0:
             log(f"snapshot {k + 1}/{n_snap}, acceptance so far {ch.accepted / ch.step_index:.2f}")
-    return data, (lbar, abar), prm
+    return data, (lbar, abar), dict(prm, dt=dt)
 
 
-def train(data, scales, iters=1500, lr=2e-3, seed=0, log=print):
+def train(data, scales, iters=1500, lr=2e-3, seed=0, log=print, budget_s=420.0):
     torch = _torch()
     torch.manual_seed(seed)
     lbar, abar = scales
@@ -219,6 +224,9 @@ def train(data, scales, iters=1500, lr=2e-3, seed=0, log=print):
     train_set, val_set = data[:-n_val], data[-n_val:]
     t0 = time.time()
     for it in range(iters):
+        if time.time() - t0 > budget_s:
+            log(f"time budget reached after {it} iterations")
+            break
         d = train_set[it % len(train_set)]
         F = net(d.u, d.nrm, d.nbr, d.ef, d.dirs)
         loss = ((F - d.target) ** 2).mean() / tgt_rms ** 2
@@ -241,9 +249,11 @@ def main():
     ap.add_argument("--snapshots", type=int, default=48)
     ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--out", default=WEIGHTS_L7)
+    ap.add_argument("--budget", type=float, default=420.0, help="training time limit in seconds")
     args = ap.parse_args()
-    data, scales, _ = generate(args.snapshots)
-    net, val, rms = train(data, scales, iters=args.iters)
+    log = lambda *a: print(*a, flush=True)
+    data, scales, _ = generate(args.snapshots, log=log)
+    net, val, rms = train(data, scales, iters=args.iters, log=log, budget_s=args.budget)
     b = to_blob(net.cpu())
     np.save(args.out, b)
     print(f"validation relative MSE (bf16 forward) {val:.4f}, target rms {rms:.4g}, weights -> {args.out}")
