@@ -157,23 +157,29 @@ def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400):
                       f"N(0,1e-4)) of the 163,842-vertex workload, {t:.1f} s, OpenMP {O.get_threads()} threads"}
 
 
-def batch_leg(stream, n_rep=48, n_leapfrog=10, n_steps=20):
-    """Replica batch: n_rep membranes of 642, 2562 and 10242 vertices with
-    their own parameters, sampled together by device-side HMC (one launch per
-    stage for all replicas, each HMC step one CUDA graph replay), against the
-    same replicas evaluated one mesh at a time (FP32 stencil, like the batch)."""
+def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_steps=20):
+    """Replica batch of the 64-membrane configuration: 16 replicas each of
+    642, 2,562, 10,242 and 40,962 vertices, reduced volume ~ U[0.6, 0.95] and
+    kappa_b ~ U[10, 50] (seeded), sampled together by device-side HMC (one
+    launch per stage for all replicas, each HMC step one CUDA graph replay),
+    against the same replicas evaluated one mesh at a time (FP32 stencil,
+    like the batch)."""
     import ctypes
 
     import torch
 
-    from trimem_gb300.workloads import workload_params
     from trimem_gb300 import capi, meshgen
+    from trimem_gb300.workloads import workload_params
 
     L = capi.lib()
+    rng = np.random.default_rng(2024)
     reps = []
-    for k in range(n_rep):
-        p, f = meshgen.jittered_icosphere(3 + k % 3, seed=100 + k)
-        reps.append((p, f, workload_params(p, f, kappa_b=10.0 + k, vfrac=0.6 + 0.005 * k)))
+    for lv in levels:
+        for k in range(n_per_level):
+            p, f = meshgen.jittered_icosphere(lv, seed=100 * lv + k)
+            reps.append((p, f, workload_params(p, f, kappa_b=float(rng.uniform(10, 50)),
+                                               vfrac=float(rng.uniform(0.6, 0.95)))))
+    n_rep = len(reps)
     nvert = sum(len(p) for p, _, _ in reps)
     b = capi.Batch([(p, f) for p, f, _ in reps], [capi.params(**prm) for _, _, prm in reps])
     b.hmc(3, n_leapfrog, 1e-6, seed=1)  # warm-up and graph capture
@@ -206,8 +212,9 @@ def batch_leg(stream, n_rep=48, n_leapfrog=10, n_steps=20):
     s1 = time.perf_counter()
     batch_rate = evals / (t1 - t0)
     seq_rate = n_sweeps * n_rep / (s1 - s0)
-    return {"replicas": n_rep, "vertices": nvert, "sizes": "642/2562/10242 vertices, 16 replicas each",
+    return {"replicas": n_rep, "vertices": nvert, "sizes": "642/2562/10242/40962 vertices, 16 replicas each",
             "hmc": f"{n_steps} steps x {n_leapfrog} leapfrog, dt 1e-6, graph replay",
+            "hmc_steps_per_s": round(n_steps / (t1 - t0), 2),
             "batch_replica_evals_per_s": round(batch_rate, 1),
             "batch_vertex_evals_per_s": round(batch_rate * nvert / n_rep, 1),
             "sequential_replica_evals_per_s": round(seq_rate, 1),
