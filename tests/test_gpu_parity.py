@@ -213,6 +213,28 @@ def test_flip_on_jittered_mesh_with_repulsion(C):
         assert rel(gg, eo.gradient(mo)) < RTOL
 
 
+@pytest.mark.parametrize("stencil", [0, 2], ids=["fp64", "df64"])
+def test_repulsion_with_cell_changes_inside_the_skin(C, stencil):
+    """Every vertex moved by up to 0.45 lc1 since the cell-list build (inside
+    the near rows' skin of lc1/2): many vertices are in another cell than at
+    the build and are still answered from the near rows, in the reference's
+    order; everything matches the oracle on the same cells."""
+    p, f = meshgen.jittered_icosphere(3, seed=6)
+    prm = workload_params(p, f, excl=1, rep_scale=1.3)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    eg.set_stencil_precision(stencil)
+    rng = np.random.default_rng(4)
+    d = rng.uniform(-1.0, 1.0, size=p.shape) * (0.45 / np.sqrt(3.0)) * prm["rep_lc1"]
+    mo.points()[:] += d
+    mg.points()[:] += d
+    po = eo.properties(mo)
+    assert po[5] > 0
+    assert abs(eg.properties(mg)[5] - po[5]) <= RTOL * po[5]
+    eng, gg = eg.gradient(mg, with_energy=True)
+    assert abs(eng - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+    assert rel(gg, eo.gradient(mo)) < RTOL
+
+
 def test_repulsion_after_a_large_move(C):
     """One vertex moved by more than half the repulsion cut-off since the
     cell-list build: the evaluation leaves the near rows for the full

@@ -424,23 +424,45 @@ __global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt,
   if (!pass) cnt[a] = n;
 }
 
-// Near rows: the candidates of each vertex whose build-time distance is
-// below rn (squared threshold rn2, rounded up), in candidate order; bit 31
-// marks pairs excluded on the build topology.
-__global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, double rn2, int pass, int* cnt,
-                       const int* off, int* out) {
+// Near rows: the build-time members of the 5 x 5 x 5 cells around each
+// vertex's build cell (x outer, z inner, members ascending) closer than rn
+// at the build (squared threshold rn2, rounded up), with their cell offset
+// and a flag for pairs excluded on the build topology.
+__global__ void k_near(int nv, const double* P, NLView nl, Topo t, const int* vcoord, int excl, double rn2, int pass,
+                       int* cnt, const int* off, int2* out) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nv) return;
+  const NLGeom& G = nl.geom[0];
   d3 pa = ld3(P, a);
   int n = 0;
   int base = pass ? off[a] : 0;
-  for (int q = nl.crow[a]; q < nl.crow[a + 1]; ++q) {
-    int b = nl.ccol[q];
-    d3 pb = ld3(P, b);
-    double dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-    if (dx * dx + dy * dy + dz * dz >= rn2) continue;
-    if (pass) out[base + n] = nl_excluded(t, excl, a, b) ? (int)(0x80000000u | (unsigned)b) : b;
-    ++n;
+  for (int dx = -2; dx <= 2; ++dx) {
+    int ii = vcoord[3 * a] + dx;
+    if (ii < 0 || ii >= G.shape[0]) continue;
+    for (int dy = -2; dy <= 2; ++dy) {
+      int jj = vcoord[3 * a + 1] + dy;
+      if (jj < 0 || jj >= G.shape[1]) continue;
+      for (int dz = -2; dz <= 2; ++dz) {
+        int kk = vcoord[3 * a + 2] + dz;
+        if (kk < 0 || kk >= G.shape[2]) continue;
+        long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
+        int st = 0;
+        int c = cell_lookup(nl, cid, &st);
+        for (int q = 0; q < c; ++q) {
+          int b = nl.cell_verts[st + q];
+          if (b == a) continue;
+          d3 pb = ld3(P, b);
+          double ex = pa.x - pb.x, ey = pa.y - pb.y, ez = pa.z - pb.z;
+          if (ex * ex + ey * ey + ez * ez >= rn2) continue;
+          if (pass) {
+            int code = (dx + 2) | ((dy + 2) << 3) | ((dz + 2) << 6);
+            if (nl_excluded(t, excl, a, b)) code |= 1 << 9;
+            out[base + n] = make_int2(b, code);
+          }
+          ++n;
+        }
+      }
+    }
   }
   if (!pass) cnt[a] = n;
 }
@@ -588,25 +610,29 @@ static void build_cells(tm_nlist* nl, NLView& V, int nv, const double* P, cudaSt
   }
 }
 
-// Near rows for repulsion queries at cut-off lc1 (skin lc1): a pair closer
+// Near rows for repulsion queries at cut-off lc1 (skin lc1).  A pair closer
 // than lc1 at query time whose vertices both moved less than lc1/2 since the
-// build was closer than 2 lc1 at the build, so the near row of a vertex that
-// is still in its build cell holds every candidate the query can accept.
+// build was closer than 2 lc1 at the build.  Cells are at least rlist wide
+// and rlist >= lc1, so such a vertex is at most one cell away from its build
+// cell and such a neighbour at most two cells away from the vertex's build
+// cell: the near row holds every candidate the query can accept, and the
+// query keeps the entries whose cell is among the 27 around its current
+// cell, in the reference's scan order (a subsequence of the row's order).
 static void build_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, double lc1, cudaStream_t s) {
   int nv = nl->nv;
   Topo t = m->topo();
   double rn = 2.0 * lc1;
   nl->nrow.ensure((size_t)nv + 1);
   nl->cnt.ensure((size_t)nv + 1);
-  k_near<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, V.excl, rn * rn * (1.0 + 1e-12), 0, nl->cnt.get(), nullptr,
-                                       nullptr);
+  k_near<<<nblk(nv, 128), 128, 0, s>>>(nv, P, V, t, nl->vcoord.get(), V.excl, rn * rn * (1.0 + 1e-12), 0,
+                                       nl->cnt.get(), nullptr, nullptr);
   TM_LAUNCH();
   TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
   int total = 0;
   exclusive_scan_int(nl->cnt.get(), nl->nrow.get(), nv + 1, &total, nl->tmp, s);
-  nl->ncol.ensure(std::max(total, 1));
-  k_near<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, V.excl, rn * rn * (1.0 + 1e-12), 1, nullptr, nl->nrow.get(),
-                                       nl->ncol.get());
+  nl->nent.ensure(std::max(total, 1));
+  k_near<<<nblk(nv, 128), 128, 0, s>>>(nv, P, V, t, nl->vcoord.get(), V.excl, rn * rn * (1.0 + 1e-12), 1,
+                                       nullptr, nl->nrow.get(), nl->nent.get());
   TM_LAUNCH();
   nl->xb.ensure(3 * (size_t)nv);
   TM_CUDA(cudaMemcpyAsync(nl->xb.get(), P, sizeof(double) * 3 * nv, cudaMemcpyDeviceToDevice, s));
@@ -615,7 +641,7 @@ static void build_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, dou
   nl->near_move2 = 0.25 * lc1 * lc1 * (1.0 - 1e-12);
   nl->topo_version = m->topo_version;
   V.nrow = nl->nrow.get();
-  V.ncol = nl->ncol.get();
+  V.nent = nl->nent.get();
 }
 
 void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, cudaStream_t s) {
@@ -640,7 +666,8 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
   k_bbox_final<<<1, BB, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
   TM_LAUNCH();
   build_cells(nl, V, nv, P, s, p.n_search == 0);
-  if (p.n_search == 0 && V.crow && p.rep_lc1 > 0) build_near(nl, m, V, P, p.rep_lc1, s);
+  if (p.n_search == 0 && V.crow && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1 && nv > 0)
+    build_near(nl, m, V, P, p.rep_lc1, s);
   if (p.n_search == 1) {
     // Verlet CSR from the cell list at cut-off rlist, rows in the reference's
     // insertion order

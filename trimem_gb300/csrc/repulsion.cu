@@ -3,10 +3,11 @@
 // sum_j exp(l/(l - lc1)) / l^r over the neighbours closer than lc1 and, for a
 // gradient, 2 sum_j phi'(l) (x_i - x_j) / l.
 //
-// A vertex whose current position still lies in its build-time cell walks
-// the precomputed candidate row of that cell (k_rep_fast), or only its near
-// row while no vertex has moved lc1/2 since the build (k_moved decides this
-// for the whole mesh before the pass); the few that moved
+// While no vertex has moved lc1/2 since the build (k_moved decides this for
+// the whole mesh before the pass) every vertex walks its near row in
+// k_rep_fast.  Otherwise a vertex whose current position still lies in its
+// build-time cell walks the precomputed candidate row of that cell; the few
+// that moved
 // to another cell are queued and walk the 27 cells through the cell table in
 // a second kernel (k_rep_slow), so the long table walk never holds a warp of
 // fast vertices.  Both produce the per-vertex values in the reference's pair
@@ -65,10 +66,17 @@ __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restri
   if (nl.kind == 0) {
     int co[3];
     bool fast = in_build_cell(nl, v, p, co);
+    int dx = 0, dy = 0, dz = 0;
+    if (near_mode) {
+      dx = co[0] - nl.bcoord[3 * v];
+      dy = co[1] - nl.bcoord[3 * v + 1];
+      dz = co[2] - nl.bcoord[3 * v + 2];
+      fast = dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
+    }
     warp_append(!fast, v, slow, nslow);
     if (!fast) return;
     if (near_mode)
-      visit_near(pt, nl, P, v, p, near_mode, x, acc);
+      visit_near(pt, nl, P, v, p, near_mode, dx, dy, dz, x, acc);
     else
       visit_candidates(pt, nl, P, v, p, x, acc);
   } else {

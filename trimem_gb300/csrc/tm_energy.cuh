@@ -168,17 +168,21 @@ __device__ __forceinline__ void visit_candidates(const PairTest& pt, const NLVie
   int lo = nl.crow[v], hi = nl.crow[v + 1];
   for (int q = lo; q < hi; ++q) visit_pair(pt, nl, P, v, p, nl.ccol[q], is_excluded, fn);
 }
-// The near row of v (a subsequence of its candidate row, so the same order).
+// The near row of v restricted to the 27 cells around its current cell,
+// which lies (ddx, ddy, ddz) from its build cell: the reference's candidates
+// of that cell closer than 2 lc1 at the build, in the reference's order.
 // mode 1: topology unchanged since the build, entries flagged excluded are
 // skipped without a test; mode 2: exclusion tested on the current topology.
 template <class F, class X>
 __device__ __forceinline__ void visit_near(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
-                                           int mode, const X& is_excluded, F& fn) {
+                                           int mode, int ddx, int ddy, int ddz, const X& is_excluded, F& fn) {
   int lo = nl.nrow[v], hi = nl.nrow[v + 1];
   for (int q = lo; q < hi; ++q) {
-    int c = nl.ncol[q];
-    if (c < 0 && mode == 1) continue;
-    int j = c & 0x7fffffff;
+    int2 c = nl.nent[q];
+    int ox = (c.y & 7) - 2 - ddx, oy = ((c.y >> 3) & 7) - 2 - ddy, oz = ((c.y >> 6) & 7) - 2 - ddz;
+    if (ox < -1 || ox > 1 || oy < -1 || oy > 1 || oz < -1 || oz > 1) continue;
+    if (mode == 1 && (c.y & (1 << 9))) continue;
+    int j = c.x;
     d3 pj;
     double s;
     if (!pair_within(pt, nl, P, p, j, &pj, &s)) continue;

@@ -110,11 +110,13 @@ struct NLView {
   const int* ccol;
   const int* bcoord;   // build-time cell coordinates, 3 per vertex
   const float* pos32;  // positions rounded to float (prefilter), may be NULL
-  // near rows: the entries of each candidate row closer than 2 lc1 at build
-  // time (same order; bit 31 set when the pair was excluded on the build
-  // topology).  Valid while no vertex moved lc1/2 or more since the build.
+  // near rows: per vertex the build-time members of the 5 x 5 x 5 cells
+  // around its build cell (x outer, z inner, members ascending) closer than
+  // 2 lc1 at the build; entry x = neighbour, y = cell offset (dx+2) |
+  // (dy+2) << 3 | (dz+2) << 6, bit 9 set when the pair was excluded on the
+  // build topology.  Valid while no vertex moved lc1/2 or more since the build.
   const int* nrow;
-  const int* ncol;
+  const int2* nent;
 };
 
 #ifdef __CUDACC__
@@ -165,7 +167,8 @@ struct tm_nlist {
   tmg::DevBuf<long long> vcid;
   tmg::DevBuf<double> bbox;
   // near rows (see NLView) and what they were built for
-  tmg::DevBuf<int> nrow, ncol, moved;
+  tmg::DevBuf<int> nrow, moved;
+  tmg::DevBuf<int2> nent;
   tmg::DevBuf<double> xb;  // positions at the build
   double near_lc1 = 0.0, near_move2 = 0.0;
   unsigned long long topo_version = 0;
