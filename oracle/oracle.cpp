@@ -1163,19 +1163,20 @@ static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, 
       before.bending = dpv[3]; before.tethering = dpv[4]; before.repulsion = dpv[5];
       dps[s] = before;
     }
-    // sequential Metropolis in window order, then commit
+    // sequential Metropolis in window order, then commit: each slot is tried
+    // on the state left by the accepted slots before it and accepted when
+    // E(props - dp) - E <= -log(u) (the device's k_metro decides the same)
     for (int s = 0; s < limit; ++s) {
       if (!ok[s]) continue;
-      props -= dps[s];
-      double en = E.energy(props);
+      Props trial = props;
+      trial -= dps[s];
+      double en = E.energy(trial);
       double de = en - e0;
-      double alpha = de < 0.0 ? 1.0 : std::exp(-de);
-      if (flip_u_of(seed, win[s]) <= alpha) {
+      if (de <= -std::log(flip_u_of(seed, win[s]))) {
+        props = trial;
         e0 = en;
         acc += 1;
         m.flip(flip_edge_of(seed, win[s], ne));
-      } else {
-        props += dps[s];
       }
     }
     pending.swap(keep);

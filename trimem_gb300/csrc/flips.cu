@@ -16,9 +16,11 @@
 //             four quad vertices before and after a virtual flip (the mesh is
 //             not touched), including the repulsion with the post-flip
 //             exclusion rings
-//   k_metro   one thread walks the window in slot order: props -= dprops,
-//             Metropolis with T = 1 (flips.cpp:142-160), losers are queued
-//             for the next window
+//   k_prep    per slot the property change of the flip and -log(u)
+//   k_metro   Metropolis with T = 1 in slot order (flips.cpp:142-160): one
+//             block tries all remaining slots on the current state, takes
+//             the first accepted one and repeats from there; losers are
+//             queued for the next window
 //   k_commit  accepted flips rewrite their six halfedges, two faces, five
 //             edge rows and four ring rows; patches are disjoint, so commits
 //             never touch the same entries
@@ -338,48 +340,111 @@ __global__ void k_delta(TopoW t, int W, unsigned long long seed, const long long
   }
 }
 
-__global__ void k_metro(int W, unsigned long long seed, const long long* win, const unsigned char* winner,
-                        const unsigned char* okf, const double* part, EP ep, FlipState* st, const int* limit,
-                        unsigned char* accepted, long long* pend) {
-  if (threadIdx.x || blockIdx.x) return;
-  int lim = *limit;
-  double props[6];
-  for (int k = 0; k < 6; ++k) props[k] = st->props[k];
-  double e0 = st->e0;
-  int acc = st->acc;
-  int np = 0;
-  for (int s = 0; s < W; ++s) {
-    accepted[s] = 0;
-    if (s >= lim || !winner[s]) {
-      pend[np++] = win[s];
-      continue;
-    }
-    if (!okf[s]) continue;
-    const double* o = part + 64 * (size_t)s;
-    double dp[6];
-    for (int k = 0; k < 6; ++k) {
-      double before = ((o[k] + o[8 + k]) + o[16 + k]) + o[24 + k];
-      // summation orders of edge_vertex_properties before (va0, va1, vb0,
-      // vb1) and after the flip (va1, vb0, vb1, va0)
-      double after = ((o[40 + k] + o[48 + k]) + o[56 + k]) + o[32 + k];
-      dp[k] = before - after;
-      props[k] -= dp[k];
-    }
-    double en = energy_of(ep, props);
-    double de = en - e0;
-    double alpha = de < 0.0 ? 1.0 : exp(-de);
-    if (flip_u_of(seed, win[s]) <= alpha) {
-      e0 = en;
-      acc += 1;
-      accepted[s] = 1;
-    } else {
-      for (int k = 0; k < 6; ++k) props[k] += dp[k];
-    }
+// per slot: the property change of the flip (before - after, in the
+// summation orders of edge_vertex_properties before (va0, va1, vb0, vb1)
+// and after the flip (va1, vb0, vb1, va0)), -log(u) and eligibility
+__global__ void k_prep(int W, unsigned long long seed, const long long* win, const unsigned char* winner,
+                       const unsigned char* okf, const double* part, const int* limit, double* dpn) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= W) return;
+  double* o8 = dpn + 8 * (size_t)s;
+  bool elig = s < *limit && winner[s] && okf[s];
+  o8[7] = elig ? 1.0 : 0.0;
+  if (!elig) return;
+  const double* o = part + 64 * (size_t)s;
+  for (int k = 0; k < 6; ++k) {
+    double before = ((o[k] + o[8 + k]) + o[16 + k]) + o[24 + k];
+    double after = ((o[40 + k] + o[48 + k]) + o[56 + k]) + o[32 + k];
+    o8[k] = before - after;
   }
-  for (int k = 0; k < 6; ++k) st->props[k] = props[k];
-  st->e0 = e0;
-  st->acc = acc;
-  st->npend = np;
+  o8[6] = -log(flip_u_of(seed, win[s]));
+}
+
+// Metropolis with T = 1 in slot order (flips.cpp:142-160): slot s is tried on
+// the state left by the accepted slots before it, trial = props - dp, and is
+// accepted when E(trial) - E <= -log(u).  Acceptances are rare, so one block
+// tries all remaining slots against the current state at once, takes the
+// first accepted one, updates the state and repeats from the next slot: the
+// same decisions as a walk in slot order.  Then the deferred proposals are
+// compacted in order for the next window.
+constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread (contiguous)
+__global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const unsigned char* winner,
+                                             const double* dpn, EP ep, FlipState* st, const int* limit,
+                                             unsigned char* accepted, long long* pend) {
+  __shared__ double sP[6], se0;
+  __shared__ int sfirst, sstart, sacc;
+  __shared__ int scan[MB];
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int k = 0; k < 6; ++k) sP[k] = st->props[k];
+    se0 = st->e0;
+    sacc = st->acc;
+    sstart = 0;
+  }
+  for (int k = 0; k < MS; ++k) {
+    int s = tid * MS + k;
+    if (s < W) accepted[s] = 0;
+  }
+  __syncthreads();
+  for (int round = 0; round <= W; ++round) {
+    if (tid == 0) sfirst = INT_MAX;
+    __syncthreads();
+    const int start = sstart;
+    for (int k = 0; k < MS; ++k) {
+      int s = tid * MS + k;
+      if (s < start || s >= W) continue;
+      const double* o8 = dpn + 8 * (size_t)s;
+      if (o8[7] == 0.0) continue;
+      double trial[6];
+      for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
+      double de = energy_of(ep, trial) - se0;
+      if (de <= o8[6]) {
+        atomicMin(&sfirst, s);
+        break;  // later slots of this thread cannot be first
+      }
+    }
+    __syncthreads();
+    const int first = sfirst;
+    if (first == INT_MAX) break;
+    if (tid == first / MS) {
+      const double* o8 = dpn + 8 * (size_t)first;
+      double trial[6];
+      for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
+      double en = energy_of(ep, trial);
+      for (int q = 0; q < 6; ++q) sP[q] = trial[q];
+      se0 = en;
+      sacc += 1;
+      accepted[first] = 1;
+      sstart = first + 1;
+    }
+    __syncthreads();
+  }
+  // deferred proposals (outside the limit or not winners), in slot order
+  const int lim = *limit;
+  int c = 0;
+  for (int k = 0; k < MS; ++k) {
+    int s = tid * MS + k;
+    if (s < W && (s >= lim || !winner[s])) ++c;
+  }
+  scan[tid] = c;
+  __syncthreads();
+  for (int o = 1; o < MB; o <<= 1) {
+    int v = tid >= o ? scan[tid - o] : 0;
+    __syncthreads();
+    scan[tid] += v;
+    __syncthreads();
+  }
+  int pos = scan[tid] - c;
+  for (int k = 0; k < MS; ++k) {
+    int s = tid * MS + k;
+    if (s < W && (s >= lim || !winner[s])) pend[pos++] = win[s];
+  }
+  if (tid == MB - 1) st->npend = scan[MB - 1];
+  if (tid == 0) {
+    for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
+    st->e0 = se0;
+    st->acc = sacc;
+  }
 }
 
 __global__ void k_commit(TopoW t, int W, unsigned long long seed, const long long* win, const unsigned char* accepted,
@@ -452,6 +517,8 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   okf.ensure(MAXB);
   acc.ensure(MAXB);
   part.ensure(64 * (size_t)MAXB);
+  DevBuf<double> dpn;
+  dpn.ensure(8 * (size_t)MAXB);
   st.ensure(1);
   limit.ensure(1);
   k_owner_init<<<nblk(ne, 256), 256, 0, s>>>(owner.get(), ne);
@@ -476,8 +543,11 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     k_delta<<<nblk(8L * W, 64), 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv,
                                           part.get(), okf.get());
     TM_LAUNCH();
-    k_metro<<<1, 1, 0, s>>>(W, seed, win.get(), winner.get(), okf.get(), part.get(), ep, st.get(), limit.get(),
-                            acc.get(), pend.get());
+    k_prep<<<nblk(W, 128), 128, 0, s>>>(W, seed, win.get(), winner.get(), okf.get(), part.get(), limit.get(),
+                                        dpn.get());
+    TM_LAUNCH();
+    k_metro<<<1, MB, 0, s>>>(W, win.get(), winner.get(), dpn.get(), ep, st.get(), limit.get(), acc.get(),
+                             pend.get());
     TM_LAUNCH();
     k_commit<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), acc.get(), st.get());
     TM_LAUNCH();
