@@ -315,6 +315,24 @@ def run_profile(args):
     gen.manual_seed(7)
     capi.check(L.tm_energy_set_stencil_precision(en.h, args.stencil))
     capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), None))
+    if args.profile_surrogate:
+        from trimem_gb300 import surrogate as S
+
+        sg = capi.Surrogate(mesh, np.load(S.WEIGHTS_L7))
+        for _ in range(args.profile_surrogate):
+            capi.check(L.tm_surrogate_gradient_device(sg.h, en.h, mesh.h, ctypes.c_void_p(x.data_ptr()),
+                                                      ctypes.c_void_p(g.data_ptr()), None))
+        torch.cuda.synchronize()
+        print("profile surrogate evaluations done:", args.profile_surrogate)
+        return
+    if args.profile_flips:
+        for k in range(args.profile_flips):
+            acc = ctypes.c_int32()
+            capi.check(L.tm_flip_device(mesh.h, en.h, ctypes.c_void_p(x.data_ptr()), 0.2, 7 + k, 1, 1024,
+                                        ctypes.byref(acc), None))
+        torch.cuda.synchronize()
+        print("profile flip sweeps done:", args.profile_flips)
+        return
     for _ in range(args.profile_evals):
         x.add_(torch.randn(x.shape, dtype=torch.float64, device="cuda", generator=gen), alpha=1e-4)
         capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()),
@@ -334,10 +352,14 @@ def main():
     ap.add_argument("--profile-evals", type=int, default=0,
                     help="only run this many device evaluations (for ncu captures) and exit")
     ap.add_argument("--stencil", type=int, default=0, help="stencil precision of --profile-evals (0, 1, 2)")
+    ap.add_argument("--profile-surrogate", type=int, default=0,
+                    help="only run this many surrogate force evaluations (for ncu captures) and exit")
+    ap.add_argument("--profile-flips", type=int, default=0,
+                    help="only run this many flip sweeps (ratio 0.2) (for ncu captures) and exit")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.profile_evals:
+    if args.profile_evals or args.profile_surrogate or args.profile_flips:
         return run_profile(args)
 
     import torch
