@@ -77,7 +77,47 @@ def make_net():
             F = (c[..., None] * dirs).sum(0) + cn[:, None] * nrm[:, :3]
             return self.scales[2] * F
 
+        def forward_sparse(self, sp):
+            """The same function with the ring sums as sparse products
+            (training): m = sum_k W_e[:, k] * (E_k h) + b_e * (A h), with
+            E_k / A the adjacency weighted by edge feature k / by one, and
+            sum_j c_ij d_ij = ((w_o * h) . (D h)) + b_o D 1 per component."""
+            F_ = torch.nn.functional
+            h = F_.silu(self.win(sp.u))
+            for r in range(NR):
+                Y = [torch.sparse.mm(a, h) for a in sp.E]
+                m = sum(self.we[r].weight[:, k] * Y[k] for k in range(FE)) + self.we[r].bias * Y[FE]
+                h = h + F_.silu(torch.cat([h, m], 1) @ self.dense[r].weight.t() + self.dense[r].bias)
+            hw = h * self.wo
+            F = torch.stack([(hw * torch.sparse.mm(d, h)).sum(1) for d in sp.D], 1) + self.bo * sp.dsum
+            F = F + (h @ self.wn + self.bn)[:, None] * sp.nrm[:, :3]
+            return self.scales[2] * F
+
     return SurrogateNet()
+
+
+class SparseInputs:
+    """Inputs as sparse adjacency matrices (COO, shared pattern): E_0..E_3
+    weighted by the edge features, E_4 by one, D_x, D_y, D_z by the unit
+    edge directions."""
+
+    def __init__(self, inp):
+        torch = _torch()
+        D, nv = inp.nbr.shape
+        sel = inp.nbr >= 0
+        rows = torch.arange(nv, device=inp.nbr.device).expand(D, nv)[sel]
+        cols = inp.nbr[sel]
+        ind = torch.stack([rows, cols])
+
+        def mat(v):
+            return torch.sparse_coo_tensor(ind, v, (nv, nv), check_invariants=False).coalesce()
+
+        self.E = [mat(inp.ef[..., k][sel]) for k in range(FE)] + [mat(torch.ones_like(inp.ef[..., 0][sel]))]
+        self.D = [mat(inp.dirs[..., k][sel]) for k in range(3)]
+        self.dsum = (inp.dirs * sel[..., None]).sum(0)
+        self.u = inp.u
+        self.nrm = inp.nrm
+        self.target = getattr(inp, "target", None)
 
 
 def to_blob(net):
@@ -222,13 +262,14 @@ def train(data, scales, iters=1500, lr=2e-3, seed=0, log=print, budget_s=420.0):
     sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, iters)
     n_val = max(1, len(data) // 8)
     train_set, val_set = data[:-n_val], data[-n_val:]
+    sparse = [SparseInputs(d) for d in train_set]
     t0 = time.time()
     for it in range(iters):
         if time.time() - t0 > budget_s:
             log(f"time budget reached after {it} iterations")
             break
-        d = train_set[it % len(train_set)]
-        F = net(d.u, d.nrm, d.nbr, d.ef, d.dirs)
+        d = sparse[it % len(sparse)]
+        F = net.forward_sparse(d)
         loss = ((F - d.target) ** 2).mean() / tgt_rms ** 2
         opt.zero_grad()
         loss.backward()
