@@ -235,6 +235,29 @@ def test_repulsion_with_cell_changes_inside_the_skin(C, stencil):
     assert rel(gg, eo.gradient(mo)) < RTOL
 
 
+def test_near_rows_across_cell_list_rebuilds(C):
+    """The near rows outlive cell-list rebuilds while no vertex has moved
+    lc1/2 from where they were built, and are rebuilt on the device when one
+    has; every evaluation matches the oracle with the same cell lists."""
+    p, f = meshgen.jittered_icosphere(3, seed=7)
+    prm = workload_params(p, f, excl=1, rep_scale=1.3)
+    mo, eo, mg, eg = _pair(C, p, f, prm)
+    rng = np.random.default_rng(9)
+    lc1 = prm["rep_lc1"]
+    for step, scale in enumerate([0.2, 0.2, 0.3, 0.05]):
+        d = rng.uniform(-1.0, 1.0, size=p.shape) * (scale / np.sqrt(3.0)) * lc1
+        mo.points()[:] += d
+        mg.points()[:] += d
+        if step:
+            eo.update_repulsion(mo)
+            eg.update_repulsion(mg)
+        po = eo.properties(mo)
+        assert abs(eg.properties(mg)[5] - po[5]) <= RTOL * max(po[5], 1e-300), step
+        eng, gg = eg.gradient(mg, with_energy=True)
+        assert abs(eng - eo.energy(mo)) <= RTOL * abs(eo.energy(mo)), step
+        assert rel(gg, eo.gradient(mo)) < RTOL, step
+
+
 def test_repulsion_after_a_large_move(C):
     """One vertex moved by more than half the repulsion cut-off since the
     cell-list build: the evaluation leaves the near rows for the full

@@ -481,6 +481,10 @@ __global__ void k_commit(TopoW t, int W, unsigned long long seed, const long lon
   if (!ok) atomicExch(&st->status, TM_ERR_TOPOLOGY);
 }
 
+__global__ void k_set_int(int* p, int v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *p = v;
+}
+
 __global__ void k_owner_init(int* owner, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) owner[i] = INT_MAX;
@@ -558,7 +562,11 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     // least one proposal and the loop ends
   }
   m->host_topo_stale = true;
-  if (hs.acc > 0) ++m->topo_version;
+  if (hs.acc > 0) {
+    ++m->topo_version;
+    k_set_int<<<1, 1, 0, s>>>(m->d_topo_ver.get(), (int)(m->topo_version & 0x7fffffff));
+    TM_LAUNCH();
+  }
   return hs.acc;
 }
 

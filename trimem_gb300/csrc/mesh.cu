@@ -383,6 +383,8 @@ static void upload_topology(tm_mesh* m) {
   m->d_edge.ensure(m->ne);
   m->d_scratch.ensure(4096);
   m->d_status.ensure(4);
+  m->d_topo_ver.ensure(1);
+  TM_CUDA(cudaMemsetAsync(m->d_topo_ver.get(), 0, sizeof(int), m->stream));
   cudaStream_t s = m->stream;
   if (nh) {
     TM_CUDA(cudaMemcpyAsync(m->d_to.get(), m->h_to.data(), sizeof(int) * nh, cudaMemcpyHostToDevice, s));

@@ -424,27 +424,38 @@ __global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt,
   if (!pass) cnt[a] = n;
 }
 
-// Near rows: the build-time members of the 5 x 5 x 5 cells around each
-// vertex's build cell (x outer, z inner, members ascending) closer than rn
-// at the build (squared threshold rn2, rounded up), with their cell offset
-// and a flag for pairs excluded on the build topology.
-__global__ void k_near(int nv, const double* P, NLView nl, Topo t, const int* vcoord, int excl, double rn2, int pass,
-                       int* cnt, const int* off, int2* out) {
+// Near rows (rebuilt only when flagged stale): the vertices closer than rn
+// to each vertex (squared threshold rn2, rounded up), found through the cell
+// table (the cells that meet the ball of radius rn), with a flag for pairs
+// excluded on the current topology.  A row longer than TM_NEAR_CAP marks the
+// rows unusable (flag[3]).
+__global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, double rn, double rn2, int* flag,
+                       int* ncnt, int* nent, double* xb) {
+  if (flag[1] == 0) return;  // rows still valid
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nv) return;
   const NLGeom& G = nl.geom[0];
   d3 pa = ld3(P, a);
+  const double* pp = &pa.x;
+  int lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = max(0, (int)floor((pp[k] - rn - G.bmin[k]) * G.inv_rl[k]) - 1);
+    hi[k] = min(G.shape[k] - 1, (int)floor((pp[k] + rn - G.bmin[k]) * G.inv_rl[k]) + 1);
+  }
   int n = 0;
-  int base = pass ? off[a] : 0;
-  for (int dx = -2; dx <= 2; ++dx) {
-    int ii = vcoord[3 * a] + dx;
-    if (ii < 0 || ii >= G.shape[0]) continue;
-    for (int dy = -2; dy <= 2; ++dy) {
-      int jj = vcoord[3 * a + 1] + dy;
-      if (jj < 0 || jj >= G.shape[1]) continue;
-      for (int dz = -2; dz <= 2; ++dz) {
-        int kk = vcoord[3 * a + 2] + dz;
-        if (kk < 0 || kk >= G.shape[2]) continue;
+  int* row = nent + (size_t)a * TM_NEAR_CAP;
+  for (int ii = lo[0]; ii <= hi[0]; ++ii)
+    for (int jj = lo[1]; jj <= hi[1]; ++jj)
+      for (int kk = lo[2]; kk <= hi[2]; ++kk) {
+        // skip cells whose box is farther than rn
+        double g2 = 0.0;
+        const int cc[3] = {ii, jj, kk};
+        for (int k = 0; k < 3; ++k) {
+          double c0 = G.bmin[k] + cc[k] * G.rl[k], c1 = c0 + G.rl[k];
+          double dd = pp[k] < c0 ? c0 - pp[k] : (pp[k] > c1 ? pp[k] - c1 : 0.0);
+          g2 += dd * dd;
+        }
+        if (g2 > rn2 * 1.000001) continue;
         long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
         int st = 0;
         int c = cell_lookup(nl, cid, &st);
@@ -454,17 +465,32 @@ __global__ void k_near(int nv, const double* P, NLView nl, Topo t, const int* vc
           d3 pb = ld3(P, b);
           double ex = pa.x - pb.x, ey = pa.y - pb.y, ez = pa.z - pb.z;
           if (ex * ex + ey * ey + ez * ez >= rn2) continue;
-          if (pass) {
-            int code = (dx + 2) | ((dy + 2) << 3) | ((dz + 2) << 6);
-            if (nl_excluded(t, excl, a, b)) code |= 1 << 9;
-            out[base + n] = make_int2(b, code);
-          }
+          if (n < TM_NEAR_CAP) row[n] = nl_excluded(t, excl, a, b) ? (int)(0x80000000u | (unsigned)b) : b;
           ++n;
         }
       }
-    }
-  }
-  if (!pass) cnt[a] = n;
+  if (n > TM_NEAR_CAP) atomicOr(&flag[3], 1);
+  ncnt[a] = min(n, TM_NEAR_CAP);
+  xb[3 * a] = pa.x;
+  xb[3 * a + 1] = pa.y;
+  xb[3 * a + 2] = pa.z;
+}
+// after a build: usable unless a row overflowed; record the topology version
+__global__ void k_near_done(int* flag, const int* dtopo) {
+  if (threadIdx.x || blockIdx.x) return;
+  if (flag[1] == 0) return;
+  flag[1] = flag[3];
+  flag[2] = *dtopo;
+  flag[3] = 0;
+}
+// before a cell-list rebuild: the rows go stale once some vertex has moved
+// lc1/2 or more from where they were built (thr2 rounded down; NaN moves)
+__global__ void k_near_check(int nv, const double* __restrict__ P, const double* __restrict__ xb, double thr2,
+                             int* flag) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv || flag[1]) return;
+  double dx = P[3 * v] - xb[3 * v], dy = P[3 * v + 1] - xb[3 * v + 1], dz = P[3 * v + 2] - xb[3 * v + 2];
+  if (!(dx * dx + dy * dy + dz * dz < thr2)) flag[1] = 1;
 }
 
 // distance_matrix of the Verlet list: rows in vertex order, d < rd
@@ -569,6 +595,7 @@ static void build_cells(tm_nlist* nl, NLView& V, int nv, const double* P, cudaSt
   TM_LAUNCH();
   V.table = nl->table.get();
   V.cell_verts = nl->cell_verts.get();
+  V.bcoord = nl->vcoord.get();  // build-time cell of every vertex
   if (nv > 0) {
     k_cell_insert<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, nl->table.get(), nl->vcid.get(), nl->vcoord.get(),
                                                 nl->vslot.get(), nl->d_count.get());
@@ -605,43 +632,46 @@ static void build_cells(tm_nlist* nl, NLView& V, int nv, const double* P, cudaSt
       TM_LAUNCH();
       V.crow = nl->crow.get();
       V.ccol = nl->ccol.get();
-      V.bcoord = nl->vcoord.get();
     }
   }
 }
 
-// Near rows for repulsion queries at cut-off lc1 (skin lc1).  A pair closer
-// than lc1 at query time whose vertices both moved less than lc1/2 since the
-// build was closer than 2 lc1 at the build.  Cells are at least rlist wide
-// and rlist >= lc1, so such a vertex is at most one cell away from its build
-// cell and such a neighbour at most two cells away from the vertex's build
-// cell: the near row holds every candidate the query can accept, and the
-// query keeps the entries whose cell is among the 27 around its current
-// cell, in the reference's scan order (a subsequence of the row's order).
-static void build_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, double lc1, cudaStream_t s) {
+// Near rows for repulsion queries at cut-off lc1 (skin lc1/2).  A pair
+// closer than lc1 at query time whose vertices both moved less than lc1/2
+// since the rows were built was closer than 2 lc1 then, so the row holds
+// every neighbour the query can accept; the query keeps the ones whose
+// build-time cell of the current cell list is among the 27 around its own
+// current cell and visits them in the reference's order.  The rows do not
+// depend on the cell list, so a cell-list rebuild rebuilds them only when a
+// vertex has moved lc1/2 since they were built (decided on the device).
+static void refresh_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, double lc1, cudaStream_t s) {
   int nv = nl->nv;
   Topo t = m->topo();
   double rn = 2.0 * lc1;
-  nl->nrow.ensure((size_t)nv + 1);
-  nl->cnt.ensure((size_t)nv + 1);
-  k_near<<<nblk(nv, 128), 128, 0, s>>>(nv, P, V, t, nl->vcoord.get(), V.excl, rn * rn * (1.0 + 1e-12), 0,
-                                       nl->cnt.get(), nullptr, nullptr);
+  if (nl->near_nv != nv || nl->near_lc1 != lc1) {
+    nl->nent.ensure((size_t)nv * TM_NEAR_CAP);
+    nl->ncnt.ensure(nv);
+    nl->xb.ensure(3 * (size_t)nv);
+    nl->nflag.ensure(4);
+    int init[4] = {0, 1, 0, 0};  // stale until built
+    TM_CUDA(cudaMemcpyAsync(nl->nflag.get(), init, sizeof(init), cudaMemcpyHostToDevice, s));
+    TM_CUDA(cudaStreamSynchronize(s));
+    nl->near_nv = nv;
+    nl->near_lc1 = lc1;
+    nl->near_move2 = 0.25 * lc1 * lc1 * (1.0 - 1e-12);
+  }
+  int* flag = nl->nflag.get();
+  k_near_check<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->xb.get(), nl->near_move2, flag);
   TM_LAUNCH();
-  TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
-  int total = 0;
-  exclusive_scan_int(nl->cnt.get(), nl->nrow.get(), nv + 1, &total, nl->tmp, s);
-  nl->nent.ensure(std::max(total, 1));
-  k_near<<<nblk(nv, 128), 128, 0, s>>>(nv, P, V, t, nl->vcoord.get(), V.excl, rn * rn * (1.0 + 1e-12), 1,
-                                       nullptr, nl->nrow.get(), nl->nent.get());
+  k_near<<<nblk(nv, 128), 128, 0, s>>>(nv, P, V, t, V.excl, rn, rn * rn * (1.0 + 1e-12), flag, nl->ncnt.get(),
+                                       nl->nent.get(), nl->xb.get());
   TM_LAUNCH();
-  nl->xb.ensure(3 * (size_t)nv);
-  TM_CUDA(cudaMemcpyAsync(nl->xb.get(), P, sizeof(double) * 3 * nv, cudaMemcpyDeviceToDevice, s));
-  nl->moved.ensure(1);
-  nl->near_lc1 = lc1;
-  nl->near_move2 = 0.25 * lc1 * lc1 * (1.0 - 1e-12);
-  nl->topo_version = m->topo_version;
-  V.nrow = nl->nrow.get();
+  k_near_done<<<1, 32, 0, s>>>(flag, m->d_topo_ver.get());
+  TM_LAUNCH();
   V.nent = nl->nent.get();
+  V.ncnt = nl->ncnt.get();
+  V.nflag = flag;
+  V.dtopo = m->d_topo_ver.get();
 }
 
 void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, cudaStream_t s) {
@@ -666,8 +696,7 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
   k_bbox_final<<<1, BB, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
   TM_LAUNCH();
   build_cells(nl, V, nv, P, s, p.n_search == 0);
-  if (p.n_search == 0 && V.crow && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1 && nv > 0)
-    build_near(nl, m, V, P, p.rep_lc1, s);
+  if (p.n_search == 0 && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1 && nv > 0) refresh_near(nl, m, V, P, p.rep_lc1, s);
   if (p.n_search == 1) {
     // Verlet CSR from the cell list at cut-off rlist, rows in the reference's
     // insertion order

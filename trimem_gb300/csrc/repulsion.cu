@@ -3,11 +3,11 @@
 // sum_j exp(l/(l - lc1)) / l^r over the neighbours closer than lc1 and, for a
 // gradient, 2 sum_j phi'(l) (x_i - x_j) / l.
 //
-// While no vertex has moved lc1/2 since the build (k_moved decides this for
-// the whole mesh before the pass) every vertex walks its near row in
-// k_rep_fast.  Otherwise a vertex whose current position still lies in its
-// build-time cell walks the precomputed candidate row of that cell; the few
-// that moved
+// While no vertex has moved lc1/2 since the near rows were built (k_moved
+// decides this for the whole mesh before the pass) every vertex walks its
+// near row in k_rep_fast.  Otherwise a vertex whose current position still
+// lies in its build-time cell walks the precomputed candidate row of that
+// cell; the few that moved
 // to another cell are queued and walk the 27 cells through the cell table in
 // a second kernel (k_rep_slow), so the long table walk never holds a warp of
 // fast vertices.  Both produce the per-vertex values in the reference's pair
@@ -45,11 +45,9 @@ template <bool GRAD>
 __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restrict__ P, NLView nl, EP ep,
                                                  double* __restrict__ pot, double* __restrict__ repg,
                                                  int* __restrict__ slow, int* __restrict__ nslow,
-                                                 const EP* __restrict__ eps, int near_mode,
-                                                 const int* __restrict__ moved) {
+                                                 const EP* __restrict__ eps, int use_near) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= t.nv) return;
-  if (near_mode && *moved) near_mode = 0;
   if (nl.vrep) {  // batch: per-replica cut-off, padding vertices have none
     int r = nl.vrep[v];
     if (r < 0) {
@@ -59,6 +57,10 @@ __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restri
     }
     ep = eps[r];
   }
+  // near rows usable: built, no vertex moved lc1/2 since (flags written by
+  // the previous kernels); mode 1 while the topology is the rows' one
+  int near_mode = 0;
+  if (use_near && nl.nflag[0] == 0 && nl.nflag[1] == 0) near_mode = nl.nflag[2] == *nl.dtopo ? 1 : 2;
   d3 p = ld3(P, v);
   PairTest pt = make_pair_test(nl, v, ep.rlc1, ep.rT);
   RepAcc acc{ep.rlc1, ep.rr, 0.0, mk(0, 0, 0), GRAD};
@@ -66,19 +68,10 @@ __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restri
   if (nl.kind == 0) {
     int co[3];
     bool fast = in_build_cell(nl, v, p, co);
-    int dx = 0, dy = 0, dz = 0;
-    if (near_mode) {
-      dx = co[0] - nl.bcoord[3 * v];
-      dy = co[1] - nl.bcoord[3 * v + 1];
-      dz = co[2] - nl.bcoord[3 * v + 2];
-      fast = dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
-    }
+    if (near_mode) fast = visit_near(pt, nl, P, v, p, near_mode, co, x, acc);
     warp_append(!fast, v, slow, nslow);
     if (!fast) return;
-    if (near_mode)
-      visit_near(pt, nl, P, v, p, near_mode, dx, dy, dz, x, acc);
-    else
-      visit_candidates(pt, nl, P, v, p, x, acc);
+    if (!near_mode) visit_candidates(pt, nl, P, v, p, x, acc);
   } else {
     visit_verlet(pt, nl, P, v, p, x, acc);
   }
@@ -138,14 +131,14 @@ __global__ void __launch_bounds__(256) k_rep_slow(Topo t, const double* __restri
   }
 }
 
-// *moved = 1 when some vertex is lc1/2 or farther from its build position
-// (squared threshold thr2, rounded down); NaN counts as moved
+// flag = 1 when some vertex is lc1/2 or farther from where the near rows
+// were built (squared threshold thr2, rounded down); NaN counts as moved
 __global__ void k_moved(int nv, const double* __restrict__ P, const double* __restrict__ xb, double thr2,
-                        int* moved) {
+                        int* flag) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
   double dx = P[3 * v] - xb[3 * v], dy = P[3 * v + 1] - xb[3 * v + 1], dz = P[3 * v + 2] - xb[3 * v + 2];
-  if (!(dx * dx + dy * dy + dz * dz < thr2)) atomicOr(moved, 1);
+  if (!(dx * dx + dy * dy + dz * dz < thr2)) atomicOr(flag, 1);
 }
 
 inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
@@ -166,19 +159,18 @@ void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos3
   NLView nlv = e->nl.view;
   nlv.pos32 = pos32;
   TM_CUDA(cudaMemsetAsync(nslow, 0, sizeof(int), s));
-  int near_mode = 0;
-  int* moved = nullptr;
-  if (nlv.kind == 0 && nlv.nrow && !eps && e->nl.near_lc1 == ep.rlc1 && e->nl.nv == nv) {
-    near_mode = m->topo_version == e->nl.topo_version ? 1 : 2;
-    moved = e->nl.moved.get();
-    TM_CUDA(cudaMemsetAsync(moved, 0, sizeof(int), s));
-    k_moved<<<nblk(nv, 256), 256, 0, s>>>(nv, P, e->nl.xb.get(), e->nl.near_move2, moved);
+  int use_near = 0;
+  if (nlv.kind == 0 && nlv.nent && !eps && e->nl.near_lc1 == ep.rlc1 && e->nl.near_nv == nv) {
+    use_near = 1;
+    int* flag = e->nl.nflag.get();
+    TM_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    k_moved<<<nblk(nv, 256), 256, 0, s>>>(nv, P, e->nl.xb.get(), e->nl.near_move2, flag);
     TM_LAUNCH();
   }
   if (want_grad)
-    k_rep_fast<true><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps, near_mode, moved);
+    k_rep_fast<true><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps, use_near);
   else
-    k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps, near_mode, moved);
+    k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps, use_near);
   TM_LAUNCH();
   if (nlv.kind == 0) {
     int grid = 8 * 152;  // 8 warps per block, one warp per queued vertex

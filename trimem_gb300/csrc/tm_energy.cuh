@@ -168,27 +168,50 @@ __device__ __forceinline__ void visit_candidates(const PairTest& pt, const NLVie
   int lo = nl.crow[v], hi = nl.crow[v + 1];
   for (int q = lo; q < hi; ++q) visit_pair(pt, nl, P, v, p, nl.ccol[q], is_excluded, fn);
 }
-// The near row of v restricted to the 27 cells around its current cell,
-// which lies (ddx, ddy, ddz) from its build cell: the reference's candidates
-// of that cell closer than 2 lc1 at the build, in the reference's order.
-// mode 1: topology unchanged since the build, entries flagged excluded are
-// skipped without a test; mode 2: exclusion tested on the current topology.
+// The neighbours of v closer than the cut-off from its near row: those whose
+// build-time cell (of the current cell list) is among the 27 cells around
+// v's current cell co are the reference's candidates.  They are visited in
+// the reference's order (cell offset x outer / z inner, then ascending
+// index): the accepted pairs, usually none or one, are sorted in registers.
+// mode 1: topology unchanged since the rows were built, entries flagged
+// excluded are skipped without a test; mode 2: exclusion tested on the
+// current topology.  Returns false (nothing visited) when more than
+// NEAR_HITS pairs are accepted; the caller then takes the cell walk.
+constexpr int NEAR_HITS = 8;
 template <class F, class X>
-__device__ __forceinline__ void visit_near(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
-                                           int mode, int ddx, int ddy, int ddz, const X& is_excluded, F& fn) {
-  int lo = nl.nrow[v], hi = nl.nrow[v + 1];
-  for (int q = lo; q < hi; ++q) {
-    int2 c = nl.nent[q];
-    int ox = (c.y & 7) - 2 - ddx, oy = ((c.y >> 3) & 7) - 2 - ddy, oz = ((c.y >> 6) & 7) - 2 - ddz;
-    if (ox < -1 || ox > 1 || oy < -1 || oy > 1 || oz < -1 || oz > 1) continue;
-    if (mode == 1 && (c.y & (1 << 9))) continue;
-    int j = c.x;
+__device__ __forceinline__ bool visit_near(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,
+                                           int mode, const int* co, const X& is_excluded, F& fn) {
+  const int* row = nl.nent + (size_t)v * TM_NEAR_CAP;
+  const int n = nl.ncnt[v];
+  long long key[NEAR_HITS];
+  double dist[NEAR_HITS];
+  d3 dif[NEAR_HITS];
+  int hits = 0;
+  for (int q = 0; q < n; ++q) {
+    int c = row[q];
+    if (mode == 1 && c < 0) continue;
+    int j = c & 0x7fffffff;
     d3 pj;
     double s;
     if (!pair_within(pt, nl, P, p, j, &pj, &s)) continue;
+    int ox = nl.bcoord[3 * j] - co[0], oy = nl.bcoord[3 * j + 1] - co[1], oz = nl.bcoord[3 * j + 2] - co[2];
+    if (ox < -1 || ox > 1 || oy < -1 || oy > 1 || oz < -1 || oz > 1) continue;
     if (mode == 2 && nl.excl > 0 && is_excluded(v, j)) continue;
-    fn(j, __dsqrt_rn(s), exact_diff(p, pj));
+    if (hits == NEAR_HITS) return false;
+    long long k = ((long long)((ox + 1) * 9 + (oy + 1) * 3 + (oz + 1)) << 32) | (long long)j;
+    int h = hits++;
+    while (h > 0 && key[h - 1] > k) {
+      key[h] = key[h - 1];
+      dist[h] = dist[h - 1];
+      dif[h] = dif[h - 1];
+      --h;
+    }
+    key[h] = k;
+    dist[h] = __dsqrt_rn(s);
+    dif[h] = exact_diff(p, pj);
   }
+  for (int h = 0; h < hits; ++h) fn((int)(key[h] & 0xffffffff), dist[h], dif[h]);
+  return true;
 }
 template <class F, class X>
 __device__ __forceinline__ void visit_cells(const PairTest& pt, const NLView& nl, const double* P, int v, d3 p,

@@ -91,6 +91,8 @@ struct NLGeom {
   int pad;
   long long stride[3];
 };
+constexpr int TM_NEAR_CAP = 48;  // near-row capacity per vertex
+
 struct NLView {
   int kind;  // 0 cell list, 1 Verlet list
   int excl;
@@ -110,13 +112,16 @@ struct NLView {
   const int* ccol;
   const int* bcoord;   // build-time cell coordinates, 3 per vertex
   const float* pos32;  // positions rounded to float (prefilter), may be NULL
-  // near rows: per vertex the build-time members of the 5 x 5 x 5 cells
-  // around its build cell (x outer, z inner, members ascending) closer than
-  // 2 lc1 at the build; entry x = neighbour, y = cell offset (dx+2) |
-  // (dy+2) << 3 | (dz+2) << 6, bit 9 set when the pair was excluded on the
-  // build topology.  Valid while no vertex moved lc1/2 or more since the build.
-  const int* nrow;
-  const int2* nent;
+  // near rows: per vertex (fixed stride TM_NEAR_CAP) the vertices closer
+  // than 2 lc1 when the rows were built, bit 31 set when the pair was
+  // excluded on the topology of that time; ncnt = row lengths.  nflag[0]:
+  // some vertex moved lc1/2 or more since (set per evaluation), nflag[1]:
+  // rows unusable (never built, overflow), nflag[2]: device topology
+  // version at the build; dtopo: the mesh's current device topology version
+  const int* nent;
+  const int* ncnt;
+  const int* nflag;
+  const int* dtopo;
 };
 
 #ifdef __CUDACC__
@@ -147,6 +152,7 @@ struct tm_mesh {
   tmg::DevBuf<int4> d_edge;
   tmg::DevBuf<double> d_scratch;  // primitives / utilities
   tmg::DevBuf<int> d_status;
+  tmg::DevBuf<int> d_topo_ver;  // device copy of topo_version (low 31 bits)
   cudaStream_t stream = nullptr;
   unsigned long long topo_version = 0;  // advanced by every flip sweep that flips
   tmg::Topo topo() const;
@@ -167,11 +173,10 @@ struct tm_nlist {
   tmg::DevBuf<long long> vcid;
   tmg::DevBuf<double> bbox;
   // near rows (see NLView) and what they were built for
-  tmg::DevBuf<int> nrow, moved;
-  tmg::DevBuf<int2> nent;
-  tmg::DevBuf<double> xb;  // positions at the build
+  tmg::DevBuf<int> nent, ncnt, nflag;
+  tmg::DevBuf<double> xb;  // positions when the near rows were built
   double near_lc1 = 0.0, near_move2 = 0.0;
-  unsigned long long topo_version = 0;
+  int near_nv = -1;
   // last query result
   std::vector<double> res_d;
   std::vector<int> res_i, res_j;
