@@ -1069,7 +1069,23 @@ static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, 
   int ne = m.ne();
   long nflips = (long)(ne * ratio);
   Props props = E.properties(m);
-  double e0 = E.energy(props);
+  // Metropolis energy as the device's flip_energy: reciprocals of the
+  // reference properties instead of divisions, same summation order
+  const Props ref = E.ref_props();
+  const double irA = 1.0 / ref.area, irV = 1.0 / ref.volume, irC = 1.0 / ref.curvature;
+  const om_params& q = E.prm;
+  auto flip_energy = [&](const Props& p) {
+    double da = p.area * irA - 1.0, dv = p.volume * irV - 1.0, dc = p.curvature * irC - 1.0;
+    double tot = 0.0;
+    tot += q.kappa_a * da * da;
+    tot += q.kappa_v * dv * dv;
+    tot += q.kappa_c * dc * dc;
+    tot += q.kappa_t * p.tethering;
+    tot += q.kappa_r * p.repulsion;
+    tot += q.kappa_b * p.bending;
+    return tot;
+  };
+  double e0 = flip_energy(props);
   std::vector<int> owner(ne, std::numeric_limits<int>::max());
   std::vector<long> pending;
   long next_new = 0;
@@ -1170,7 +1186,7 @@ static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, 
       if (!ok[s]) continue;
       Props trial = props;
       trial -= dps[s];
-      double en = E.energy(trial);
+      double en = flip_energy(trial);
       double de = en - e0;
       if (de <= -std::log(flip_u_of(seed, win[s]))) {
         props = trial;

@@ -267,10 +267,28 @@ __device__ void vprops_ring(const Ring& R, int v, const double* P, const EP& ep,
 }
 
 // ---- window kernels --------------------------------------------------------
-__global__ void k_flip_init(EP ep, const Globals* g, FlipState* st) {
+// Energy of a property set for the Metropolis test: the penalty energy of
+// src/kernel.h:110-122 in its summation order, with the reciprocals of the
+// reference properties (rounded once on the host) in place of divisions.
+struct FlipE {
+  double irA, irV, irC, ka, kv, kc, kt, kr, kb;
+};
+__device__ __forceinline__ double flip_energy(const FlipE& f, const double* p) {
+  double da = p[0] * f.irA - 1.0, dv = p[1] * f.irV - 1.0, dc = p[2] * f.irC - 1.0;
+  double tot = 0.0;
+  tot += f.ka * da * da;
+  tot += f.kv * dv * dv;
+  tot += f.kc * dc * dc;
+  tot += f.kt * p[4];
+  tot += f.kr * p[5];
+  tot += f.kb * p[3];
+  return tot;
+}
+
+__global__ void k_flip_init(FlipE fe, const Globals* g, FlipState* st) {
   if (threadIdx.x || blockIdx.x) return;
   for (int k = 0; k < 6; ++k) st->props[k] = g->props[k];
-  st->e0 = energy_of(ep, st->props);
+  st->e0 = flip_energy(fe, st->props);
   st->acc = 0;
   st->npend = 0;
   st->status = 0;
@@ -369,7 +387,7 @@ __global__ void k_prep(int W, unsigned long long seed, const long long* win, con
 // compacted in order for the next window.
 constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread (contiguous)
 __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const unsigned char* winner,
-                                             const double* dpn, EP ep, FlipState* st, const int* limit,
+                                             const double* dpn, FlipE fe, FlipState* st, const int* limit,
                                              unsigned char* accepted, long long* pend) {
   __shared__ double sP[6], se0;
   __shared__ int sfirst, sstart, sacc;
@@ -397,7 +415,7 @@ __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const
       if (o8[7] == 0.0) continue;
       double trial[6];
       for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
-      double de = energy_of(ep, trial) - se0;
+      double de = flip_energy(fe, trial) - se0;
       if (de <= o8[6]) {
         atomicMin(&sfirst, s);
         break;  // later slots of this thread cannot be first
@@ -410,7 +428,7 @@ __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const
       const double* o8 = dpn + 8 * (size_t)first;
       double trial[6];
       for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
-      double en = energy_of(ep, trial);
+      double en = flip_energy(fe, trial);
       for (int q = 0; q < 6; ++q) sP[q] = trial[q];
       se0 = en;
       sacc += 1;
@@ -527,7 +545,8 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   limit.ensure(1);
   k_owner_init<<<nblk(ne, 256), 256, 0, s>>>(owner.get(), ne);
   TM_LAUNCH();
-  k_flip_init<<<1, 1, 0, s>>>(ep, e->glob.get(), st.get());
+  FlipE fe{1.0 / ep.refA, 1.0 / ep.refV, 1.0 / ep.refC, ep.ka, ep.kv, ep.kc, ep.kt, ep.kr, ep.kb};
+  k_flip_init<<<1, 1, 0, s>>>(fe, e->glob.get(), st.get());
   TM_LAUNCH();
   FlipState hs;
   hs.npend = 0;
@@ -550,7 +569,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     k_prep<<<nblk(W, 128), 128, 0, s>>>(W, seed, win.get(), winner.get(), okf.get(), part.get(), limit.get(),
                                         dpn.get());
     TM_LAUNCH();
-    k_metro<<<1, MB, 0, s>>>(W, win.get(), winner.get(), dpn.get(), ep, st.get(), limit.get(), acc.get(),
+    k_metro<<<1, MB, 0, s>>>(W, win.get(), winner.get(), dpn.get(), fe, st.get(), limit.get(), acc.get(),
                              pend.get());
     TM_LAUNCH();
     k_commit<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), acc.get(), st.get());
