@@ -96,12 +96,6 @@ inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 
 __device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x)); }
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // vertex features, normal and embedding (one thread per vertex)
 __global__ void k_sfeat(Topo t, const FaceF* __restrict__ fd, const EdgeF* __restrict__ ed,
                         const float* __restrict__ rho, const SurW* __restrict__ W, float* __restrict__ u,
@@ -163,39 +157,59 @@ __device__ __forceinline__ void edge_feat(const EdgeF& E, float ri, float rj, fl
   ef[3] = 0.5f * (rj + ri) * lbar;
 }
 
-// m_i = sum_j (W_e e_ij + b_e) * h_j (one warp per vertex, two channels per lane)
+__device__ __forceinline__ void unpack8(uint4 v, float* f) {
+  const __nv_bfloat162* b = reinterpret_cast<const __nv_bfloat162*>(&v);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float2 x = __bfloat1622float2(b[q]);
+    f[2 * q] = x.x;
+    f[2 * q + 1] = x.y;
+  }
+}
+__device__ __forceinline__ uint4 pack8(const float* f) {
+  uint4 v;
+  __nv_bfloat162* b = reinterpret_cast<__nv_bfloat162*>(&v);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) b[q] = __floats2bfloat162_rn(f[2 * q], f[2 * q + 1]);
+  return v;
+}
+
+// m_i = sum_j (W_e e_ij + b_e) * h_j: eight threads per vertex, eight
+// channels (16 bytes of h_j) per thread
 __global__ void k_agg(Topo t, const EdgeF* __restrict__ ed, const float* __restrict__ rho,
                       const SurW* __restrict__ W, int r, const __nv_bfloat16* __restrict__ h,
                       __nv_bfloat16* __restrict__ mout) {
-  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = g >> 3, sub = g & 7;
   if (i >= t.nv) return;
-  const int c0 = 2 * lane, c1 = c0 + 1;
-  float w0[FE], w1[FE];
-  for (int k = 0; k < FE; ++k) {
-    w0[k] = W->we[r][c0 * FE + k];
-    w1[k] = W->we[r][c1 * FE + k];
+  float w[8][FE], b[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int ch = 8 * sub + c;
+#pragma unroll
+    for (int k = 0; k < FE; ++k) w[c][k] = W->we[r][ch * FE + k];
+    b[c] = W->be[r][ch];
   }
-  const float b0 = W->be[r][c0], b1 = W->be[r][c1], lbar = W->lbar;
-  const float ri = rho[i];
-  const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(h);
-  float a0 = 0.f, a1 = 0.f;
-  int d = t.val[i];
+  const float lbar = W->lbar, ri = rho[i];
+  const uint4* h4 = reinterpret_cast<const uint4*>(h);
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const int d = t.val[i];
   for (int m = 0; m < d; ++m) {
     int4 s = t.slot[(size_t)m * t.nv + i];
-    int j = s.x;
+    const int j = s.x;
     float ef[FE];
     edge_feat(ed[s.z], ri, rho[j], lbar, ef);
-    float g0 = b0, g1 = b1;
-    for (int k = 0; k < FE; ++k) {
-      g0 += w0[k] * ef[k];
-      g1 += w1[k] * ef[k];
+    float hj[8];
+    unpack8(h4[(size_t)j * (H / 8) + sub], hj);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      float gt = b[c];
+#pragma unroll
+      for (int k = 0; k < FE; ++k) gt += w[c][k] * ef[k];
+      acc[c] += gt * hj[c];
     }
-    float2 hj = __bfloat1622float2(h2[(size_t)j * (H / 2) + lane]);
-    a0 += g0 * hj.x;
-    a1 += g1 * hj.y;
   }
-  reinterpret_cast<__nv_bfloat162*>(mout)[(size_t)i * (H / 2) + lane] = __floats2bfloat162_rn(a0, a1);
+  reinterpret_cast<uint4*>(mout)[(size_t)i * (H / 8) + sub] = pack8(acc);
 }
 
 // h_out = h + SiLU([h | m] W^T + b) for 128 vertices per CTA on the tensor cores
@@ -287,32 +301,48 @@ __global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorM
   if (warp == 0) tmem_dealloc(tmem, 64);
 }
 
-// output head: g = g_local - s (sum_j c_ij t_ij + c_i N_i) (one warp per vertex)
+// output head: g = g_local - s (sum_j c_ij d_ij + c_i N_i), eight threads
+// per vertex with eight channels each; the channel sums are reduced within
+// the eight threads in a fixed order
 __global__ void k_out(Topo t, Split S, const float* __restrict__ nrm, const SurW* __restrict__ W,
                       const __nv_bfloat16* __restrict__ h, const double* __restrict__ gloc, double* __restrict__ g) {
-  int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt >> 3, sub = gt & 7;
   if (i >= t.nv) return;
-  const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(h);
-  float2 hi = __bfloat1622float2(h2[(size_t)i * (H / 2) + lane]);
-  const float wo0 = W->wo[2 * lane], wo1 = W->wo[2 * lane + 1];
-  const float pi0 = wo0 * hi.x, pi1 = wo1 * hi.y;
-  float cn = warp_sum(W->wn[2 * lane] * hi.x + W->wn[2 * lane + 1] * hi.y) + W->bn;
-  f3 F = cn * f3{nrm[4 * (size_t)i], nrm[4 * (size_t)i + 1], nrm[4 * (size_t)i + 2]};
-  int d = t.val[i];
-  for (int m = 0; m < d; ++m) {
-    int j = t.nbr[(size_t)m * t.nv + i];
-    float2 hj = __bfloat1622float2(h2[(size_t)j * (H / 2) + lane]);
-    float c = warp_sum(pi0 * hj.x + pi1 * hj.y) + W->bo;
-    f3 e = S.diff(j, i);
-    float l = fnorm(e);
-    F += (c / l) * e;
+  const unsigned gmask = 0xffu << (threadIdx.x & 24);  // the eight threads of this vertex
+  const uint4* h4 = reinterpret_cast<const uint4*>(h);
+  float hi[8], pi[8];
+  unpack8(h4[(size_t)i * (H / 8) + sub], hi);
+  float cn = 0.f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    pi[c] = W->wo[8 * sub + c] * hi[c];
+    cn += W->wn[8 * sub + c] * hi[c];
   }
-  if (lane == 0) {
-    const float s = W->fscale;
-    g[3 * (size_t)i] = gloc[3 * (size_t)i] - (double)(s * F.x);
-    g[3 * (size_t)i + 1] = gloc[3 * (size_t)i + 1] - (double)(s * F.y);
-    g[3 * (size_t)i + 2] = gloc[3 * (size_t)i + 2] - (double)(s * F.z);
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) cn += __shfl_xor_sync(gmask, cn, o);
+  cn += W->bn;
+  f3 F = cn * f3{nrm[4 * (size_t)i], nrm[4 * (size_t)i + 1], nrm[4 * (size_t)i + 2]};
+  const float bo = W->bo;
+  const int d = t.val[i];
+  for (int m = 0; m < d; ++m) {
+    const int j = t.nbr[(size_t)m * t.nv + i];
+    float hj[8];
+    unpack8(h4[(size_t)j * (H / 8) + sub], hj);
+    float c = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) c += pi[q] * hj[q];
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) c += __shfl_xor_sync(gmask, c, o);
+    c += bo;
+    f3 e = S.diff(j, i);
+    F += (c / fnorm(e)) * e;
+  }
+  if (sub == 0) {
+    const float sc = W->fscale;
+    g[3 * (size_t)i] = gloc[3 * (size_t)i] - (double)(sc * F.x);
+    g[3 * (size_t)i + 1] = gloc[3 * (size_t)i + 1] - (double)(sc * F.y);
+    g[3 * (size_t)i + 2] = gloc[3 * (size_t)i + 2] - (double)(sc * F.z);
   }
 }
 
@@ -430,12 +460,12 @@ void surrogate_grad(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* P,
   TM_LAUNCH();
   int cur = 0;
   for (int r = 0; r < NR; ++r) {
-    k_agg<<<nblk(32L * nv, 256), 256, 0, s>>>(t, ed, rho, W, r, sg->hb[cur].get(), sg->mb.get());
+    k_agg<<<nblk(8L * nv, 256), 256, 0, s>>>(t, ed, rho, W, r, sg->hb[cur].get(), sg->mb.get());
     TM_LAUNCH();
     dense_launch(sg->map_h[cur], sg->map_m, sg->map_w[r], W->b[r], sg->hb[cur ^ 1].get(), nv, sg->status.get(), s);
     cur ^= 1;
   }
-  k_out<<<nblk(32L * nv, 256), 256, 0, s>>>(t, S, sg->nrm.get(), W, sg->hb[cur].get(), sg->gloc.get(), g);
+  k_out<<<nblk(8L * nv, 256), 256, 0, s>>>(t, S, sg->nrm.get(), W, sg->hb[cur].get(), sg->gloc.get(), g);
   TM_LAUNCH();
 }
 
