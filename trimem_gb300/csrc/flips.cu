@@ -261,8 +261,17 @@ __device__ void vprops_ring(const Ring& R, int v, const double* P, const EP& ep,
   double pot = 0.0;
   const double lc1 = ep.rlc1;
   const int rr = ep.rr;
-  for_each_neighbour_x(nl, P, v, xv, lc1, ep.rT, excl,
-                       [&](int, double l, d3) { pot += exp(l / (l - lc1)) / ipow(l, rr); });
+  auto add = [&](int, double l, d3) { pot += exp(l / (l - lc1)) / ipow(l, rr); };
+  // the near rows when usable (exclusion tested with this ring's rules),
+  // else the candidate row / cell walk; both visit in the reference's order
+  bool done = false;
+  if (nl.kind == 0 && nl.nent && nl.nflag[0] == 0 && nl.nflag[1] == 0) {
+    PairTest pt = make_pair_test(nl, v, lc1, ep.rT);
+    int co[3];
+    in_build_cell(nl, v, xv, co);
+    done = visit_near(pt, nl, P, v, xv, 2, co, excl, add);
+  }
+  if (!done) for_each_neighbour_x(nl, P, v, xv, lc1, ep.rT, excl, add);
   out[5] = pot;
 }
 
