@@ -575,11 +575,11 @@ def main():
         cb = cpu_baseline(p, f, prm)
 
     # this library's kernels per step: 8 per FP64 evaluation (k_face, k_edge,
-    # k_bond_short, k_moved, k_rep_fast, k_rep_slow, k_vertex, k_grad) and 22
+    # k_bond_short, k_moved, k_rep_fast, k_rep_slow, k_vertex, k_grad) and 14
     # per cell-list rebuild (box 2, table 1, insert 1, counts 1, scan 3,
-    # starts 1, scatter 1, sort 1, candidate rows 2 + scan 3, near rows
-    # 2 + scan 3); the displacement and L2-flush kernels are torch's
-    launches_per_step = 8 * EVALS_PER_STEP + 22
+    # starts 1, scatter 1, sort 1, near-row check / build / done 3); the
+    # displacement and L2-flush kernels are torch's
+    launches_per_step = 8 * EVALS_PER_STEP + 14
     peaks_fp64 = {"fp64_gflops_measured_probe": 1196.0}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,

@@ -695,8 +695,11 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
   }
   k_bbox_final<<<1, BB, 0, s>>>(nv > 0 ? nb : 0, nl->bbox.get(), p.rlist, nl->geom.get());
   TM_LAUNCH();
-  build_cells(nl, V, nv, P, s, p.n_search == 0);
-  if (p.n_search == 0 && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1 && nv > 0) refresh_near(nl, m, V, P, p.rep_lc1, s);
+  // with near rows the candidate rows are not needed: the rare fallback
+  // (a vertex moved lc1/2 since the rows were built) takes the cell walk
+  const bool near = p.n_search == 0 && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1 && nv > 0;
+  build_cells(nl, V, nv, P, s, p.n_search == 0 && !near);
+  if (near) refresh_near(nl, m, V, P, p.rep_lc1, s);
   if (p.n_search == 1) {
     // Verlet CSR from the cell list at cut-off rlist, rows in the reference's
     // insertion order
