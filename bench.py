@@ -238,12 +238,15 @@ def chain_start():
     return x0, f, prm, info
 
 
+DT_CANDIDATES = (5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6, 5e-7, 2e-7)
+
+
 def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=100, weights=None):
     """ESS/s of the bending energy of a device chain: per step one HMC move
     (20 velocity-Verlet steps, m 1, T 1) and one flip sweep (ratio 0.2,
     98,304 attempts), neighbour list rebuilt every step.  dt: the largest of
-    5e-5 (the large-mesh runs' step), 2e-5, 1e-5, ... with pilot acceptance
-    >= 0.5 unless given."""
+    DT_CANDIDATES (from 5e-5, the large-mesh runs' step) with pilot
+    acceptance >= 0.5 unless given."""
     import torch
 
     from trimem_gb300 import capi
@@ -258,7 +261,7 @@ def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=100, weights=N
     sg = capi.Surrogate(mesh, weights) if weights is not None else None
     pilot = None
     if dt is None:
-        dt, pilot = tune_dt(mesh, en, x, stream=stream, force=sg)
+        dt, pilot = tune_dt(mesh, en, x, candidates=DT_CANDIDATES, stream=stream, force=sg)
     ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=11, stream=stream, force=sg)
     ch.run(n_burn)
     torch.cuda.synchronize()
@@ -564,7 +567,8 @@ def main():
         from trimem_gb300 import surrogate as S
 
         if os.path.exists(S.WEIGHTS_L7):
-            chain["surrogate"] = chain_leg(stream, start, 0, dt=plain["dt"], weights=np.load(S.WEIGHTS_L7))
+            # the surrogate chain tunes its own step on the same rule
+            chain["surrogate"] = chain_leg(stream, start, 0, weights=np.load(S.WEIGHTS_L7))
         else:
             chain["surrogate"] = {"error": "no trained weights"}
     except Exception as exc:
