@@ -329,6 +329,15 @@ def run_profile(args):
         print("profile surrogate evaluations done:", args.profile_surrogate)
         return
     if args.profile_flips:
+        # the chains' state: relaxed membrane, initial area / volume targets
+        from trimem_gb300.mc.device import relaxed_state
+
+        prm0 = dict(prm, cont_lambda=0.0)
+        x0, _ = relaxed_state(p, f, prm0)
+        mesh = capi.Mesh(x0, f)
+        en = capi.Energy(mesh, capi.params(**prm0))
+        x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
+        capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), None))
         for k in range(args.profile_flips):
             acc = ctypes.c_int32()
             capi.check(L.tm_flip_device(mesh.h, en.h, ctypes.c_void_p(x.data_ptr()), 0.2, 7 + k, 1, 1024,
