@@ -241,7 +241,7 @@ def chain_start():
 DT_CANDIDATES = (5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6, 5e-7, 2e-7)
 
 
-def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=100, weights=None):
+def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=200, weights=None):
     """ESS/s of the bending energy of a device chain: per step one HMC move
     (20 velocity-Verlet steps, m 1, T 1) and one flip sweep (ratio 0.2,
     98,304 attempts), neighbour list rebuilt every step.  dt: the largest of
