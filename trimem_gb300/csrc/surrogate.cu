@@ -174,42 +174,48 @@ __device__ __forceinline__ uint4 pack8(const float* f) {
   return v;
 }
 
-// m_i = sum_j (W_e e_ij + b_e) * h_j: eight threads per vertex, eight
-// channels (16 bytes of h_j) per thread
-__global__ void k_agg(Topo t, const EdgeF* __restrict__ ed, const float* __restrict__ rho,
-                      const SurW* __restrict__ W, int r, const __nv_bfloat16* __restrict__ h,
-                      __nv_bfloat16* __restrict__ mout) {
+// m_i = sum_j (W_e e_ij + b_e) * h_j: sixteen threads per vertex, four
+// channels (8 bytes of h_j) per thread; the next ring slot is loaded while
+// the current neighbour is summed
+__global__ void __launch_bounds__(256) k_agg(Topo t, const EdgeF* __restrict__ ed, const float* __restrict__ rho,
+                                             const SurW* __restrict__ W, int r, const __nv_bfloat16* __restrict__ h,
+                                             __nv_bfloat16* __restrict__ mout) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = g >> 3, sub = g & 7;
+  const int i = g >> 4, sub = g & 15;
   if (i >= t.nv) return;
-  float w[8][FE], b[8];
+  float4 w[4];
+  float b[4];
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const int ch = 8 * sub + c;
-#pragma unroll
-    for (int k = 0; k < FE; ++k) w[c][k] = W->we[r][ch * FE + k];
+  for (int c = 0; c < 4; ++c) {
+    const int ch = 4 * sub + c;
+    w[c] = *reinterpret_cast<const float4*>(&W->we[r][ch * FE]);
     b[c] = W->be[r][ch];
   }
   const float lbar = W->lbar, ri = rho[i];
-  const uint4* h4 = reinterpret_cast<const uint4*>(h);
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  const uint2* h2 = reinterpret_cast<const uint2*>(h);
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
   const int d = t.val[i];
+  int4 s = d > 0 ? t.slot[i] : make_int4(0, 0, 0, 0);
   for (int m = 0; m < d; ++m) {
-    int4 s = t.slot[(size_t)m * t.nv + i];
+    const int4 sn = m + 1 < d ? t.slot[(size_t)(m + 1) * t.nv + i] : s;
     const int j = s.x;
+    const uint2 hv = h2[(size_t)j * (H / 4) + sub];
     float ef[FE];
     edge_feat(ed[s.z], ri, rho[j], lbar, ef);
-    float hj[8];
-    unpack8(h4[(size_t)j * (H / 8) + sub], hj);
+    const float2 h01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&hv.x));
+    const float2 h23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&hv.y));
+    const float hj[4] = {h01.x, h01.y, h23.x, h23.y};
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      float gt = b[c];
-#pragma unroll
-      for (int k = 0; k < FE; ++k) gt += w[c][k] * ef[k];
+    for (int c = 0; c < 4; ++c) {
+      float gt = b[c] + w[c].x * ef[0] + w[c].y * ef[1] + w[c].z * ef[2] + w[c].w * ef[3];
       acc[c] += gt * hj[c];
     }
+    s = sn;
   }
-  reinterpret_cast<uint4*>(mout)[(size_t)i * (H / 8) + sub] = pack8(acc);
+  uint2 o;
+  *reinterpret_cast<__nv_bfloat162*>(&o.x) = __floats2bfloat162_rn(acc[0], acc[1]);
+  *reinterpret_cast<__nv_bfloat162*>(&o.y) = __floats2bfloat162_rn(acc[2], acc[3]);
+  reinterpret_cast<uint2*>(mout)[(size_t)i * (H / 4) + sub] = o;
 }
 
 // h_out = h + SiLU([h | m] W^T + b) for 128 vertices per CTA on the tensor cores
@@ -460,7 +466,7 @@ void surrogate_grad(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* P,
   TM_LAUNCH();
   int cur = 0;
   for (int r = 0; r < NR; ++r) {
-    k_agg<<<nblk(8L * nv, 256), 256, 0, s>>>(t, ed, rho, W, r, sg->hb[cur].get(), sg->mb.get());
+    k_agg<<<nblk(16L * nv, 256), 256, 0, s>>>(t, ed, rho, W, r, sg->hb[cur].get(), sg->mb.get());
     TM_LAUNCH();
     dense_launch(sg->map_h[cur], sg->map_m, sg->map_w[r], W->b[r], sg->hb[cur ^ 1].get(), nv, sg->status.get(), s);
     cur ^= 1;
