@@ -64,10 +64,10 @@ def config(extra=None):
 
 
 def read_traffic():
-    """DRAM bytes per launch of each evaluation kernel from the committed ncu
-    summary (profiles/eval_kernels_L7_full.md)."""
+    """DRAM bytes per launch of each evaluation stage from the committed ncu
+    summary (profiles/eval_kernels_L7_fp64_sections.md)."""
     out = {}
-    path = os.path.join(ROOT, "profiles", "eval_kernels_L7_full.md")
+    path = os.path.join(ROOT, "profiles", "eval_kernels_L7_fp64_sections.md")
     try:
         for line in open(path):
             parts = line.split()
