@@ -8,7 +8,8 @@
 //   k_fill    window = deferred proposals (in order) + new proposals
 //   k_claim   each proposal claims the edges of its patch (the 1-ring edges
 //             of the quad's four vertices and the edges opposite them,
-//             flip_utils.cpp:43-68) with atomicMin of its window slot
+//             flip_utils.cpp:43-68) with atomicMax of a (window, slot) tag
+//             that the lowest slot of the current window wins
 //   k_winner  a proposal whose patch it owns entirely is a winner; in
 //             serial mode the window is cut at the first loser, so proposals
 //             are decided in proposal order
@@ -96,19 +97,6 @@ __device__ __forceinline__ Quad quad_of(const TopoW& t, int e) {
   return q;
 }
 
-template <class F>
-__device__ __forceinline__ void for_patch(const TopoW& t, const Quad& q, F&& fn) {
-  int vs[4] = {q.va0, q.va1, q.vb0, q.vb1};
-  for (int k = 0; k < 4; ++k) {
-    int v = vs[k];
-    int d = t.val[v];
-    for (int m = 0; m < d; ++m) {
-      int4 s = t.slot[(size_t)m * t.nv + v];
-      fn(s.z);
-      fn(s.w);
-    }
-  }
-}
 
 __device__ bool flip_ok(const TopoW& t, int e) {
   if (t.face[2 * e] < 0 || t.face[2 * e + 1] < 0) return false;
@@ -312,29 +300,48 @@ __global__ void k_fill(int W, long long next_new, const long long* pend, const F
   win[s] = s < np ? pend[s] : next_new + (s - np);
 }
 
-__global__ void k_claim(TopoW t, int W, unsigned long long seed, const long long* win, int* owner) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= W) return;
-  Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
-  for_patch(t, q, [&](int x) { atomicMin(&owner[x], s); });
+// Patch ownership without a release pass: owner[x] holds the largest tag
+// (window << 12) | (4095 - slot) claimed so far in this sweep, so within a
+// window the lowest slot wins and tags of earlier windows lose.  Four
+// threads per slot, one per quad vertex of the patch.
+__device__ __forceinline__ int owner_tag(int wid, int s) { return (wid << 12) | (4095 - s); }
+__device__ __forceinline__ int quad_vertex(const Quad& q, int k) {
+  return k == 0 ? q.va0 : (k == 1 ? q.va1 : (k == 2 ? q.vb0 : q.vb1));
+}
+template <class F>
+__device__ __forceinline__ void for_ring_edges(const TopoW& t, int v, F&& fn) {
+  int d = t.val[v];
+  for (int m = 0; m < d; ++m) {
+    int4 s = t.slot[(size_t)m * t.nv + v];
+    fn(s.z);
+    fn(s.w);
+  }
 }
 
-__global__ void k_winner(TopoW t, int W, int mode, unsigned long long seed, const long long* win, const int* owner,
-                         unsigned char* winner, int* limit) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_claim(TopoW t, int W, int wid, unsigned long long seed, const long long* win, int* owner) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = g >> 2, k = g & 3;
   if (s >= W) return;
   Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
+  const int tag = owner_tag(wid, s);
+  for_ring_edges(t, quad_vertex(q, k), [&](int x) { atomicMax(&owner[x], tag); });
+}
+
+__global__ void k_winner(TopoW t, int W, int wid, int mode, unsigned long long seed, const long long* win,
+                         const int* owner, unsigned char* winner, int* limit) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = g >> 2, k = g & 3;
+  if (s >= W) return;
+  Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
+  const int tag = owner_tag(wid, s);
   bool ok = true;
-  for_patch(t, q, [&](int x) { ok = ok && (owner[x] == s); });
-  winner[s] = ok ? 1 : 0;
-  if (!ok && mode == 0) atomicMin(limit, s);
-}
-
-__global__ void k_release(TopoW t, int W, unsigned long long seed, const long long* win, int* owner) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= W) return;
-  Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
-  for_patch(t, q, [&](int x) { owner[x] = INT_MAX; });
+  for_ring_edges(t, quad_vertex(q, k), [&](int x) { ok = ok && (owner[x] == tag); });
+  const unsigned gmask = 0xfu << (threadIdx.x & 28);  // the four threads of this slot
+  ok = __all_sync(gmask, ok);
+  if (k == 0) {
+    winner[s] = ok ? 1 : 0;
+    if (!ok && mode == 0) atomicMin(limit, s);
+  }
 }
 
 // 8 threads per slot: (quad vertex 0..3) x (before, after)
@@ -394,7 +401,7 @@ __global__ void k_prep(int W, unsigned long long seed, const long long* win, con
 // first accepted one, updates the state and repeats from the next slot: the
 // same decisions as a walk in slot order.  Then the deferred proposals are
 // compacted in order for the next window.
-constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread (contiguous)
+constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread
 __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const unsigned char* winner,
                                              const double* dpn, FlipE fe, FlipState* st, const int* limit,
                                              unsigned char* accepted, long long* pend) {
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const
     __syncthreads();
     const int start = sstart;
     for (int k = 0; k < MS; ++k) {
-      int s = tid * MS + k;
+      int s = k * MB + tid;  // strided: every thread has a slot in small windows
       if (s < start || s >= W) continue;
       const double* o8 = dpn + 8 * (size_t)s;
       if (o8[7] == 0.0) continue;
@@ -433,7 +440,7 @@ __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const
     __syncthreads();
     const int first = sfirst;
     if (first == INT_MAX) break;
-    if (tid == first / MS) {
+    if (tid == first % MB) {
       const double* o8 = dpn + 8 * (size_t)first;
       double trial[6];
       for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
@@ -514,7 +521,7 @@ __global__ void k_set_int(int* p, int v) {
 
 __global__ void k_owner_init(int* owner, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) owner[i] = INT_MAX;
+  if (i < n) owner[i] = 0;  // below every window's tags
 }
 
 inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
@@ -561,16 +568,18 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   hs.npend = 0;
   long long next_new = 0;
   int B = batch;
+  int wid = 0;  // window number of the ownership tags
   while (hs.npend > 0 || next_new < nflips) {
     int W = (int)std::min<long long>(B, hs.npend + (nflips - next_new));
     k_fill<<<nblk(W, 256), 256, 0, s>>>(W, next_new, pend.get(), st.get(), win.get(), limit.get());
     TM_LAUNCH();
     next_new += W - hs.npend;
-    k_claim<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), owner.get());
+    ++wid;
+    if (wid >= (1 << 19)) fail(TM_ERR_ARG, "too many windows in one sweep");
+    k_claim<<<nblk(4L * W, 64), 64, 0, s>>>(t, W, wid, seed, win.get(), owner.get());
     TM_LAUNCH();
-    k_winner<<<nblk(W, 128), 128, 0, s>>>(t, W, mode, seed, win.get(), owner.get(), winner.get(), limit.get());
-    TM_LAUNCH();
-    k_release<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), owner.get());
+    k_winner<<<nblk(4L * W, 64), 64, 0, s>>>(t, W, wid, mode, seed, win.get(), owner.get(), winner.get(),
+                                           limit.get());
     TM_LAUNCH();
     k_delta<<<nblk(8L * W, 64), 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv,
                                           part.get(), okf.get());
