@@ -196,72 +196,6 @@ struct TableExclW {
   }
 };
 
-// vertex_properties (src/mesh_properties.cpp:12-49) over an explicit ring
-template <class X>
-__device__ void vprops_ring(const Ring& R, int v, const double* P, const EP& ep, const NLView& nl, const X& excl,
-                            double* out) {
-  d3 xv = ld3(P, v);
-  double A = 0, V = 0, C = 0, T = 0;
-  int n = R.n;
-  for (int m = 0; m < n; ++m) {
-    if (!R.f[m]) continue;
-    int j = R.r[m], k = R.r[m == 0 ? n - 1 : m - 1];
-    int mn = m + 1 == n ? 0 : m + 1;
-    d3 xj = ld3(P, j), xk = ld3(P, k);
-    d3 ev = xj - xv;
-    double el = norm(ev);
-    d3 N0 = cross(ev, xk - xv);
-    double fa = norm(N0) / 2;
-    double th = 0.0;
-    if (R.f[mn]) {
-      d3 xn = ld3(P, R.r[mn]);
-      d3 N1 = cross(xn - xv, ev);
-      double den = norm(N0) * norm(N1);
-      if (den != 0.0) {
-        double c = fmin(1.0, fmax(-1.0, dot(N0, N1) / den));
-        double a = acos(c);
-        th = dot(cross(N0, N1), ev) >= 0.0 ? a : -a;
-      }
-    }
-    C += 0.5 * el * th;
-    A += fa;
-    V += dot(cross(xj, xk), xv) / 6;
-    if (ep.btype == 0) {
-      int r = ep.r;
-      if (el > ep.lc0)
-        T += ipow((double)r, r + 1) * ipow(el - ep.lc0, r);
-      else if (el < ep.lc1)
-        T += exp(el / (el - ep.lc1)) / ipow(el, r);
-    } else {
-      double q = fa / ep.a0 - 1.0;
-      T += q * q;
-    }
-  }
-  A /= 3;
-  V /= 3;
-  C /= 2;
-  T /= ep.tdiv;
-  out[0] = A;
-  out[1] = V;
-  out[2] = C;
-  out[3] = 2 * C * C / A;
-  out[4] = T;
-  double pot = 0.0;
-  const double lc1 = ep.rlc1;
-  const int rr = ep.rr;
-  auto add = [&](int, double l, d3) { pot += exp(l / (l - lc1)) / ipow(l, rr); };
-  // the near rows when usable (exclusion tested with this ring's rules),
-  // else the candidate row / cell walk; both visit in the reference's order
-  bool done = false;
-  if (nl.kind == 0 && nl.nent && nl.nflag[0] == 0 && nl.nflag[1] == 0) {
-    PairTest pt = make_pair_test(nl, v, lc1, ep.rT);
-    int co[3];
-    in_build_cell(nl, v, xv, co);
-    done = visit_near(pt, nl, P, v, xv, 2, co, excl, add);
-  }
-  if (!done) for_each_neighbour_x(nl, P, v, xv, lc1, ep.rT, excl, add);
-  out[5] = pot;
-}
 
 // ---- window kernels --------------------------------------------------------
 // Energy of a property set for the Metropolis test: the penalty energy of
@@ -344,33 +278,135 @@ __global__ void k_winner(TopoW t, int W, int wid, int mode, unsigned long long s
   }
 }
 
-// 8 threads per slot: (quad vertex 0..3) x (before, after)
-__global__ void k_delta(TopoW t, int W, unsigned long long seed, const long long* win, const unsigned char* winner,
-                        const int* limit, const double* P, EP ep, NLView nl, double* part, unsigned char* okf) {
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  int s = tid >> 3, sub = tid & 7;
+// repulsion value of vertex v at xv (mesh_repulsion.h:28-79): the near rows
+// when usable (exclusion tested with the given rules), else the candidate
+// row / cell walk; both visit in the reference's order
+template <class X>
+__device__ double repulsion_of(int v, d3 xv, const double* P, const EP& ep, const NLView& nl, const X& excl) {
+  double pot = 0.0;
+  const double lc1 = ep.rlc1;
+  const int rr = ep.rr;
+  auto add = [&](int, double l, d3) { pot += exp(l / (l - lc1)) / ipow(l, rr); };
+  bool done = false;
+  if (nl.kind == 0 && nl.nent && nl.nflag[0] == 0 && nl.nflag[1] == 0) {
+    PairTest pt = make_pair_test(nl, v, lc1, ep.rT);
+    int co[3];
+    in_build_cell(nl, v, xv, co);
+    done = visit_near(pt, nl, P, v, xv, 2, co, excl, add);
+  }
+  if (!done) for_each_neighbour_x(nl, P, v, xv, lc1, ep.rT, excl, add);
+  return pot;
+}
+
+// One block of 64 threads per slot: 8 variants (quad vertex sub & 3, before
+// the flip for sub < 4, after it otherwise) x 8 workers.  The ring of each
+// variant goes to shared memory, the workers compute the per-position terms
+// of vertex_properties (src/mesh_properties.cpp:12-49) in parallel, and one
+// worker sums them in ring order while
+// another computes the repulsion.
+__global__ void __launch_bounds__(64) k_delta(TopoW t, int W, unsigned long long seed, const long long* win,
+                                              const unsigned char* winner, const int* limit, const double* P,
+                                              EP ep, NLView nl, double* part, unsigned char* okf) {
+  __shared__ int sr[8][TM_MAXVAL + 1];
+  __shared__ unsigned char sf[8][TM_MAXVAL + 1];
+  __shared__ int sn[8];
+  __shared__ double term[8][TM_MAXVAL + 1][4];
+  const int s = blockIdx.x;
+  const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
   if (s >= W) return;
-  double* o = part + 8 * 8 * (size_t)s + 8 * sub;
   if (s >= *limit || !winner[s]) {
-    if (sub == 0) okf[s] = 0;
+    if (threadIdx.x == 0) okf[s] = 0;
     return;
   }
-  int e = flip_edge_of(seed, win[s], t.ne);
-  bool ok = flip_ok(t, e);
-  if (sub == 0) okf[s] = ok ? 1 : 0;
+  const int e = flip_edge_of(seed, win[s], t.ne);
+  const bool ok = flip_ok(t, e);
+  if (threadIdx.x == 0) okf[s] = ok ? 1 : 0;
   if (!ok) return;
-  Quad q = quad_of(t, e);
-  int vs[4] = {q.va0, q.va1, q.vb0, q.vb1};
-  int v = vs[sub & 3];
-  Ring R;
-  if (sub < 4) {
-    load_ring(t, v, R);
-    TableExclW x{t, nl.excl};
-    vprops_ring(R, v, P, ep, nl, x, o);
-  } else {
-    ring_after(t, q, v, R);
-    OverlayExcl x{t, q, nl.excl};
-    vprops_ring(R, v, P, ep, nl, x, o);
+  const Quad q = quad_of(t, e);
+  const int v = quad_vertex(q, sub & 3);
+  if (w8 == 0) {
+    Ring R;
+    if (sub < 4)
+      load_ring(t, v, R);
+    else
+      ring_after(t, q, v, R);
+    sn[sub] = R.n;
+    for (int m = 0; m < R.n; ++m) {
+      sr[sub][m] = R.r[m];
+      sf[sub][m] = R.f[m] ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  const int n = sn[sub];
+  const d3 xv = ld3(P, v);
+  for (int m = w8; m < n; m += 8) {
+    double tc = 0.0, ta = 0.0, tv = 0.0, tt = 0.0;
+    if (sf[sub][m]) {
+      int j = sr[sub][m], k = sr[sub][m == 0 ? n - 1 : m - 1];
+      int mn = m + 1 == n ? 0 : m + 1;
+      d3 xj = ld3(P, j), xk = ld3(P, k);
+      d3 ev = xj - xv;
+      double el = norm(ev);
+      d3 N0 = cross(ev, xk - xv);
+      double fa = norm(N0) / 2;
+      double th = 0.0;
+      if (sf[sub][mn]) {
+        d3 xn = ld3(P, sr[sub][mn]);
+        d3 N1 = cross(xn - xv, ev);
+        double den = norm(N0) * norm(N1);
+        if (den != 0.0) {
+          double c = fmin(1.0, fmax(-1.0, dot(N0, N1) / den));
+          double a = acos(c);
+          th = dot(cross(N0, N1), ev) >= 0.0 ? a : -a;
+        }
+      }
+      tc = 0.5 * el * th;
+      ta = fa;
+      tv = dot(cross(xj, xk), xv) / 6;
+      if (ep.btype == 0) {
+        int r = ep.r;
+        if (el > ep.lc0)
+          tt = ipow((double)r, r + 1) * ipow(el - ep.lc0, r);
+        else if (el < ep.lc1)
+          tt = exp(el / (el - ep.lc1)) / ipow(el, r);
+      } else {
+        double qa = fa / ep.a0 - 1.0;
+        tt = qa * qa;
+      }
+    }
+    term[sub][m][0] = tc;
+    term[sub][m][1] = ta;
+    term[sub][m][2] = tv;
+    term[sub][m][3] = tt;
+  }
+  __syncthreads();
+  double* o = part + 8 * 8 * (size_t)s + 8 * sub;
+  if (w8 == 0) {
+    double A = 0, V = 0, C = 0, T = 0;
+    for (int m = 0; m < n; ++m) {
+      if (!sf[sub][m]) continue;
+      C += term[sub][m][0];
+      A += term[sub][m][1];
+      V += term[sub][m][2];
+      T += term[sub][m][3];
+    }
+    A /= 3;
+    V /= 3;
+    C /= 2;
+    T /= ep.tdiv;
+    o[0] = A;
+    o[1] = V;
+    o[2] = C;
+    o[3] = 2 * C * C / A;
+    o[4] = T;
+  } else if (w8 == 1) {
+    if (sub < 4) {
+      TableExclW x{t, nl.excl};
+      o[5] = repulsion_of(v, xv, P, ep, nl, x);
+    } else {
+      OverlayExcl x{t, q, nl.excl};
+      o[5] = repulsion_of(v, xv, P, ep, nl, x);
+    }
   }
 }
 
@@ -581,8 +617,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     k_winner<<<nblk(4L * W, 64), 64, 0, s>>>(t, W, wid, mode, seed, win.get(), owner.get(), winner.get(),
                                            limit.get());
     TM_LAUNCH();
-    k_delta<<<nblk(8L * W, 64), 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv,
-                                          part.get(), okf.get());
+    k_delta<<<W, 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get());
     TM_LAUNCH();
     k_prep<<<nblk(W, 128), 128, 0, s>>>(W, seed, win.get(), winner.get(), okf.get(), part.get(), limit.get(),
                                         dpn.get());
