@@ -399,7 +399,29 @@ void tm_energy::ensure(int nv_, int ne_, int nf_) {
   TM_CUDA(cudaMemsetAsync(glob.get(), 0, sizeof(tmg::Globals), stream));
 }
 
+void tm_energy::to_host(double* dst, const double* src, size_t n) {
+  cudaPointerAttributes a{};
+  bool pinned = cudaPointerGetAttributes(&a, dst) == cudaSuccess && a.type == cudaMemoryTypeHost;
+  cudaGetLastError();  // a pageable pointer may leave an error code behind
+  if (pinned || n == 0) {
+    TM_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+    TM_CUDA(cudaStreamSynchronize(stream));
+    return;
+  }
+  if (h_stage_n < n) {
+    if (h_stage) cudaFreeHost(h_stage);
+    h_stage = nullptr;
+    h_stage_n = 0;
+    TM_CUDA(cudaMallocHost(&h_stage, sizeof(double) * n));
+    h_stage_n = n;
+  }
+  TM_CUDA(cudaMemcpyAsync(h_stage, src, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+  TM_CUDA(cudaStreamSynchronize(stream));
+  std::memcpy(dst, h_stage, sizeof(double) * n);
+}
+
 tm_energy::~tm_energy() {
+  if (h_stage) cudaFreeHost(h_stage);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -517,10 +539,9 @@ int tm_energy_gradient(tm_energy* e, tm_mesh* m, double* grad, double* energy) {
   TM_API_BEGIN
   if (!grad) fail(TM_ERR_ARG, "NULL output");
   eval_host(e, m, true, false);
-  TM_CUDA(cudaMemcpyAsync(grad, e->grad.get(), sizeof(double) * 3 * m->nv, cudaMemcpyDeviceToHost, e->stream));
   if (energy)
     TM_CUDA(cudaMemcpyAsync(energy, &e->glob.get()->comps[6], sizeof(double), cudaMemcpyDeviceToHost, e->stream));
-  TM_CUDA(cudaStreamSynchronize(e->stream));
+  e->to_host(grad, e->grad.get(), 3 * (size_t)m->nv);
   TM_API_END
 }
 

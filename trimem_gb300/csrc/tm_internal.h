@@ -209,7 +209,12 @@ struct tm_energy {
   tmg::DevBuf<float> pos32, poslo;
   tmg::DevBuf<tmg::Globals> glob;
   cudaStream_t stream = nullptr;
+  double* h_stage = nullptr;  // page-locked staging for results copied to pageable host memory
+  size_t h_stage_n = 0;
   void ensure(int nv_, int ne_, int nf_);
+  // copies n doubles from device memory to host memory dst (via the
+  // page-locked staging buffer when dst is pageable) and synchronises
+  void to_host(double* dst, const double* src, size_t n);
   ~tm_energy();
 };
 
