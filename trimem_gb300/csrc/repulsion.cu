@@ -173,7 +173,7 @@ void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos3
     k_rep_fast<false><<<nblk(nv, 256), 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps, use_near);
   TM_LAUNCH();
   if (nlv.kind == 0) {
-    int grid = 2 * 152;  // 8 warps per block, each walks the queue one vertex at a time
+    int grid = 8 * 152;  // 8 warps per block, one warp per queued vertex (all of them when the near rows are stale)
     if (want_grad)
       k_rep_slow<true><<<grid, 256, 0, s>>>(t, P, nlv, ep, pot, repg, slow, nslow, eps);
     else
