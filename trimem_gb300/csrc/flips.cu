@@ -13,18 +13,18 @@
 //   k_winner  a proposal whose patch it owns entirely is a winner; in
 //             serial mode the window is cut at the first loser, so proposals
 //             are decided in proposal order
-//   k_delta   8 threads per winner evaluate the vertex properties of the
+//   k_delta   one block per winner evaluates the vertex properties of the
 //             four quad vertices before and after a virtual flip (the mesh is
 //             not touched), including the repulsion with the post-flip
-//             exclusion rings
-//   k_prep    per slot the property change of the flip and -log(u)
+//             exclusion rings, and reduces them to the property change of
+//             the flip and -log(u)
 //   k_metro   Metropolis with T = 1 in slot order (flips.cpp:142-160): one
 //             block tries all remaining slots on the current state, takes
 //             the first accepted one and repeats from there; losers are
 //             queued for the next window
 //   k_commit  accepted flips rewrite their six halfedges, two faces, five
-//             edge rows and four ring rows; patches are disjoint, so commits
-//             never touch the same entries
+//             edge rows and four ring rows (one block per flip); patches are
+//             disjoint, so commits never touch the same entries
 // Proposals come from a counter-based SplitMix64 stream of (seed, index), so
 // a sweep is reproducible and matches the CPU port of this algorithm.
 // A flip is also refused when it would raise a valence above TM_MAXVAL.
@@ -306,7 +306,7 @@ __device__ double repulsion_of(int v, d3 xv, const double* P, const EP& ep, cons
 // another computes the repulsion.
 __global__ void __launch_bounds__(64) k_delta(TopoW t, int W, unsigned long long seed, const long long* win,
                                               const unsigned char* winner, const int* limit, const double* P,
-                                              EP ep, NLView nl, double* part, unsigned char* okf) {
+                                              EP ep, NLView nl, double* part, unsigned char* okf, double* dpn) {
   __shared__ int sr[8][TM_MAXVAL + 1];
   __shared__ unsigned char sf[8][TM_MAXVAL + 1];
   __shared__ int sn[8];
@@ -315,12 +315,18 @@ __global__ void __launch_bounds__(64) k_delta(TopoW t, int W, unsigned long long
   const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
   if (s >= W) return;
   if (s >= *limit || !winner[s]) {
-    if (threadIdx.x == 0) okf[s] = 0;
+    if (threadIdx.x == 0) {
+      okf[s] = 0;
+      dpn[8 * (size_t)s + 7] = 0.0;
+    }
     return;
   }
   const int e = flip_edge_of(seed, win[s], t.ne);
   const bool ok = flip_ok(t, e);
-  if (threadIdx.x == 0) okf[s] = ok ? 1 : 0;
+  if (threadIdx.x == 0) {
+    okf[s] = ok ? 1 : 0;
+    if (!ok) dpn[8 * (size_t)s + 7] = 0.0;
+  }
   if (!ok) return;
   const Quad q = quad_of(t, e);
   const int v = quad_vertex(q, sub & 3);
@@ -408,26 +414,21 @@ __global__ void __launch_bounds__(64) k_delta(TopoW t, int W, unsigned long long
       o[5] = repulsion_of(v, xv, P, ep, nl, x);
     }
   }
-}
-
-// per slot: the property change of the flip (before - after, in the
-// summation orders of edge_vertex_properties before (va0, va1, vb0, vb1)
-// and after the flip (va1, vb0, vb1, va0)), -log(u) and eligibility
-__global__ void k_prep(int W, unsigned long long seed, const long long* win, const unsigned char* winner,
-                       const unsigned char* okf, const double* part, const int* limit, double* dpn) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= W) return;
-  double* o8 = dpn + 8 * (size_t)s;
-  bool elig = s < *limit && winner[s] && okf[s];
-  o8[7] = elig ? 1.0 : 0.0;
-  if (!elig) return;
-  const double* o = part + 64 * (size_t)s;
-  for (int k = 0; k < 6; ++k) {
-    double before = ((o[k] + o[8 + k]) + o[16 + k]) + o[24 + k];
-    double after = ((o[40 + k] + o[48 + k]) + o[56 + k]) + o[32 + k];
-    o8[k] = before - after;
+  __syncthreads();
+  // the property change of the flip (before - after, in the summation orders
+  // of edge_vertex_properties before (va0, va1, vb0, vb1) and after the flip
+  // (va1, vb0, vb1, va0)), -log(u) and the eligibility flag
+  if (threadIdx.x == 0) {
+    const double* op = part + 64 * (size_t)s;
+    double* o8 = dpn + 8 * (size_t)s;
+    for (int k = 0; k < 6; ++k) {
+      double before = ((op[k] + op[8 + k]) + op[16 + k]) + op[24 + k];
+      double after = ((op[40 + k] + op[48 + k]) + op[56 + k]) + op[32 + k];
+      o8[k] = before - after;
+    }
+    o8[6] = -log(flip_u_of(seed, win[s]));
+    o8[7] = 1.0;
   }
-  o8[6] = -log(flip_u_of(seed, win[s]));
 }
 
 // Metropolis with T = 1 in slot order (flips.cpp:142-160): slot s is tried on
@@ -517,38 +518,49 @@ __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const
   }
 }
 
-__global__ void k_commit(TopoW t, int W, unsigned long long seed, const long long* win, const unsigned char* accepted,
-                         FlipState* st) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+// one block of 32 threads per slot (accepted slots only do work): the
+// half-edge rewiring, then the two face rows and five edge rows, then the
+// four ring rows, each stage in parallel
+__global__ void __launch_bounds__(32) k_commit(TopoW t, int W, unsigned long long seed, const long long* win,
+                                               const unsigned char* accepted, FlipState* st) {
+  const int s = blockIdx.x;
   if (s >= W || !accepted[s]) return;
-  int e = flip_edge_of(seed, win[s], t.ne);
-  int a0 = 2 * e, b0 = 2 * e + 1;
-  int a1 = t.next[a0], a2 = t.next[a1], b1 = t.next[b0], b2 = t.next[b1];
-  int va0 = t.to[a0], va1 = t.to[a1], vb0 = t.to[b0], vb1 = t.to[b1];
-  int fa = t.face[a0], fb = t.face[b0];
-  t.to[a0] = va1;
-  t.to[b0] = vb1;
-  t.next[a0] = a2;
-  t.next[a2] = b1;
-  t.next[b1] = a0;
-  t.next[b0] = b2;
-  t.next[b2] = a1;
-  t.next[a1] = b0;
-  t.face[a1] = fb;
-  t.face[b1] = fa;
-  t.fhe[fa] = a0;
-  t.fhe[fb] = b0;
-  if (t.vout[va0] == b0) t.vout[va0] = a1;
-  if (t.vout[vb0] == a0) t.vout[vb0] = b1;
-  face_row(t, fa);
-  face_row(t, fb);
-  edge_row(t, e);
-  edge_row(t, a1 >> 1);
-  edge_row(t, a2 >> 1);
-  edge_row(t, b1 >> 1);
-  edge_row(t, b2 >> 1);
-  bool ok = ring_row(t, va0) & ring_row(t, va1) & ring_row(t, vb0) & ring_row(t, vb1);
-  if (!ok) atomicExch(&st->status, TM_ERR_TOPOLOGY);
+  const int tid = threadIdx.x;
+  const int e = flip_edge_of(seed, win[s], t.ne);
+  const int a0 = 2 * e, b0 = 2 * e + 1;
+  const int a1 = t.next[a0], a2 = t.next[a1], b1 = t.next[b0], b2 = t.next[b1];
+  const int va0 = t.to[a0], va1 = t.to[a1], vb0 = t.to[b0], vb1 = t.to[b1];
+  const int fa = t.face[a0], fb = t.face[b0];
+  __syncthreads();  // every thread has read the old wiring
+  if (tid == 0) {
+    t.to[a0] = va1;
+    t.to[b0] = vb1;
+    t.next[a0] = a2;
+    t.next[a2] = b1;
+    t.next[b1] = a0;
+    t.next[b0] = b2;
+    t.next[b2] = a1;
+    t.next[a1] = b0;
+    t.face[a1] = fb;
+    t.face[b1] = fa;
+    t.fhe[fa] = a0;
+    t.fhe[fb] = b0;
+    if (t.vout[va0] == b0) t.vout[va0] = a1;
+    if (t.vout[vb0] == a0) t.vout[vb0] = b1;
+  }
+  __syncthreads();
+  if (tid == 0) face_row(t, fa);
+  if (tid == 1) face_row(t, fb);
+  if (tid == 2) edge_row(t, e);
+  if (tid == 3) edge_row(t, a1 >> 1);
+  if (tid == 4) edge_row(t, a2 >> 1);
+  if (tid == 5) edge_row(t, b1 >> 1);
+  if (tid == 6) edge_row(t, b2 >> 1);
+  __syncthreads();
+  if (tid < 4) {
+    const int v = tid == 0 ? va0 : (tid == 1 ? va1 : (tid == 2 ? vb0 : vb1));
+    if (!ring_row(t, v)) atomicExch(&st->status, TM_ERR_TOPOLOGY);
+  }
 }
 
 __global__ void k_set_int(int* p, int v) {
@@ -617,15 +629,13 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     k_winner<<<nblk(4L * W, 64), 64, 0, s>>>(t, W, wid, mode, seed, win.get(), owner.get(), winner.get(),
                                            limit.get());
     TM_LAUNCH();
-    k_delta<<<W, 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get());
-    TM_LAUNCH();
-    k_prep<<<nblk(W, 128), 128, 0, s>>>(W, seed, win.get(), winner.get(), okf.get(), part.get(), limit.get(),
-                                        dpn.get());
+    k_delta<<<W, 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get(),
+                             dpn.get());
     TM_LAUNCH();
     k_metro<<<1, MB, 0, s>>>(W, win.get(), winner.get(), dpn.get(), fe, st.get(), limit.get(), acc.get(),
                              pend.get());
     TM_LAUNCH();
-    k_commit<<<nblk(W, 128), 128, 0, s>>>(t, W, seed, win.get(), acc.get(), st.get());
+    k_commit<<<W, 32, 0, s>>>(t, W, seed, win.get(), acc.get(), st.get());
     TM_LAUNCH();
     TM_CUDA(cudaMemcpyAsync(&hs, st.get(), sizeof(FlipState), cudaMemcpyDeviceToHost, s));
     TM_CUDA(cudaStreamSynchronize(s));
