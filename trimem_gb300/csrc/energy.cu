@@ -343,6 +343,10 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
   k_face<<<nfb, 256, 0, s>>>(t, P, fd, e->pos32.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
+  // the repulsion pass needs only the positions: it overlaps the edge kernels
+  // (in sequence when the stages are timed)
+  const bool conc = ev == nullptr;
+  if (conc) fork_repulsion(e, m, P, want_grad, s, true);
   int* blist = e->slow.get() + std::max(m->nv, 1) + 1;
   int* bcnt = blist + std::max(m->ne, 1);
   TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
@@ -351,8 +355,10 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
   if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(P, t, ed, e->ebond.get(), ep, blist, bcnt);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
-  repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
-                 e->slow.get() + std::max(m->nv, 1), s);
+  if (conc)
+    join_repulsion(e, s, true);
+  else
+    fork_repulsion(e, m, P, want_grad, s, false);
   int nb = std::max(1, nblk(t.nv, VB));
   if (want_vprops)
     k_vertex<true><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, e->rho.get(),
@@ -422,6 +428,9 @@ void tm_energy::to_host(double* dst, const double* src, size_t n) {
 
 tm_energy::~tm_energy() {
   if (h_stage) cudaFreeHost(h_stage);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (aux) cudaStreamDestroy(aux);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -455,6 +464,9 @@ int tm_energy_create(tm_mesh* m, const tm_params* p, tm_energy** out) {
   std::unique_ptr<tm_energy> e(new tm_energy());
   e->prm = *p;
   TM_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  TM_CUDA(cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking));
+  TM_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+  TM_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
   m->upload_points(e->stream);
   tmg::nlist_make(&e->nl, m, e->prm, m->d_pts.get(), e->stream);
   // initial properties: the reference properties are still unset (zero) and

@@ -456,14 +456,19 @@ void energy_eval32(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bo
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
   if (m->nv) k_split<<<nblk(3L * m->nv, 256), 256, 0, s>>>(m->nv, P, e->pos32.get(), lo);
   TM_LAUNCH();
+  const bool conc = ev == nullptr;  // repulsion overlaps the face and edge kernels
+  if (conc) fork_repulsion(e, m, P, want_grad, s, true);
   if (t.nf) k_face32<<<nblk(t.nf, 256), 256, 0, s>>>(t, S, fd);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
   if (t.ne) k_edge32<<<nblk(t.ne, 256), 256, 0, s>>>(t, S, fd, ed, eb, ep);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
-  repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), repg, e->slow.get(),
-                 e->slow.get() + std::max(m->nv, 1), s);
+  if (conc)
+    join_repulsion(e, s, true);
+  else
+    fork_repulsion(e, m, P, want_grad, s, false);
+  (void)repg;
   int nb = std::max(1, nblk(t.nv, VB));
   (void)want_vprops;
   k_vertex32<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), ep, rho, e->partials.get(), e->glob.get());

@@ -382,6 +382,8 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
   if (m->nv) k_split_df<<<nblk(3L * m->nv, 256), 256, 0, s>>>(3 * m->nv, P, e->pos32.get(), e->poslo.get());
   TM_LAUNCH();
+  const bool conc = ev == nullptr;  // repulsion overlaps the face and edge kernels
+  if (conc) fork_repulsion(e, m, P, want_grad, s, true);
   if (t.nf) k_face_df<<<nblk(t.nf, 256), 256, 0, s>>>(t, X, fd);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
@@ -393,8 +395,10 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   if (t.ne) k_bond_short_df<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(ed, eb, ep, epd, blist, bcnt);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
-  repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
-                 e->slow.get() + std::max(m->nv, 1), s);
+  if (conc)
+    join_repulsion(e, s, true);
+  else
+    fork_repulsion(e, m, P, want_grad, s, false);
   int nb = std::max(1, nblk(t.nv, VB));
   k_vertex_df<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), ep, epd, rho, e->partials.get(), e->glob.get());
   TM_LAUNCH();

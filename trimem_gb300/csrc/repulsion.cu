@@ -182,4 +182,22 @@ void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos3
   }
 }
 
+void fork_repulsion(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, cudaStream_t s, bool concurrent) {
+  const int n1 = std::max(m->nv, 1);
+  if (!concurrent || !e->aux) {
+    repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
+                   e->slow.get() + n1, s);
+    return;
+  }
+  TM_CUDA(cudaEventRecord(e->ev_fork, s));
+  TM_CUDA(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
+  repulsion_eval(e, m, P, e->pos32.get(), want_grad, e->reppot.get(), e->repg.get(), e->slow.get(),
+                 e->slow.get() + n1, e->aux);
+  TM_CUDA(cudaEventRecord(e->ev_join, e->aux));
+}
+
+void join_repulsion(tm_energy* e, cudaStream_t s, bool concurrent) {
+  if (concurrent && e->aux) TM_CUDA(cudaStreamWaitEvent(s, e->ev_join, 0));
+}
+
 }  // namespace tmg

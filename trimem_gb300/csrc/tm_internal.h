@@ -209,6 +209,10 @@ struct tm_energy {
   tmg::DevBuf<float> pos32, poslo;
   tmg::DevBuf<tmg::Globals> glob;
   cudaStream_t stream = nullptr;
+  // second stream: the repulsion pass runs there, concurrent with the
+  // edge kernels, between a fork and a join event
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   double* h_stage = nullptr;  // page-locked staging for results copied to pageable host memory
   size_t h_stage_n = 0;
   void ensure(int nv_, int ne_, int nf_);
@@ -229,6 +233,11 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* d_points, bool w
 // repg; slow must hold nv + 1 ints
 void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos32, bool want_grad, double* pot,
                     double* repg, int* slow, int* nslow, cudaStream_t s, const EP* eps = nullptr);
+// the repulsion pass of an evaluation into e->reppot / e->repg, started on
+// e->aux after the work already queued on s (concurrent = false: on s);
+// join_repulsion makes s wait for it
+void fork_repulsion(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, cudaStream_t s, bool concurrent);
+void join_repulsion(tm_energy* e, cudaStream_t s, bool concurrent);
 // learned surrogate gradient (surrogate.cu)
 void surrogate_grad(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
                     cudaStream_t s);
