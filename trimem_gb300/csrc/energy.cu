@@ -406,28 +406,14 @@ void tm_energy::ensure(int nv_, int ne_, int nf_) {
 }
 
 void tm_energy::to_host(double* dst, const double* src, size_t n) {
-  cudaPointerAttributes a{};
-  bool pinned = cudaPointerGetAttributes(&a, dst) == cudaSuccess && a.type == cudaMemoryTypeHost;
-  cudaGetLastError();  // a pageable pointer may leave an error code behind
-  if (pinned || n == 0) {
-    TM_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
-    TM_CUDA(cudaStreamSynchronize(stream));
-    return;
-  }
-  if (h_stage_n < n) {
-    if (h_stage) cudaFreeHost(h_stage);
-    h_stage = nullptr;
-    h_stage_n = 0;
-    TM_CUDA(cudaMallocHost(&h_stage, sizeof(double) * n));
-    h_stage_n = n;
-  }
-  TM_CUDA(cudaMemcpyAsync(h_stage, src, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
+  // direct copy: for pageable destinations the driver's own staged copy beat
+  // a page-locked staging buffer plus memcpy (the destination is a fresh
+  // array whose pages are touched for the first time either way)
+  if (n) TM_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost, stream));
   TM_CUDA(cudaStreamSynchronize(stream));
-  std::memcpy(dst, h_stage, sizeof(double) * n);
 }
 
 tm_energy::~tm_energy() {
-  if (h_stage) cudaFreeHost(h_stage);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
   if (aux) cudaStreamDestroy(aux);

@@ -213,11 +213,8 @@ struct tm_energy {
   // edge kernels, between a fork and a join event
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  double* h_stage = nullptr;  // page-locked staging for results copied to pageable host memory
-  size_t h_stage_n = 0;
   void ensure(int nv_, int ne_, int nf_);
-  // copies n doubles from device memory to host memory dst (via the
-  // page-locked staging buffer when dst is pageable) and synchronises
+  // copies n doubles from device memory to host memory dst and synchronises
   void to_host(double* dst, const double* src, size_t n);
   ~tm_energy();
 };
