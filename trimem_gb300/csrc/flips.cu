@@ -4,7 +4,8 @@
 // (flip_serial) or lets OpenMP threads lock the edge patches of their
 // proposals and serialises the acceptance in a critical section
 // (flip_parallel_batches).  Here a sweep is a sequence of windows of
-// proposals, every step on the device:
+// proposals, every step on the device (windows are queued eight at a time;
+// their size lives in device memory, so no window waits for the host):
 //   k_fill    window = deferred proposals (in order) + new proposals
 //   k_claim   each proposal claims the edges of its patch (the 1-ring edges
 //             of the quad's four vertices and the edges opposite them,
@@ -75,13 +76,21 @@ __device__ __forceinline__ double flip_u_of(unsigned long long seed, long long p
   return (double)(flip_key(seed, p, 1) >> 11) * 0x1.0p-53;
 }
 
+// Sweep state in device memory.  A window's size W and number wid are set
+// by k_fill from the state the previous window left, so windows follow each
+// other without the host; W = 0 once every proposal is decided.
 struct FlipState {
   double props[8];
   double e0;
+  long long next_new;  // first proposal not yet in a window
+  long long nn_next;   // next_new after the current window (committed by k_metro)
+  long long nflips;
   int acc;
   int limit;
   int npend;
   int status;
+  int W;
+  int wid;
 };
 
 struct Quad {
@@ -216,22 +225,32 @@ __device__ __forceinline__ double flip_energy(const FlipE& f, const double* p) {
   return tot;
 }
 
-__global__ void k_flip_init(FlipE fe, const Globals* g, FlipState* st) {
+__global__ void k_flip_init(FlipE fe, const Globals* g, long long nflips, FlipState* st) {
   if (threadIdx.x || blockIdx.x) return;
   for (int k = 0; k < 6; ++k) st->props[k] = g->props[k];
   st->e0 = flip_energy(fe, st->props);
+  st->next_new = 0;
+  st->nn_next = 0;
+  st->nflips = nflips;
+  st->W = 0;
+  st->wid = 0;
   st->acc = 0;
   st->npend = 0;
   st->status = 0;
 }
 
-__global__ void k_fill(int W, long long next_new, const long long* pend, const FlipState* st, long long* win,
-                       int* limit) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0) *limit = W;
-  if (s >= W) return;
-  int np = st->npend;
-  win[s] = s < np ? pend[s] : next_new + (s - np);
+__global__ void k_fill(int B, const long long* pend, FlipState* st, long long* win, int* limit) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = st->npend;
+  const long long nn = st->next_new;
+  const int W = (int)min((long long)B, (long long)np + (st->nflips - nn));
+  if (s == 0) {
+    *limit = W;
+    st->W = W;
+    st->wid += W > 0 ? 1 : 0;
+    st->nn_next = nn + (W - np);
+  }
+  if (s < W) win[s] = s < np ? pend[s] : nn + (s - np);
 }
 
 // Patch ownership without a release pass: owner[x] holds the largest tag
@@ -252,19 +271,21 @@ __device__ __forceinline__ void for_ring_edges(const TopoW& t, int v, F&& fn) {
   }
 }
 
-__global__ void k_claim(TopoW t, int W, int wid, unsigned long long seed, const long long* win, int* owner) {
+__global__ void k_claim(TopoW t, const FlipState* st, unsigned long long seed, const long long* win, int* owner) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   int s = g >> 2, k = g & 3;
+  const int W = st->W, wid = st->wid;
   if (s >= W) return;
   Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
   const int tag = owner_tag(wid, s);
   for_ring_edges(t, quad_vertex(q, k), [&](int x) { atomicMax(&owner[x], tag); });
 }
 
-__global__ void k_winner(TopoW t, int W, int wid, int mode, unsigned long long seed, const long long* win,
+__global__ void k_winner(TopoW t, const FlipState* st, int mode, unsigned long long seed, const long long* win,
                          const int* owner, unsigned char* winner, int* limit) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   int s = g >> 2, k = g & 3;
+  const int W = st->W, wid = st->wid;
   if (s >= W) return;
   Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
   const int tag = owner_tag(wid, s);
@@ -304,16 +325,17 @@ __device__ double repulsion_of(int v, d3 xv, const double* P, const EP& ep, cons
 // of vertex_properties (src/mesh_properties.cpp:12-49) in parallel, and one
 // worker sums them in ring order while
 // another computes the repulsion.
-__global__ void __launch_bounds__(64) k_delta(TopoW t, int W, unsigned long long seed, const long long* win,
-                                              const unsigned char* winner, const int* limit, const double* P,
-                                              EP ep, NLView nl, double* part, unsigned char* okf, double* dpn) {
+__global__ void __launch_bounds__(64) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
+                                              const long long* win, const unsigned char* winner, const int* limit,
+                                              const double* P, EP ep, NLView nl, double* part, unsigned char* okf,
+                                              double* dpn) {
   __shared__ int sr[8][TM_MAXVAL + 1];
   __shared__ unsigned char sf[8][TM_MAXVAL + 1];
   __shared__ int sn[8];
   __shared__ double term[8][TM_MAXVAL + 1][4];
   const int s = blockIdx.x;
   const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
-  if (s >= W) return;
+  if (s >= st->W) return;
   if (s >= *limit || !winner[s]) {
     if (threadIdx.x == 0) {
       okf[s] = 0;
@@ -439,13 +461,15 @@ __global__ void __launch_bounds__(64) k_delta(TopoW t, int W, unsigned long long
 // same decisions as a walk in slot order.  Then the deferred proposals are
 // compacted in order for the next window.
 constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread
-__global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const unsigned char* winner,
+__global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsigned char* winner,
                                              const double* dpn, FlipE fe, FlipState* st, const int* limit,
                                              unsigned char* accepted, long long* pend) {
   __shared__ double sP[6], se0;
   __shared__ int sfirst, sstart, sacc;
   __shared__ int scan[MB];
   const int tid = threadIdx.x;
+  const int W = st->W;
+  __syncthreads();  // every thread has read W before thread 0 may write the state
   if (tid == 0) {
     for (int k = 0; k < 6; ++k) sP[k] = st->props[k];
     se0 = st->e0;
@@ -515,16 +539,17 @@ __global__ void __launch_bounds__(MB) k_metro(int W, const long long* win, const
     for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
     st->e0 = se0;
     st->acc = sacc;
+    st->next_new = st->nn_next;
   }
 }
 
 // one block of 32 threads per slot (accepted slots only do work): the
 // half-edge rewiring, then the two face rows and five edge rows, then the
 // four ring rows, each stage in parallel
-__global__ void __launch_bounds__(32) k_commit(TopoW t, int W, unsigned long long seed, const long long* win,
+__global__ void __launch_bounds__(32) k_commit(TopoW t, unsigned long long seed, const long long* win,
                                                const unsigned char* accepted, FlipState* st) {
   const int s = blockIdx.x;
-  if (s >= W || !accepted[s]) return;
+  if (s >= st->W || !accepted[s]) return;
   const int tid = threadIdx.x;
   const int e = flip_edge_of(seed, win[s], t.ne);
   const int a0 = 2 * e, b0 = 2 * e + 1;
@@ -610,38 +635,39 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   k_owner_init<<<nblk(ne, 256), 256, 0, s>>>(owner.get(), ne);
   TM_LAUNCH();
   FlipE fe{1.0 / ep.refA, 1.0 / ep.refV, 1.0 / ep.refC, ep.ka, ep.kv, ep.kc, ep.kt, ep.kr, ep.kb};
-  k_flip_init<<<1, 1, 0, s>>>(fe, e->glob.get(), st.get());
+  k_flip_init<<<1, 1, 0, s>>>(fe, e->glob.get(), nflips, st.get());
   TM_LAUNCH();
+  // windows are queued in groups without host round trips; W and the window
+  // number live on the device, and a window after the last one is empty
+  // (W = 0: every kernel returns at once)
+  const int B = batch;
+  constexpr int GROUP = 8;
   FlipState hs;
-  hs.npend = 0;
-  long long next_new = 0;
-  int B = batch;
-  int wid = 0;  // window number of the ownership tags
-  while (hs.npend > 0 || next_new < nflips) {
-    int W = (int)std::min<long long>(B, hs.npend + (nflips - next_new));
-    k_fill<<<nblk(W, 256), 256, 0, s>>>(W, next_new, pend.get(), st.get(), win.get(), limit.get());
-    TM_LAUNCH();
-    next_new += W - hs.npend;
-    ++wid;
-    if (wid >= (1 << 19)) fail(TM_ERR_ARG, "too many windows in one sweep");
-    k_claim<<<nblk(4L * W, 64), 64, 0, s>>>(t, W, wid, seed, win.get(), owner.get());
-    TM_LAUNCH();
-    k_winner<<<nblk(4L * W, 64), 64, 0, s>>>(t, W, wid, mode, seed, win.get(), owner.get(), winner.get(),
-                                           limit.get());
-    TM_LAUNCH();
-    k_delta<<<W, 64, 0, s>>>(t, W, seed, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get(),
-                             dpn.get());
-    TM_LAUNCH();
-    k_metro<<<1, MB, 0, s>>>(W, win.get(), winner.get(), dpn.get(), fe, st.get(), limit.get(), acc.get(),
-                             pend.get());
-    TM_LAUNCH();
-    k_commit<<<W, 32, 0, s>>>(t, W, seed, win.get(), acc.get(), st.get());
-    TM_LAUNCH();
+  for (;;) {
+    for (int k = 0; k < GROUP; ++k) {
+      k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st.get(), win.get(), limit.get());
+      TM_LAUNCH();
+      k_claim<<<nblk(4L * B, 64), 64, 0, s>>>(t, st.get(), seed, win.get(), owner.get());
+      TM_LAUNCH();
+      k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st.get(), mode, seed, win.get(), owner.get(), winner.get(),
+                                             limit.get());
+      TM_LAUNCH();
+      k_delta<<<B, 64, 0, s>>>(t, st.get(), seed, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(),
+                               okf.get(), dpn.get());
+      TM_LAUNCH();
+      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), fe, st.get(), limit.get(), acc.get(),
+                               pend.get());
+      TM_LAUNCH();
+      k_commit<<<B, 32, 0, s>>>(t, seed, win.get(), acc.get(), st.get());
+      TM_LAUNCH();
+    }
     TM_CUDA(cudaMemcpyAsync(&hs, st.get(), sizeof(FlipState), cudaMemcpyDeviceToHost, s));
     TM_CUDA(cudaStreamSynchronize(s));
     if (hs.status) fail(TM_ERR_TOPOLOGY, "flip produced a valence above TM_MAXVAL");
     // slot 0 of a window always owns its patch, so every window decides at
-    // least one proposal and the loop ends
+    // least one proposal and the sweep ends
+    if (hs.npend == 0 && hs.next_new >= nflips) break;
+    if (hs.wid >= (1 << 19) - GROUP) fail(TM_ERR_ARG, "too many windows in one sweep");
   }
   m->host_topo_stale = true;
   if (hs.acc > 0) {
