@@ -163,21 +163,11 @@ def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400):
                       f"N(0,1e-4)) of the 163,842-vertex workload, {t:.1f} s, OpenMP {O.get_threads()} threads"}
 
 
-def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_steps=20):
-    """Replica batch of the 64-membrane configuration: 16 replicas each of
-    642, 2,562, 10,242 and 40,962 vertices, reduced volume ~ U[0.6, 0.95] and
-    kappa_b ~ U[10, 50] (seeded), sampled together by device-side HMC (one
-    launch per stage for all replicas, each HMC step one CUDA graph replay),
-    against the same replicas evaluated one mesh at a time (FP32 stencil,
-    like the batch)."""
-    import ctypes
-
-    import torch
-
-    from trimem_gb300 import capi, meshgen
+def batch_members(n_per_level=16, levels=(3, 4, 5, 6)):
+    """The 64 membranes of the batch configuration: (points, faces, params)."""
+    from trimem_gb300 import meshgen
     from trimem_gb300.workloads import workload_params
 
-    L = capi.lib()
     rng = np.random.default_rng(2024)
     reps = []
     for lv in levels:
@@ -185,6 +175,29 @@ def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_step
             p, f = meshgen.jittered_icosphere(lv, seed=100 * lv + k)
             reps.append((p, f, workload_params(p, f, kappa_b=float(rng.uniform(10, 50)),
                                                vfrac=float(rng.uniform(0.6, 0.95)))))
+    return reps
+
+
+def batch_replicas():
+    from trimem_gb300 import capi
+
+    reps = batch_members()
+    return capi.Batch([(p, f) for p, f, _ in reps], [capi.params(**prm) for _, _, prm in reps])
+
+
+def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_steps=20):
+    """Replica batch of the 64-membrane configuration: 16 replicas each of
+    642, 2,562, 10,242 and 40,962 vertices, reduced volume ~ U[0.6, 0.95] and
+    kappa_b ~ U[10, 50] (seeded), sampled together by device-side HMC (one
+    launch per stage for all replicas, each HMC step one CUDA graph replay),
+    against the same replicas evaluated one mesh at a time (FP32 stencil,
+    like the batch)."""
+    import torch
+
+    from trimem_gb300 import capi
+
+    L = capi.lib()
+    reps = batch_members(n_per_level, levels)
     n_rep = len(reps)
     nvert = sum(len(p) for p, _, _ in reps)
     b = capi.Batch([(p, f) for p, f, _ in reps], [capi.params(**prm) for _, _, prm in reps])
@@ -314,6 +327,11 @@ def run_profile(args):
 
     from trimem_gb300 import capi
 
+    if args.profile_batch:
+        b = batch_replicas()
+        b.hmc(args.profile_batch, 10, 1e-6, seed=1, use_graph=False)
+        print("profile batch HMC steps done:", args.profile_batch)
+        return
     p, f, prm = workload()
     mesh = capi.Mesh(p, f)
     en = capi.Energy(mesh, capi.params(**prm))
@@ -374,10 +392,12 @@ def main():
                     help="only run this many surrogate force evaluations (for ncu captures) and exit")
     ap.add_argument("--profile-flips", type=int, default=0,
                     help="only run this many flip sweeps (ratio 0.2) (for ncu captures) and exit")
+    ap.add_argument("--profile-batch", type=int, default=0,
+                    help="only run this many HMC steps of the 64-replica batch (for ncu captures) and exit")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.profile_evals or args.profile_surrogate or args.profile_flips:
+    if args.profile_evals or args.profile_surrogate or args.profile_flips or args.profile_batch:
         return run_profile(args)
 
     import torch
