@@ -207,8 +207,11 @@ static void upload_eps(tm_batch* b) {
 }
 
 static void rebuild_nlist(tm_batch* b) {
+  // near rows when every replica's cells are at least its repulsion cut-off
+  bool near = true;
+  for (const tm_params& p : b->prm) near = near && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1;
   nlist_make_batch(&b->en->nl, b->mesh.get(), b->R, b->vrep.get(), b->rblocks.get(), b->rlist.get(),
-                   b->prm[0].exclusion_level, b->x.get(), b->stream);
+                   b->prm[0].exclusion_level, b->x.get(), b->stream, b->eps.get(), near);
 }
 
 // block sizes of {split, face, edge, grad} by timing each candidate

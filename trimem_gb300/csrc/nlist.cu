@@ -25,6 +25,7 @@
 #include <cstring>
 #include <memory>
 
+#include "tm_energy.cuh"
 #include "tm_internal.h"
 #include "tm_math.cuh"
 
@@ -430,11 +431,20 @@ __global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt,
 // excluded on the current topology.  A row longer than TM_NEAR_CAP marks the
 // rows unusable (flag[3]).
 __global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, double rn, double rn2, int* flag,
-                       int* ncnt, int* nent, double* xb) {
+                       int* ncnt, int* nent, double* xb, const EP* eps) {
   if (flag[1] == 0) return;  // rows still valid
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nv) return;
-  const NLGeom& G = nl.geom[0];
+  const int rep = rep_of(nl, a);
+  if (rep < 0) {  // padding vertex of a batch
+    ncnt[a] = 0;
+    return;
+  }
+  if (eps) {  // batch: the replica's cut-off
+    rn = 2.0 * eps[rep].rlc1;
+    rn2 = rn * rn * (1.0 + 1e-12);
+  }
+  const NLGeom& G = nl.geom[rep];
   d3 pa = ld3(P, a);
   const double* pp = &pa.x;
   int lo[3], hi[3];
@@ -458,7 +468,7 @@ __global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, dou
         if (g2 > rn2 * 1.000001) continue;
         long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
         int st = 0;
-        int c = cell_lookup(nl, cid, &st);
+        int c = cell_lookup(nl, cell_key(cid, rep), &st);
         for (int q = 0; q < c; ++q) {
           int b = nl.cell_verts[st + q];
           if (b == a) continue;
@@ -486,9 +496,14 @@ __global__ void k_near_done(int* flag, const int* dtopo) {
 // before a cell-list rebuild: the rows go stale once some vertex has moved
 // lc1/2 or more from where they were built (thr2 rounded down; NaN moves)
 __global__ void k_near_check(int nv, const double* __restrict__ P, const double* __restrict__ xb, double thr2,
-                             int* flag) {
+                             int* flag, const int* __restrict__ vrep, const EP* __restrict__ eps) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv || flag[1]) return;
+  if (vrep) {  // batch: the replica's skin, padding vertices never move
+    int r = vrep[v];
+    if (r < 0) return;
+    thr2 = 0.25 * eps[r].rlc1 * eps[r].rlc1 * (1.0 - 1e-12);
+  }
   double dx = P[3 * v] - xb[3 * v], dy = P[3 * v + 1] - xb[3 * v + 1], dz = P[3 * v + 2] - xb[3 * v + 2];
   if (!(dx * dx + dy * dy + dz * dz < thr2)) flag[1] = 1;
 }
@@ -644,7 +659,8 @@ static void build_cells(tm_nlist* nl, NLView& V, int nv, const double* P, cudaSt
 // current cell and visits them in the reference's order.  The rows do not
 // depend on the cell list, so a cell-list rebuild rebuilds them only when a
 // vertex has moved lc1/2 since they were built (decided on the device).
-static void refresh_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, double lc1, cudaStream_t s) {
+static void refresh_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, double lc1, cudaStream_t s,
+                         const EP* eps = nullptr) {
   int nv = nl->nv;
   Topo t = m->topo();
   double rn = 2.0 * lc1;
@@ -661,10 +677,10 @@ static void refresh_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, d
     nl->near_move2 = 0.25 * lc1 * lc1 * (1.0 - 1e-12);
   }
   int* flag = nl->nflag.get();
-  k_near_check<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->xb.get(), nl->near_move2, flag);
+  k_near_check<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->xb.get(), nl->near_move2, flag, V.vrep, eps);
   TM_LAUNCH();
   k_near<<<nblk(nv, 128), 128, 0, s>>>(nv, P, V, t, V.excl, rn, rn * rn * (1.0 + 1e-12), flag, nl->ncnt.get(),
-                                       nl->nent.get(), nl->xb.get());
+                                       nl->nent.get(), nl->xb.get(), eps);
   TM_LAUNCH();
   k_near_done<<<1, 32, 0, s>>>(flag, m->d_topo_ver.get());
   TM_LAUNCH();
@@ -732,7 +748,8 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
 }
 
 void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
-                      const double* d_rlist, int excl, const double* P, cudaStream_t s) {
+                      const double* d_rlist, int excl, const double* P, cudaStream_t s, const EP* d_eps,
+                      bool near) {
   if (excl < 0 || excl > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
   int nv = m->nv;
   nl->nv = nv;
@@ -753,7 +770,10 @@ void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const 
   }
   k_bbox_final_batch<<<R, BB, 0, s>>>(d_rblocks, nl->bbox.get(), d_rlist, nl->geom.get());
   TM_LAUNCH();
-  build_cells(nl, V, nv, P, s, true);
+  build_cells(nl, V, nv, P, s, !near);
+  // near rows with each replica's cut-off (the lc1 argument only tags the
+  // rows: any positive value)
+  if (near && nv > 0) refresh_near(nl, m, V, P, 1.0, s, d_eps);
 }
 
 int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* P, double rd, cudaStream_t s) {

@@ -134,9 +134,14 @@ __global__ void __launch_bounds__(256) k_rep_slow(Topo t, const double* __restri
 // flag = 1 when some vertex is lc1/2 or farther from where the near rows
 // were built (squared threshold thr2, rounded down); NaN counts as moved
 __global__ void k_moved(int nv, const double* __restrict__ P, const double* __restrict__ xb, double thr2,
-                        int* flag) {
+                        int* flag, const int* __restrict__ vrep, const EP* __restrict__ eps) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= nv) return;
+  if (vrep) {  // batch: the replica's skin, padding vertices never move
+    int r = vrep[v];
+    if (r < 0) return;
+    thr2 = 0.25 * eps[r].rlc1 * eps[r].rlc1 * (1.0 - 1e-12);
+  }
   double dx = P[3 * v] - xb[3 * v], dy = P[3 * v + 1] - xb[3 * v + 1], dz = P[3 * v + 2] - xb[3 * v + 2];
   if (!(dx * dx + dy * dy + dz * dz < thr2)) atomicOr(flag, 1);
 }
@@ -160,11 +165,11 @@ void repulsion_eval(tm_energy* e, tm_mesh* m, const double* P, const float* pos3
   nlv.pos32 = pos32;
   TM_CUDA(cudaMemsetAsync(nslow, 0, sizeof(int), s));
   int use_near = 0;
-  if (nlv.kind == 0 && nlv.nent && !eps && e->nl.near_lc1 == ep.rlc1 && e->nl.near_nv == nv) {
+  if (nlv.kind == 0 && nlv.nent && e->nl.near_nv == nv && (eps || e->nl.near_lc1 == ep.rlc1)) {
     use_near = 1;
     int* flag = e->nl.nflag.get();
     TM_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
-    k_moved<<<nblk(nv, 256), 256, 0, s>>>(nv, P, e->nl.xb.get(), e->nl.near_move2, flag);
+    k_moved<<<nblk(nv, 256), 256, 0, s>>>(nv, P, e->nl.xb.get(), e->nl.near_move2, flag, nlv.vrep, eps);
     TM_LAUNCH();
   }
   if (want_grad)

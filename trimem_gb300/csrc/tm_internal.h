@@ -257,7 +257,8 @@ int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* d_points, 
 // cell list over a batch of replicas (disjoint-union mesh with replica-aligned
 // 256-vertex blocks): per-replica boxes and cut-offs, replica-tagged cells
 void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
-                      const double* d_rlist, int excl, const double* d_points, cudaStream_t s);
+                      const double* d_rlist, int excl, const double* d_points, cudaStream_t s, const EP* d_eps,
+                      bool near);
 int64_t nlist_point_distances(tm_nlist* nl, tm_mesh* m, const double* d_points, int pid, double rdist,
                               cudaStream_t s);
 // smallest double T with sqrt(T) >= d (IEEE round-to-nearest sqrt), so that
