@@ -327,8 +327,8 @@ __device__ double repulsion_of(int v, d3 xv, const double* P, const EP& ep, cons
 // another computes the repulsion.
 __global__ void __launch_bounds__(64) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
                                               const long long* win, const unsigned char* winner, const int* limit,
-                                              const double* P, EP ep, NLView nl, double* part, unsigned char* okf,
-                                              double* dpn) {
+                                              const double* P, EP ep, FlipE fe, NLView nl, double* part,
+                                              unsigned char* okf, double* dpn) {
   __shared__ int sr[8][TM_MAXVAL + 1];
   __shared__ unsigned char sf[8][TM_MAXVAL + 1];
   __shared__ int sn[8];
@@ -449,7 +449,11 @@ __global__ void __launch_bounds__(64) k_delta(TopoW t, const FlipState* st, unsi
       o8[k] = before - after;
     }
     o8[6] = -log(flip_u_of(seed, win[s]));
-    o8[7] = 1.0;
+    // the Metropolis test on the state at the start of the window (the
+    // first round of k_metro): 2 = accepted there, 1 = rejected there
+    double trial[6];
+    for (int k = 0; k < 6; ++k) trial[k] = st->props[k] - o8[k];
+    o8[7] = flip_energy(fe, trial) - st->e0 <= o8[6] ? 2.0 : 1.0;
   }
 }
 
@@ -490,10 +494,15 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
       if (s < start || s >= W) continue;
       const double* o8 = dpn + 8 * (size_t)s;
       if (o8[7] == 0.0) continue;
-      double trial[6];
-      for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
-      double de = flip_energy(fe, trial) - se0;
-      if (de <= o8[6]) {
+      bool acc_s;
+      if (round == 0) {  // decided by k_delta on this same state
+        acc_s = o8[7] == 2.0;
+      } else {
+        double trial[6];
+        for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
+        acc_s = flip_energy(fe, trial) - se0 <= o8[6];
+      }
+      if (acc_s) {
         atomicMin(&sfirst, s);
         break;  // later slots of this thread cannot be first
       }
@@ -652,8 +661,8 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st.get(), mode, seed, win.get(), owner.get(), winner.get(),
                                              limit.get());
       TM_LAUNCH();
-      k_delta<<<B, 64, 0, s>>>(t, st.get(), seed, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(),
-                               okf.get(), dpn.get());
+      k_delta<<<B, 64, 0, s>>>(t, st.get(), seed, win.get(), winner.get(), limit.get(), P, ep, fe, nlv,
+                               part.get(), okf.get(), dpn.get());
       TM_LAUNCH();
       k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), fe, st.get(), limit.get(), acc.get(),
                                pend.get());
