@@ -53,6 +53,10 @@ typedef struct tm_nlist tm_nlist;
 const char* tm_last_error(void);
 /* Name of the CUDA device the library runs on; fails when none is present. */
 int tm_device_name(char* buf, int len);
+/* Page-locked host memory (results copied there from the device need no
+ * staging); the Python module hands such buffers to numpy. */
+int tm_host_alloc(int64_t bytes, void** out);
+int tm_host_free(void* p);
 
 /* ---- mesh ---------------------------------------------------------------
  * TriMesh(points, faces): src/bindings.cpp:87-109, src/mesh_py.cpp:12-70.

@@ -58,6 +58,8 @@ def params(**kw):
 _SIGS = {
     "tm_last_error": (ctypes.c_char_p, []),
     "tm_device_name": (_i32, [ctypes.c_char_p, _i32]),
+    "tm_host_alloc": (_i32, [_i64, _pp]),
+    "tm_host_free": (_i32, [_p]),
     "tm_mesh_create": (_i32, [_dp, _i64, _ip, _i64, _pp]),
     "tm_mesh_destroy": (_i32, [_p]),
     "tm_mesh_counts": (_i32, [_p, _i64p, _i64p, _i64p]),

@@ -21,7 +21,61 @@
 
 #include "trimem_gpu.h"
 
+
 namespace py = pybind11;
+
+namespace {
+
+// Result arrays of gradients live in page-locked memory, recycled through a
+// small pool: the device writes them without staging, and their pages are
+// never first touched inside a timed copy.  A buffer returns to the pool
+// when numpy releases the array.
+struct PinnedPool {
+  std::multimap<size_t, void*> free_list;
+  void* take(size_t bytes) {
+    auto it = free_list.find(bytes);
+    if (it != free_list.end()) {
+      void* p = it->second;
+      free_list.erase(it);
+      return p;
+    }
+    void* p = nullptr;
+    if (tm_host_alloc((int64_t)bytes, &p) != TM_OK) return nullptr;
+    return p;
+  }
+  void give(size_t bytes, void* p) {
+    if (free_list.size() < 8)
+      free_list.emplace(bytes, p);
+    else
+      tm_host_free(p);
+  }
+};
+PinnedPool& pinned_pool() {
+  static PinnedPool* pool = new PinnedPool();  // outlives module teardown
+  return *pool;
+}
+struct PoolBlock {
+  size_t bytes;
+  void* p;
+};
+
+// (rows, cols) float64 array in pooled page-locked memory (plain numpy
+// memory when page-locked memory is not available)
+py::array_t<double> pinned_array(py::ssize_t rows, py::ssize_t cols) {
+  size_t bytes = sizeof(double) * (size_t)rows * (size_t)cols;
+  void* p = pinned_pool().take(bytes);
+  if (!p) return py::array_t<double>({rows, cols});
+  auto* blk = new PoolBlock{bytes, p};
+  py::capsule owner(blk, [](void* q) {
+    auto* b = static_cast<PoolBlock*>(q);
+    pinned_pool().give(b->bytes, b->p);
+    delete b;
+  });
+  return py::array_t<double>({rows, cols}, {(py::ssize_t)(cols * sizeof(double)), (py::ssize_t)sizeof(double)},
+                             static_cast<double*>(p), owner);
+}
+
+}  // namespace
 
 namespace {
 
@@ -309,7 +363,7 @@ struct EnergyManager {
     return e;
   }
   py::array_t<double> gradient(TriMesh& m) {
-    py::array_t<double> out({(py::ssize_t)m.nv(), (py::ssize_t)3});
+    py::array_t<double> out = pinned_array((py::ssize_t)m.nv(), 3);
     check(tm_energy_gradient(h, m.h, out.mutable_data(), nullptr));
     return out;
   }
@@ -563,7 +617,7 @@ PYBIND11_MODULE(core, m) {
       .def(
           "energy_gradient",
           [](EnergyManager& e, TriMesh& t) {
-            py::array_t<double> out({(py::ssize_t)t.nv(), (py::ssize_t)3});
+            py::array_t<double> out = pinned_array((py::ssize_t)t.nv(), 3);
             double en = 0;
             check(tm_energy_gradient(e.h, t.h, out.mutable_data(), &en));
             return py::make_tuple(en, out);

@@ -1,3 +1,4 @@
+#include <algorithm>
 // Error plumbing and deterministic scan / reduction helpers.
 #include <cmath>
 #include <cstdio>
@@ -116,5 +117,25 @@ extern "C" int tm_device_name(char* buf, int len) {
     return TM_ERR_CUDA;
   }
   snprintf(buf, len, "%s", p.name);
+  return TM_OK;
+}
+
+extern "C" int tm_host_alloc(int64_t bytes, void** out) {
+  if (!out || bytes < 0) {
+    tmg::set_last_error("invalid argument");
+    return TM_ERR_ARG;
+  }
+  *out = nullptr;
+  if (cudaMallocHost(out, (size_t)std::max<int64_t>(bytes, 1)) != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    tmg::set_last_error("page-locked allocation failed");
+    return TM_ERR_NOMEM;
+  }
+  return TM_OK;
+}
+
+extern "C" int tm_host_free(void* p) {
+  if (p) cudaFreeHost(p);
   return TM_OK;
 }
