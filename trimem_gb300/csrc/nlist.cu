@@ -770,7 +770,10 @@ void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const 
   }
   k_bbox_final_batch<<<R, BB, 0, s>>>(d_rblocks, nl->bbox.get(), d_rlist, nl->geom.get());
   TM_LAUNCH();
-  build_cells(nl, V, nv, P, s, !near);
+  // candidate rows as well: unrelaxed replicas can move a skin's width
+  // within a few steps, and then the candidate rows keep most vertices off
+  // the cell walk
+  build_cells(nl, V, nv, P, s, true);
   // near rows with each replica's cut-off (the lc1 argument only tags the
   // rows: any positive value)
   if (near && nv > 0) refresh_near(nl, m, V, P, 1.0, s, d_eps);
