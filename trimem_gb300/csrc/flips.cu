@@ -325,7 +325,7 @@ __device__ double repulsion_of(int v, d3 xv, const double* P, const EP& ep, cons
 // of vertex_properties (src/mesh_properties.cpp:12-49) in parallel, and one
 // worker sums them in ring order while
 // another computes the repulsion.
-__global__ void __launch_bounds__(64) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
+__global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
                                               const long long* win, const unsigned char* winner, const int* limit,
                                               const double* P, EP ep, FlipE fe, NLView nl, double* part,
                                               unsigned char* okf, double* dpn) {
