@@ -246,37 +246,45 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
     FaceD Fc;
     int fcur = slot_face(sc.y);
     if (fcur >= 0) Fc = fd[fcur];
+    const double gV6 = gV * (1.0 / 6.0);
+    // scalar multiples of face normals are summed per face: the dihedral
+    // term of edge (i, j) reaches the normal of the next face, so its part
+    // is carried to the next slot (the last one wraps to the first face)
+    double carry = 0.0;
+    d3 n0 = mk(0, 0, 0);
     for (int m = 0; m < d; ++m) {
       int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
       int fnx = slot_face(sn.y);
       FaceD Fn;
       if (fnx >= 0) Fn = fd[fnx];
+      double carry_next = 0.0;
       if (fcur >= 0) {
         int ci = slot_corner(sc.y);
         double cj = cot_at(Fc, ci == 2 ? 0 : ci + 1);
         double ck = cot_at(Fc, ci == 0 ? 2 : ci - 1);
         d3 n = mk(Fc.nx, Fc.ny, Fc.nz);
+        if (m == 0) n0 = n;
         // face (i, j, k): area and volume terms
         double alpha = gA - kb23 * (ri * ri + rj * rj + rk * rk);
         if (ep.btype == 1) alpha += ep.kt * 2.0 * (Fc.A / ep.a0 - 1.0) / ep.a0;
         acc += (0.5 * alpha) * cross(n, xk - xj);
-        acc += (gV * (1.0 / 6.0)) * cross(xj, xk);
+        acc += gV6 * cross(xj, xk);
         // edge (i, j): length and dihedral terms
         EdgeD E = ed[sc.z];
         double w = hgC + kb * (ri + rj);
         double cl = w * E.th + (ep.btype == 0 ? ep.kt * E.db : 0.0);
         acc += (-cl * fabs(E.il)) * (xj - xi);
+        double cn = carry;
         if (E.il > 0.0) {
           int cin = slot_corner(sn.y);
-          double cjn = cot_at(Fn, cin == 0 ? 2 : cin - 1);
-          acc += w * (cj * n + cjn * mk(Fn.nx, Fn.ny, Fn.nz));
+          cn += w * cj;
+          carry_next = w * cot_at(Fn, cin == 0 ? 2 : cin - 1);
         }
         // edge (j, k) opposite i: dihedral term
-        if (ed[sc.w].il > 0.0) {
-          double wo = hgC + kb * (rj + rk);
-          acc += (-wo * (cj + ck)) * n;
-        }
+        if (ed[sc.w].il > 0.0) cn -= (hgC + kb * (rj + rk)) * (cj + ck);
+        acc += cn * n;
       }
+      carry = carry_next;
       xk = xj;
       rk = rj;
       sc = sn;
@@ -285,6 +293,7 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
       xj = ld3(P, sn.x);
       rj = rho[sn.x];
     }
+    acc += carry * n0;  // the last edge's part on the first face
   }
   st3(grad, i, acc);
 }

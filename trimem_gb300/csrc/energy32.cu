@@ -192,16 +192,22 @@ __global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __
     int fcur = slot_face(sc.y);
     if (fcur >= 0) Fc = fd[fcur];
     f3 xi_abs = S.h(i);
+    // normal multiples summed per face; the dihedral part of edge (i, j) on
+    // the next face is carried to the next slot
+    float carry = 0.0f;
+    f3 n0 = {0.0f, 0.0f, 0.0f};
     for (int m = 0; m < d; ++m) {
       int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
       int fnx = slot_face(sn.y);
       FaceF Fn;
       if (fnx >= 0) Fn = fd[fnx];
+      float carry_next = 0.0f;
       if (fcur >= 0) {
         int ci = slot_corner(sc.y);
         float cj = cotf_at(Fc, ci == 2 ? 0 : ci + 1);
         float ck = cotf_at(Fc, ci == 0 ? 2 : ci - 1);
         f3 n = {Fc.nx, Fc.ny, Fc.nz};
+        if (m == 0) n0 = n;
         float alpha = gA - kb23 * (ri * ri + rj * rj + rk * rk);
         if (ep.btype == 1) alpha += kt * 2.0f * (Fc.A / a0 - 1.0f) / a0;
         acc += (0.5f * alpha) * fcross(n, xk - xj);
@@ -212,16 +218,16 @@ __global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __
         float w = hgC + kb * (ri + rj);
         float cl = w * E.th + (ep.btype == 0 ? kt * E.db : 0.0f);
         acc += (-cl / E.l) * xj;
+        float cn = carry;
         if (E.flag != 0.0f) {
           int cin = slot_corner(sn.y);
-          float cjn = cotf_at(Fn, cin == 0 ? 2 : cin - 1);
-          acc += w * (cj * n + cjn * f3{Fn.nx, Fn.ny, Fn.nz});
+          cn += w * cj;
+          carry_next = w * cotf_at(Fn, cin == 0 ? 2 : cin - 1);
         }
-        if (ed[sc.w].flag != 0.0f) {
-          float wo = hgC + kb * (rj + rk);
-          acc += (-wo * (cj + ck)) * n;
-        }
+        if (ed[sc.w].flag != 0.0f) cn -= (hgC + kb * (rj + rk)) * (cj + ck);
+        acc += cn * n;
       }
+      carry = carry_next;
       xk = xj;
       rk = rj;
       sc = sn;
@@ -230,6 +236,7 @@ __global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __
       xj = S.diff(sn.x, i);
       rj = rho[sn.x];
     }
+    acc += carry * n0;
   }
   grad[3 * i] = acc.x;
   grad[3 * i + 1] = acc.y;
@@ -389,16 +396,22 @@ __global__ void __launch_bounds__(256) k_grad32b(Topo t, Split S, const FaceF* _
     int fcur = slot_face(sc.y);
     if (fcur >= 0) Fc = fd[fcur];
     f3 xi_abs = S.h(i);
+    // normal multiples summed per face; the dihedral part of edge (i, j) on
+    // the next face is carried to the next slot
+    float carry = 0.0f;
+    f3 n0 = {0.0f, 0.0f, 0.0f};
     for (int m = 0; m < d; ++m) {
       int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
       int fnx = slot_face(sn.y);
       FaceF Fn;
       if (fnx >= 0) Fn = fd[fnx];
+      float carry_next = 0.0f;
       if (fcur >= 0) {
         int ci = slot_corner(sc.y);
         float cj = cotf_at(Fc, ci == 2 ? 0 : ci + 1);
         float ck = cotf_at(Fc, ci == 0 ? 2 : ci - 1);
         f3 n = {Fc.nx, Fc.ny, Fc.nz};
+        if (m == 0) n0 = n;
         float alpha = gA - kb23 * (ri * ri + rj * rj + rk * rk);
         if (ep.btype == 1) alpha += kt * 2.0f * (Fc.A / a0 - 1.0f) / a0;
         acc += (0.5f * alpha) * fcross(n, xk - xj);
@@ -408,16 +421,16 @@ __global__ void __launch_bounds__(256) k_grad32b(Topo t, Split S, const FaceF* _
         float w = hgC + kb * (ri + rj);
         float cl = w * E.th + (ep.btype == 0 ? kt * E.db : 0.0f);
         acc += (-cl / E.l) * xj;
+        float cn = carry;
         if (E.flag != 0.0f) {
           int cin = slot_corner(sn.y);
-          float cjn = cotf_at(Fn, cin == 0 ? 2 : cin - 1);
-          acc += w * (cj * n + cjn * f3{Fn.nx, Fn.ny, Fn.nz});
+          cn += w * cj;
+          carry_next = w * cotf_at(Fn, cin == 0 ? 2 : cin - 1);
         }
-        if (ed[sc.w].flag != 0.0f) {
-          float wo = hgC + kb * (rj + rk);
-          acc += (-wo * (cj + ck)) * n;
-        }
+        if (ed[sc.w].flag != 0.0f) cn -= (hgC + kb * (rj + rk)) * (cj + ck);
+        acc += cn * n;
       }
+      carry = carry_next;
       xk = xj;
       rk = rj;
       sc = sn;
@@ -426,6 +439,7 @@ __global__ void __launch_bounds__(256) k_grad32b(Topo t, Split S, const FaceF* _
       xj = S.diff(sn.x, i);
       rj = rho[sn.x];
     }
+    acc += carry * n0;
   }
   grad[3 * i] = acc.x;
   grad[3 * i + 1] = acc.y;

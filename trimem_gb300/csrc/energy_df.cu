@@ -296,15 +296,22 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
     df3 dj = X.at(sc.x) - xi;
     df rj = rho[sc.x];
     int fcur = slot_face(sc.y);
+    // scalar multiples of face normals are summed per face: the dihedral
+    // term of edge (i, j) reaches the normal of the next face, so its part
+    // is carried to the next slot (the last one wraps to the first face)
+    df carry = df_make(0.0f);
+    df3 n0 = acc;
     for (int m = 0; m < d; ++m) {
       int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
       int fnx = slot_face(sn.y);
+      df carry_next = df_make(0.0f);
       if (fcur >= 0) {
         const FaceDF& Fc = fd[fcur];
         int ci = slot_corner(sc.y);
         df cj = cot_df(Fc, ci == 2 ? 0 : ci + 1);
         df ck = cot_df(Fc, ci == 0 ? 2 : ci - 1);
         df3 n = {Fc.nx, Fc.ny, Fc.nz};
+        if (m == 0) n0 = n;
         // face (i, j, k): area and volume terms
         df alpha = gA - epd.kb23 * (ri * ri + rj * rj + rk * rk);
         if (ep.btype == 1) alpha += ldexp2(epd.kt * (Fc.A * epd.inv_a0 - df_make(1.0f)) * epd.inv_a0, 2.0f);
@@ -319,19 +326,17 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
         if (ep.btype == 0) cl += epd.kt * E.db;
         const df il = E.il.hi < 0.0f ? -E.il : E.il;
         acc += (-(cl * il)) * dj;
+        df cn = carry;
         if (E.il.hi > 0.0f) {
-          const FaceDF& Fn = fd[fnx];
           int cin = slot_corner(sn.y);
-          df cjn = cot_df(Fn, cin == 0 ? 2 : cin - 1);
-          df3 nn = {Fn.nx, Fn.ny, Fn.nz};
-          acc += df3{w * (cj * n.x + cjn * nn.x), w * (cj * n.y + cjn * nn.y), w * (cj * n.z + cjn * nn.z)};
+          cn += w * cj;
+          carry_next = w * cot_df(fd[fnx], cin == 0 ? 2 : cin - 1);
         }
         // edge (j, k) opposite i: dihedral term
-        if (ed[sc.w].il.hi > 0.0f) {
-          df wo = hgC + kb * (rj + rk);
-          acc += (-(wo * (cj + ck))) * n;
-        }
+        if (ed[sc.w].il.hi > 0.0f) cn -= (hgC + kb * (rj + rk)) * (cj + ck);
+        acc += cn * n;
       }
+      carry = carry_next;
       dk = dj;
       rk = rj;
       sc = sn;
@@ -339,6 +344,7 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
       dj = X.at(sn.x) - xi;
       rj = rho[sn.x];
     }
+    acc += carry * n0;  // the last edge's part on the first face
   }
   if (d > 0) acc += gV6 * (vcr + dcross(xi, vtel));
   d3 r = ld3(repg, i);
