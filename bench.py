@@ -1,6 +1,6 @@
 """Benchmark: FP64 energy+gradient evaluations per second on one GB300.
 
-Workload (BASELINE metric "grad evals/s ..., 1 GB300, 163k verts"): a level-7
+Workload (metric "grad evals/s" on one GB300 at 163k vertices): a level-7
 icosphere (163,842 vertices, 327,680 faces), vertices jittered by 13% of the
 mean edge length (seed 0), the energy of the very-large-mesh configuration
 (kb 20, ka 1e6, kv 1e6, kc 0, kt 1e5, kr 1e3, reduced-volume target 0.65,
@@ -302,6 +302,8 @@ def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=200, weights=N
     t1 = time.perf_counter()
     bend = prm["kappa_b"] * trace[:, 3]
     e = ess(bend)
+    rv = 6.0 * np.sqrt(np.pi) * trace[:, 1] / trace[:, 0] ** 1.5  # reduced volume
+    e_rv = ess(rv)
     return {"dt": dt, "pilot_acceptance": pilot, "steps": n_steps, "burn_in": n_burn,
             "seconds": round(t1 - t0, 3), "ms_per_step": round((t1 - t0) * 1e3 / n_steps, 3),
             "acceptance": round((ch.accepted - a0) / n_steps, 3),
@@ -309,7 +311,9 @@ def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=200, weights=N
             "ms_per_move": {k: round((ch.seconds[k] - sec0[k]) * 1e3 / n_steps, 3) for k in sec0},
             "flip_attempts_per_s": round(int(0.2 * mesh.counts()[1]) * n_steps / max(ch.seconds["flip"] - sec0["flip"], 1e-9), 1),
             "ess_bending": round(e, 2), "ess_per_s": round(e / (t1 - t0), 3),
-            "bending_mean": float(bend.mean()), "bending_sd": float(bend.std())}
+            "bending_mean": float(bend.mean()), "bending_sd": float(bend.std()),
+            "ess_reduced_volume": round(e_rv, 2), "ess_reduced_volume_per_s": round(e_rv / (t1 - t0), 3),
+            "reduced_volume_mean": float(rv.mean())}
 
 
 def run_reference(args):
@@ -374,7 +378,7 @@ def run_profile(args):
         capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), None))
         for k in range(args.profile_flips):
             acc = ctypes.c_int32()
-            capi.check(L.tm_flip_device(mesh.h, en.h, ctypes.c_void_p(x.data_ptr()), 0.2, 7 + k, 1, 1024,
+            capi.check(L.tm_flip_device(mesh.h, en.h, ctypes.c_void_p(x.data_ptr()), 0.2, 7 + k, 1, 4096,
                                         ctypes.byref(acc), None))
         torch.cuda.synchronize()
         print("profile flip sweeps done:", args.profile_flips)
@@ -525,7 +529,7 @@ def main():
     dname = names[dom]
     achieved = kbytes[dname] / (kms[dom] * 1e-3) / 1e9
     traffic = read_traffic().get(dname)
-    # whole evaluation: SURVEY per-vertex algorithmic bytes (132 B/vertex)
+    # whole evaluation: 132 algorithmic bytes per vertex
     eval_bytes = 132 * V
     roofline = {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 5), "traffic": traffic, "peak_source": peak_note,

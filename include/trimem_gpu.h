@@ -247,6 +247,10 @@ int tm_batch_positions(tm_batch* b, double* host_x, int direction);
 /* energy of every replica (n_rep values) and optionally the gradient */
 int tm_batch_energy(tm_batch* b, double* energies, double* grad);
 int tm_batch_update_repulsion(tm_batch* b);
+/* neighbour list rebuilt after every `every`-th HMC step of tm_batch_hmc
+ * (0: never; default 1), like the evaluator callback of the reference's HMC
+ * (src/trimem/mc/evaluators.py) */
+int tm_batch_set_refresh(tm_batch* b, int every);
 /* n_steps HMC steps of every replica (n_leapfrog velocity-Verlet steps of
  * size dt, mass, temperature; per-replica Metropolis); use_graph replays one
  * captured step as a CUDA graph.  accepted[r] = accepted steps. */

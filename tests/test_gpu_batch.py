@@ -58,3 +58,19 @@ def test_batch_hmc_graph_replay_is_deterministic(C):
     x_init = [p for p, _, _ in reps]
     assert any(np.abs(x - xi).max() > 0 for x, xi in zip(runs[1][1], x_init))
     assert all(np.isfinite(x).all() for x in runs[1][1])
+
+
+def test_batch_hmc_refresh_changes_no_result(C):
+    """Rebuilding the neighbour list between steps only changes which path
+    finds the pairs (near rows, candidate rows or the cell walk), all in the
+    reference's pair order: positions and decisions are identical."""
+    reps = _replicas()
+    runs = []
+    for refresh in (0, 1, 2):
+        b = C.Batch([(p, f) for p, f, _ in reps], [C.params(**prm) for _, _, prm in reps])
+        acc = b.hmc(6, 5, 2e-6, seed=5, refresh=refresh)
+        runs.append((acc, b.positions()))
+    for acc, xs in runs[1:]:
+        assert np.array_equal(acc, runs[0][0])
+        for x0, x1 in zip(runs[0][1], xs):
+            assert np.array_equal(x0, x1)

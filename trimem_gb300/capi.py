@@ -108,6 +108,7 @@ _SIGS = {
     "tm_batch_energy": (_i32, [_p, _dp, _dp]),
     "tm_batch_update_repulsion": (_i32, [_p]),
     "tm_batch_hmc": (_i32, [_p, _i32, _i32, _d, _d, _d, ctypes.c_uint64, _i32, _ip]),
+    "tm_batch_set_refresh": (_i32, [_p, _i32]),
     "tm_minimize_device": (_i32, [_p, _p, _p, _i32, _i32, _d, _d, _ip, _dp, _p]),
     "tm_surrogate_create": (_i32, [_p, ctypes.POINTER(ctypes.c_float), _i64, _pp]),
     "tm_surrogate_destroy": (_i32, [_p]),
@@ -375,7 +376,12 @@ class Batch:
     def update_repulsion(self):
         check(lib().tm_batch_update_repulsion(self.h))
 
-    def hmc(self, n_steps, n_leapfrog, dt, mass=1.0, temperature=1.0, seed=0, use_graph=True):
+    def hmc(self, n_steps, n_leapfrog, dt, mass=1.0, temperature=1.0, seed=0, use_graph=True, refresh=None):
+        """n_steps HMC steps of every replica; accepted steps per replica.
+        refresh: rebuild the neighbour list after every refresh-th step
+        (0: never; None keeps the current setting, initially 1)."""
+        if refresh is not None:
+            check(lib().tm_batch_set_refresh(self.h, int(refresh)))
         acc = np.zeros(self.R, np.int32)
         check(lib().tm_batch_hmc(self.h, int(n_steps), int(n_leapfrog), float(dt), float(mass),
                                  float(temperature), int(seed), int(bool(use_graph)), _iptr(acc)))

@@ -64,6 +64,11 @@ struct tm_batch {
   int g_L = -1;
   double g_dt = 0, g_m = 0, g_T = 0;
   unsigned long long g_seed = 0;
+  NLView g_view{};  // the neighbour-list view baked into the graph's launches
+  // neighbour list rebuilt after every refresh-th HMC step (0: never), like
+  // the evaluator callback of the reference's HMC
+  int refresh = 1;
+  long long steps_done = 0;
   ~tm_batch() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
@@ -383,35 +388,50 @@ int tm_batch_update_repulsion(tm_batch* b) {
   TM_API_END
 }
 
+int tm_batch_set_refresh(tm_batch* b, int every) {
+  TM_API_BEGIN
+  if (!b || every < 0) fail(TM_ERR_ARG, "invalid argument");
+  b->refresh = every;
+  TM_API_END
+}
+
 int tm_batch_hmc(tm_batch* b, int n_steps, int n_leapfrog, double dt, double mass, double temperature,
                  uint64_t seed, int use_graph, int32_t* accepted) {
   TM_API_BEGIN
   if (!b || n_steps < 0 || n_leapfrog < 0 || !(mass > 0) || !(temperature > 0)) fail(TM_ERR_ARG, "invalid argument");
   cudaStream_t s = b->stream;
   TM_CUDA(cudaMemsetAsync(b->acc.get(), 0, sizeof(int) * b->R, s));
-  if (use_graph && n_steps > 0) {
-    bool same = b->gexec && b->g_L == n_leapfrog && b->g_dt == dt && b->g_m == mass && b->g_T == temperature &&
-                b->g_seed == seed;
-    if (!same) {
-      if (b->gexec) cudaGraphExecDestroy(b->gexec);
-      if (b->graph) cudaGraphDestroy(b->graph);
-      b->gexec = nullptr;
-      b->graph = nullptr;
-      batch_hmc_step(b, n_leapfrog, dt, mass, temperature, seed, s);  // allocations happen outside capture
-      TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < n_steps; ++k) {
+    if (use_graph) {
+      // the graph holds one step with the current neighbour-list view; a
+      // rebuild that moved or resized a buffer invalidates it
+      const NLView& v = b->en->nl.view;
+      bool same = b->gexec && b->g_L == n_leapfrog && b->g_dt == dt && b->g_m == mass &&
+                  b->g_T == temperature && b->g_seed == seed && std::memcmp(&b->g_view, &v, sizeof(NLView)) == 0;
+      if (same) {
+        TM_CUDA(cudaGraphLaunch(b->gexec, s));
+      } else {
+        if (b->gexec) cudaGraphExecDestroy(b->gexec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->gexec = nullptr;
+        b->graph = nullptr;
+        batch_hmc_step(b, n_leapfrog, dt, mass, temperature, seed, s);  // allocations happen outside capture
+        TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        batch_hmc_step(b, n_leapfrog, dt, mass, temperature, seed, s);
+        TM_CUDA(cudaStreamEndCapture(s, &b->graph));
+        TM_CUDA(cudaGraphInstantiate(&b->gexec, b->graph, 0));
+        b->g_L = n_leapfrog;
+        b->g_dt = dt;
+        b->g_m = mass;
+        b->g_T = temperature;
+        b->g_seed = seed;
+        std::memcpy(&b->g_view, &v, sizeof(NLView));
+      }
+    } else {
       batch_hmc_step(b, n_leapfrog, dt, mass, temperature, seed, s);
-      TM_CUDA(cudaStreamEndCapture(s, &b->graph));
-      TM_CUDA(cudaGraphInstantiate(&b->gexec, b->graph, 0));
-      b->g_L = n_leapfrog;
-      b->g_dt = dt;
-      b->g_m = mass;
-      b->g_T = temperature;
-      b->g_seed = seed;
-      --n_steps;
     }
-    for (int k = 0; k < n_steps; ++k) TM_CUDA(cudaGraphLaunch(b->gexec, s));
-  } else {
-    for (int k = 0; k < n_steps; ++k) batch_hmc_step(b, n_leapfrog, dt, mass, temperature, seed, s);
+    ++b->steps_done;
+    if (b->refresh > 0 && b->steps_done % b->refresh == 0) rebuild_nlist(b);
   }
   if (accepted)
     TM_CUDA(cudaMemcpyAsync(accepted, b->acc.get(), sizeof(int) * b->R, cudaMemcpyDeviceToHost, s));

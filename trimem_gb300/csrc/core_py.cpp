@@ -671,7 +671,7 @@ PYBIND11_MODULE(core, m) {
         return acc;
       },
       py::arg("mesh"), py::arg("estore"), py::arg("flip_ratio"), py::arg("seed") = py::none(),
-      py::arg("batch") = 1024);
+      py::arg("batch") = 4096);
 
   py::class_<Point>(m, "Point")
       .def("__getitem__",

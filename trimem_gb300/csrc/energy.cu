@@ -65,8 +65,9 @@ __global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__
   d3 pa = ld3(P, a), pb = ld3(P, b), pc = ld3(P, c);
   d3 eab = pb - pa, eac = pc - pa, ebc = pc - pb;
   d3 N = cross(eab, eac);
-  double nn = norm(N);
-  double inv = 1.0 / nn;
+  double n2 = dot(N, N);
+  double inv = rsqrt(n2);
+  double nn = n2 * inv;
   FaceD F;
   F.nx = N.x * inv;
   F.ny = N.y * inv;
@@ -80,24 +81,30 @@ __global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__
 }
 
 __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd, EdgeD* __restrict__ ed,
-                       double* __restrict__ ebond, EP ep, int* __restrict__ blist, int* __restrict__ bcnt) {
+                       double* __restrict__ ebond, EP ep, int* __restrict__ blist, int* __restrict__ bcnt,
+                       const double2* __restrict__ sct) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= t.ne) return;
   int4 E = t.edge[e];
   d3 pi = ld3(P, E.x), pj = ld3(P, E.y);
   d3 ev = pj - pi;
-  double l = norm(ev);
+  double l2 = dot(ev, ev);
+  double il = rsqrt(l2);
+  double l = l2 * il;
   EdgeD o;
   o.l = l;
   o.th = 0.0;
-  o.il = -1.0 / l;
+  o.il = -il;
   if (E.z >= 0 && E.w >= 0) {
     FaceD F0 = fd[E.z], F1 = fd[E.w];
     d3 n0 = mk(F0.nx, F0.ny, F0.nz), n1 = mk(F1.nx, F1.ny, F1.nz);
-    double c = fmin(1.0, fmax(-1.0, dot(n0, n1)));
-    double a = acos(c);
-    o.th = dot(cross(n0, n1), ev) >= 0.0 ? a : -a;
-    o.il = -o.il;
+    // both normals are perpendicular to the shared edge, so n0 x n1 lies
+    // along it: its projection on the unit edge is the signed sine, whose
+    // sign is the reference's sign test (n0 x n1) . e >= 0
+    double sd = dot(cross(n0, n1), ev) * il;
+    double a = angle_sc(fabs(sd), dot(n0, n1), sct);
+    o.th = sd >= 0.0 ? a : -a;
+    o.il = il;
   }
   // flat-bottom edge penalty: above the flat bottom inline (products only);
   // edges below it (exp and divisions in FP64) go to a list handled by
@@ -247,6 +254,8 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
     int fcur = slot_face(sc.y);
     if (fcur >= 0) Fc = fd[fcur];
     const double gV6 = gV * (1.0 / 6.0);
+    const double ri2 = ri * ri;
+    double rk2 = rk * rk, rj2 = rj * rj;
     // scalar multiples of face normals are summed per face: the dihedral
     // term of edge (i, j) reaches the normal of the next face, so its part
     // is carried to the next slot (the last one wraps to the first face)
@@ -264,11 +273,15 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
         double ck = cot_at(Fc, ci == 0 ? 2 : ci - 1);
         d3 n = mk(Fc.nx, Fc.ny, Fc.nz);
         if (m == 0) n0 = n;
-        // face (i, j, k): area and volume terms
-        double alpha = gA - kb23 * (ri * ri + rj * rj + rk * rk);
+        // face (i, j, k): area and volume terms, (alpha/2) n x (x_k - x_j)
+        // + (gV/6) x_j x x_k = ((alpha/2) n + (gV/6) x_j) x (x_k - x_j)
+        double alpha = gA - kb23 * (ri2 + rj2 + rk2);
         if (ep.btype == 1) alpha += ep.kt * 2.0 * (Fc.A / ep.a0 - 1.0) / ep.a0;
-        acc += (0.5 * alpha) * cross(n, xk - xj);
-        acc += gV6 * cross(xj, xk);
+        d3 u = (0.5 * alpha) * n + gV6 * xj;
+        d3 e = xk - xj;
+        acc.x = fma(u.y, e.z, fma(-u.z, e.y, acc.x));
+        acc.y = fma(u.z, e.x, fma(-u.x, e.z, acc.y));
+        acc.z = fma(u.x, e.y, fma(-u.y, e.x, acc.z));
         // edge (i, j): length and dihedral terms
         EdgeD E = ed[sc.z];
         double w = hgC + kb * (ri + rj);
@@ -287,11 +300,13 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
       carry = carry_next;
       xk = xj;
       rk = rj;
+      rk2 = rj2;
       sc = sn;
       fcur = fnx;
       Fc = Fn;
       xj = ld3(P, sn.x);
       rj = rho[sn.x];
+      rj2 = rj * rj;
     }
     acc += carry * n0;  // the last edge's part on the first face
   }
@@ -359,7 +374,7 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
   int* blist = e->slow.get() + std::max(m->nv, 1) + 1;
   int* bcnt = blist + std::max(m->ne, 1);
   TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
-  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep, blist, bcnt);
+  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep, blist, bcnt, e->sct.get());
   TM_LAUNCH();
   if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(P, t, ed, e->ebond.get(), ep, blist, bcnt);
   TM_LAUNCH();
@@ -462,6 +477,14 @@ int tm_energy_create(tm_mesh* m, const tm_params* p, tm_energy** out) {
   TM_CUDA(cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking));
   TM_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
   TM_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+  {
+    std::vector<double2> sc(tmg::TM_SCT_N);
+    for (int k = 0; k < tmg::TM_SCT_N; ++k) sc[k] = make_double2(std::sin(k / 128.0), std::cos(k / 128.0));
+    e->sct.ensure(tmg::TM_SCT_N);
+    TM_CUDA(cudaMemcpyAsync(e->sct.get(), sc.data(), sizeof(double2) * tmg::TM_SCT_N, cudaMemcpyHostToDevice,
+                            e->stream));
+    TM_CUDA(cudaStreamSynchronize(e->stream));
+  }
   m->upload_points(e->stream);
   tmg::nlist_make(&e->nl, m, e->prm, m->d_pts.get(), e->stream);
   // initial properties: the reference properties are still unset (zero) and
@@ -723,7 +746,7 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   k_face<<<nfb, 256, 0, s>>>(t, d_points, fd, pos32);
   TM_LAUNCH();
   TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
-  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, d_points, fd, ed, ebond, ep, blist, bcnt);
+  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, d_points, fd, ed, ebond, ep, blist, bcnt, e->sct.get());
   TM_LAUNCH();
   if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(d_points, t, ed, ebond, ep, blist, bcnt);
   TM_LAUNCH();

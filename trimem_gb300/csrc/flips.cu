@@ -225,6 +225,45 @@ __device__ __forceinline__ double flip_energy(const FlipE& f, const double* p) {
   return tot;
 }
 
+// Float filter of the Metropolis test E(props - dp) - E(props) <= -log u:
+// the energy change is written without cancellation (quadratic penalties
+// as k t (t - 2 d0), d0 = props/ref - 1 of the current state, t = dp/ref;
+// the linear terms as -k dp) and evaluated from float copies.  A decision
+// is taken only when it is farther from the threshold than a bound on the
+// float error (relative 1e-4 of the terms' magnitudes), the FP64 rounding
+// of the exact test (1e-12 of |E|) and the float rounding of -log u;
+// otherwise (rare) the exact FP64 test decides.
+struct FlipEF {
+  float irA, irV, irC, ka, kv, kc, kt, kr, kb;
+};
+// per-state constants of the filter: d0 of area, volume, curvature and the
+// FP64 rounding bound
+__device__ __forceinline__ void filter_state(const FlipE& f, const double* p, float* q) {
+  double da = p[0] * f.irA - 1.0, dv = p[1] * f.irV - 1.0, dc = p[2] * f.irC - 1.0;
+  double mag = fabs(f.ka * da * da) + fabs(f.kv * dv * dv) + fabs(f.kc * dc * dc) + fabs(f.kt * p[4]) +
+               fabs(f.kr * p[5]) + fabs(f.kb * p[3]);
+  q[0] = (float)da;
+  q[1] = (float)dv;
+  q[2] = (float)dc;
+  q[3] = (float)(1e-12 * mag);
+}
+// 1 accept, 0 reject, -1 too close to call in float
+__device__ __forceinline__ int metro_filter(const FlipEF& g, const float* q, const float* f8) {
+  float ta = f8[0] * g.irA, tv = f8[1] * g.irV, tc = f8[2] * g.irC;
+  float xa = g.ka * ta * (ta - 2.0f * q[0]);
+  float xv = g.kv * tv * (tv - 2.0f * q[1]);
+  float xc = g.kc * tc * (tc - 2.0f * q[2]);
+  float xl = g.kt * f8[4] + g.kr * f8[5] + g.kb * f8[3];
+  float S = fabsf(g.ka * ta) * (fabsf(ta) + 2.0f * fabsf(q[0])) + fabsf(g.kv * tv) * (fabsf(tv) + 2.0f * fabsf(q[1])) +
+            fabsf(g.kc * tc) * (fabsf(tc) + 2.0f * fabsf(q[2])) + fabsf(g.kt * f8[4]) + fabsf(g.kr * f8[5]) +
+            fabsf(g.kb * f8[3]);
+  float m = 1e-4f * S + q[3] + 1e-6f * fabsf(f8[6]);
+  float d = ((xa + xv) + xc - xl) - f8[6];
+  if (d < -m) return 1;
+  if (d > m) return 0;
+  return -1;  // also for NaN and overflow
+}
+
 __global__ void k_flip_init(FlipE fe, const Globals* g, long long nflips, FlipState* st) {
   if (threadIdx.x || blockIdx.x) return;
   for (int k = 0; k < 6; ++k) st->props[k] = g->props[k];
@@ -319,6 +358,67 @@ __device__ double repulsion_of(int v, d3 xv, const double* P, const EP& ep, cons
   return pot;
 }
 
+// Repulsion value of vertex v at xv from its near row, computed by the 8
+// lanes w8 of one variant (gmask: those lanes): each lane tests every 8th
+// entry (distance, build cell, exclusion on the given rules) and the
+// accepted pairs go to shared memory (key: the reference's visiting order,
+// as in visit_near); each lane evaluates the pair of its rank and lane 0
+// adds the values in rank order: the same sum, bit for bit, as the
+// sequential walk of visit_near.  Returns false (on every lane) when the
+// rows are stale or hold more than NEAR_HITS accepted pairs.
+template <class X>
+__device__ bool repulsion_near8(int v, d3 xv, const double* P, const EP& ep, const NLView& nl, const X& excl,
+                                int w8, unsigned gmask, long long* skey, double* sval, double* sterm,
+                                double* pot) {
+  if (!(nl.kind == 0 && nl.nent && nl.nflag[0] == 0 && nl.nflag[1] == 0)) return false;
+  const double lc1 = ep.rlc1;
+  PairTest pt = make_pair_test(nl, v, lc1, ep.rT);
+  int co[3];
+  in_build_cell(nl, v, xv, co);
+  const int* row = nl.nent + (size_t)v * TM_NEAR_CAP;
+  const int n = nl.ncnt[v];
+  const unsigned below = (1u << (threadIdx.x & 31)) - 1u;
+  int total = 0;
+  for (int q0 = 0; q0 < n; q0 += 8) {
+    const int q = q0 + w8;
+    bool acc = false;
+    long long key = 0;
+    double sq = 0.0;
+    if (q < n) {
+      int j = row[q] & 0x7fffffff;
+      d3 pj;
+      if (pair_within(pt, nl, P, xv, j, &pj, &sq)) {
+        int ox = nl.bcoord[3 * j] - co[0], oy = nl.bcoord[3 * j + 1] - co[1], oz = nl.bcoord[3 * j + 2] - co[2];
+        acc = ox >= -1 && ox <= 1 && oy >= -1 && oy <= 1 && oz >= -1 && oz <= 1 && !(nl.excl > 0 && excl(v, j));
+        key = ((long long)((ox + 1) * 9 + (oy + 1) * 3 + (oz + 1)) << 32) | (long long)j;
+      }
+    }
+    const unsigned b = __ballot_sync(gmask, acc);
+    const int pos = total + __popc(b & below);
+    if (acc && pos < NEAR_HITS) {
+      skey[pos] = key;
+      sval[pos] = sq;
+    }
+    total += __popc(b);
+  }
+  if (total > NEAR_HITS) return false;
+  __syncwarp(gmask);
+  if (w8 < total) {
+    const long long k = skey[w8];
+    int rank = 0;
+    for (int h = 0; h < total; ++h) rank += skey[h] < k ? 1 : 0;
+    const double l = __dsqrt_rn(sval[w8]);
+    sterm[rank] = exp(l / (l - lc1)) / ipow(l, ep.rr);
+  }
+  __syncwarp(gmask);
+  if (w8 == 0) {
+    double acc = 0.0;
+    for (int h = 0; h < total; ++h) acc += sterm[h];
+    *pot = acc;
+  }
+  return true;
+}
+
 // One block of 64 threads per slot: 8 variants (quad vertex sub & 3, before
 // the flip for sub < 4, after it otherwise) x 8 workers.  The ring of each
 // variant goes to shared memory, the workers compute the per-position terms
@@ -328,11 +428,14 @@ __device__ double repulsion_of(int v, d3 xv, const double* P, const EP& ep, cons
 __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
                                               const long long* win, const unsigned char* winner, const int* limit,
                                               const double* P, EP ep, FlipE fe, NLView nl, double* part,
-                                              unsigned char* okf, double* dpn) {
+                                              unsigned char* okf, double* dpn, float* dpf,
+                                              const double2* __restrict__ sct) {
   __shared__ int sr[8][TM_MAXVAL + 1];
   __shared__ unsigned char sf[8][TM_MAXVAL + 1];
   __shared__ int sn[8];
   __shared__ double term[8][TM_MAXVAL + 1][4];
+  __shared__ long long rkey[8][NEAR_HITS];
+  __shared__ double rval[8][NEAR_HITS], rterm[8][NEAR_HITS];
   const int s = blockIdx.x;
   const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
   if (s >= st->W) return;
@@ -340,6 +443,7 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
     if (threadIdx.x == 0) {
       okf[s] = 0;
       dpn[8 * (size_t)s + 7] = 0.0;
+      dpf[8 * (size_t)s + 7] = 0.0f;
     }
     return;
   }
@@ -347,7 +451,10 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
   const bool ok = flip_ok(t, e);
   if (threadIdx.x == 0) {
     okf[s] = ok ? 1 : 0;
-    if (!ok) dpn[8 * (size_t)s + 7] = 0.0;
+    if (!ok) {
+      dpn[8 * (size_t)s + 7] = 0.0;
+      dpf[8 * (size_t)s + 7] = 0.0f;
+    }
   }
   if (!ok) return;
   const Quad q = quad_of(t, e);
@@ -374,23 +481,30 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
       int mn = m + 1 == n ? 0 : m + 1;
       d3 xj = ld3(P, j), xk = ld3(P, k);
       d3 ev = xj - xv;
-      double el = norm(ev);
+      double l2 = dot(ev, ev);
+      double il = rsqrt(l2);
+      double el = l2 * il;
       d3 N0 = cross(ev, xk - xv);
-      double fa = norm(N0) / 2;
+      double n0s = dot(N0, N0);
+      double r0 = rsqrt(n0s);
+      double fa = 0.5 * (n0s * r0);
       double th = 0.0;
       if (sf[sub][mn]) {
         d3 xn = ld3(P, sr[sub][mn]);
         d3 N1 = cross(xn - xv, ev);
-        double den = norm(N0) * norm(N1);
-        if (den != 0.0) {
-          double c = fmin(1.0, fmax(-1.0, dot(N0, N1) / den));
-          double a = acos(c);
-          th = dot(cross(N0, N1), ev) >= 0.0 ? a : -a;
+        double n1s = dot(N1, N1);
+        if (n0s != 0.0 && n1s != 0.0) {
+          // dihedral angle from cosine and signed sine (N0 x N1 lies along
+          // the edge; its sign is the reference's test (N0 x N1) . e >= 0)
+          double inv = r0 * rsqrt(n1s);
+          double sd = dot(cross(N0, N1), ev) * (inv * il);
+          double a = angle_sc(fabs(sd), dot(N0, N1) * inv, sct);
+          th = sd >= 0.0 ? a : -a;
         }
       }
       tc = 0.5 * el * th;
       ta = fa;
-      tv = dot(cross(xj, xk), xv) / 6;
+      tv = dot(cross(xj, xk), xv) * (1.0 / 6.0);
       if (ep.btype == 0) {
         int r = ep.r;
         if (el > ep.lc0)
@@ -427,14 +541,23 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
     o[2] = C;
     o[3] = 2 * C * C / A;
     o[4] = T;
-  } else if (w8 == 1) {
+  }
+  // repulsion: the near row shared by the variant's 8 lanes, else one lane
+  // walks the cell list
+  {
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);
+    double pot = 0.0;
+    bool near;
     if (sub < 4) {
       TableExclW x{t, nl.excl};
-      o[5] = repulsion_of(v, xv, P, ep, nl, x);
+      near = repulsion_near8(v, xv, P, ep, nl, x, w8, gmask, rkey[sub], rval[sub], rterm[sub], &pot);
+      if (!near && w8 == 0) pot = repulsion_of(v, xv, P, ep, nl, x);
     } else {
       OverlayExcl x{t, q, nl.excl};
-      o[5] = repulsion_of(v, xv, P, ep, nl, x);
+      near = repulsion_near8(v, xv, P, ep, nl, x, w8, gmask, rkey[sub], rval[sub], rterm[sub], &pot);
+      if (!near && w8 == 0) pot = repulsion_of(v, xv, P, ep, nl, x);
     }
+    if (w8 == 0) o[5] = pot;
   }
   __syncthreads();
   // the property change of the flip (before - after, in the summation orders
@@ -454,6 +577,8 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
     double trial[6];
     for (int k = 0; k < 6; ++k) trial[k] = st->props[k] - o8[k];
     o8[7] = flip_energy(fe, trial) - st->e0 <= o8[6] ? 2.0 : 1.0;
+    float* f8 = dpf + 8 * (size_t)s;
+    for (int k = 0; k < 8; ++k) f8[k] = (float)o8[k];
   }
 }
 
@@ -466,9 +591,11 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
 // compacted in order for the next window.
 constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread
 __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsigned char* winner,
-                                             const double* dpn, FlipE fe, FlipState* st, const int* limit,
-                                             unsigned char* accepted, long long* pend) {
+                                             const double* dpn, const float* dpf, FlipE fe, FlipEF fg,
+                                             FlipState* st, const int* limit, unsigned char* accepted,
+                                             long long* pend) {
   __shared__ double sP[6], se0;
+  __shared__ float sq[4];
   __shared__ int sfirst, sstart, sacc;
   __shared__ int scan[MB];
   const int tid = threadIdx.x;
@@ -479,6 +606,7 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
     se0 = st->e0;
     sacc = st->acc;
     sstart = 0;
+    filter_state(fe, sP, sq);
   }
   for (int k = 0; k < MS; ++k) {
     int s = tid * MS + k;
@@ -492,15 +620,21 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
     for (int k = 0; k < MS; ++k) {
       int s = k * MB + tid;  // strided: every thread has a slot in small windows
       if (s < start || s >= W) continue;
-      const double* o8 = dpn + 8 * (size_t)s;
-      if (o8[7] == 0.0) continue;
+      const float* f8 = dpf + 8 * (size_t)s;
+      if (f8[7] == 0.0f) continue;
       bool acc_s;
       if (round == 0) {  // decided by k_delta on this same state
-        acc_s = o8[7] == 2.0;
+        acc_s = f8[7] == 2.0f;
       } else {
-        double trial[6];
-        for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
-        acc_s = flip_energy(fe, trial) - se0 <= o8[6];
+        int fd = metro_filter(fg, sq, f8);
+        if (fd >= 0) {
+          acc_s = fd == 1;
+        } else {
+          const double* o8 = dpn + 8 * (size_t)s;
+          double trial[6];
+          for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
+          acc_s = flip_energy(fe, trial) - se0 <= o8[6];
+        }
       }
       if (acc_s) {
         atomicMin(&sfirst, s);
@@ -517,6 +651,7 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
       double en = flip_energy(fe, trial);
       for (int q = 0; q < 6; ++q) sP[q] = trial[q];
       se0 = en;
+      filter_state(fe, sP, sq);
       sacc += 1;
       accepted[first] = 1;
       sstart = first + 1;
@@ -624,12 +759,17 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   NLView nlv = e->nl.view;
   nlv.pos32 = e->pos32.get();  // written by the evaluation above
   TopoW t = m->topo_w();
-  DevBuf<int> owner;
-  DevBuf<long long> win, pend;
-  DevBuf<unsigned char> winner, okf, acc;
-  DevBuf<double> part;
-  DevBuf<FlipState> st;
-  DevBuf<int> limit;
+  // workspace of the energy handle: no allocation per sweep
+  DevBuf<int>& owner = e->fw_owner;
+  DevBuf<int>& limit = e->fw_limit;
+  DevBuf<long long>& win = e->fw_win;
+  DevBuf<long long>& pend = e->fw_pend;
+  DevBuf<unsigned char>& winner = e->fw_winner;
+  DevBuf<unsigned char>& okf = e->fw_okf;
+  DevBuf<unsigned char>& acc = e->fw_acc;
+  DevBuf<double>& part = e->fw_part;
+  DevBuf<double>& dpn = e->fw_dpn;
+  DevBuf<float>& dpf = e->fw_dpf;
   owner.ensure(ne);
   win.ensure(MAXB);
   pend.ensure(MAXB);
@@ -637,14 +777,17 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   okf.ensure(MAXB);
   acc.ensure(MAXB);
   part.ensure(64 * (size_t)MAXB);
-  DevBuf<double> dpn;
   dpn.ensure(8 * (size_t)MAXB);
-  st.ensure(1);
+  dpf.ensure(8 * (size_t)MAXB);
+  e->fw_state.ensure(sizeof(FlipState));
   limit.ensure(1);
+  FlipState* st = reinterpret_cast<FlipState*>(e->fw_state.get());
   k_owner_init<<<nblk(ne, 256), 256, 0, s>>>(owner.get(), ne);
   TM_LAUNCH();
   FlipE fe{1.0 / ep.refA, 1.0 / ep.refV, 1.0 / ep.refC, ep.ka, ep.kv, ep.kc, ep.kt, ep.kr, ep.kb};
-  k_flip_init<<<1, 1, 0, s>>>(fe, e->glob.get(), nflips, st.get());
+  FlipEF fg{(float)fe.irA, (float)fe.irV, (float)fe.irC, (float)fe.ka, (float)fe.kv,
+            (float)fe.kc, (float)fe.kt, (float)fe.kr, (float)fe.kb};
+  k_flip_init<<<1, 1, 0, s>>>(fe, e->glob.get(), nflips, st);
   TM_LAUNCH();
   // windows are queued in groups without host round trips; W and the window
   // number live on the device, and a window after the last one is empty
@@ -654,23 +797,23 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   FlipState hs;
   for (;;) {
     for (int k = 0; k < GROUP; ++k) {
-      k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st.get(), win.get(), limit.get());
+      k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st, win.get(), limit.get());
       TM_LAUNCH();
-      k_claim<<<nblk(4L * B, 64), 64, 0, s>>>(t, st.get(), seed, win.get(), owner.get());
+      k_claim<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, seed, win.get(), owner.get());
       TM_LAUNCH();
-      k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st.get(), mode, seed, win.get(), owner.get(), winner.get(),
+      k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, mode, seed, win.get(), owner.get(), winner.get(),
                                              limit.get());
       TM_LAUNCH();
-      k_delta<<<B, 64, 0, s>>>(t, st.get(), seed, win.get(), winner.get(), limit.get(), P, ep, fe, nlv,
-                               part.get(), okf.get(), dpn.get());
+      k_delta<<<B, 64, 0, s>>>(t, st, seed, win.get(), winner.get(), limit.get(), P, ep, fe, nlv,
+                               part.get(), okf.get(), dpn.get(), dpf.get(), e->sct.get());
       TM_LAUNCH();
-      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), fe, st.get(), limit.get(), acc.get(),
-                               pend.get());
+      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(),
+                               acc.get(), pend.get());
       TM_LAUNCH();
-      k_commit<<<B, 32, 0, s>>>(t, seed, win.get(), acc.get(), st.get());
+      k_commit<<<B, 32, 0, s>>>(t, seed, win.get(), acc.get(), st);
       TM_LAUNCH();
     }
-    TM_CUDA(cudaMemcpyAsync(&hs, st.get(), sizeof(FlipState), cudaMemcpyDeviceToHost, s));
+    TM_CUDA(cudaMemcpyAsync(&hs, st, sizeof(FlipState), cudaMemcpyDeviceToHost, s));
     TM_CUDA(cudaStreamSynchronize(s));
     if (hs.status) fail(TM_ERR_TOPOLOGY, "flip produced a valence above TM_MAXVAL");
     // slot 0 of a window always owns its patch, so every window decides at

@@ -30,6 +30,25 @@ constexpr int VB = 256;  // threads per block of k_vertex (fixed: it sets the re
 
 __device__ __forceinline__ double cot_at(const FaceD& F, int c) { return c == 0 ? F.c0 : (c == 1 ? F.c1 : F.c2); }
 
+// Unsigned angle theta in [0, pi] from s = sin(theta) >= 0 and
+// c = cos(theta) of two unit vectors: a float atan2 estimate rounded to the
+// grid t0 = k/128, whose sine and cosine sct holds (sct[k] = {sin, cos}),
+// then theta = t0 + asin(x) with x = s cos t0 - c sin t0 = sin(theta - t0).
+// |x| <= 1/256 plus the float error, so asin(x) = x + x^3/6 + 3 x^5/40 is
+// exact to below 1e-18; s^2 + c^2 = 1 within rounding enters x only at
+// that order.  Unlike acos(c) it keeps full relative accuracy for small
+// angles.  NaN inputs give NaN (the grid index is clamped).
+__device__ __forceinline__ double angle_sc(double s, double c, const double2* __restrict__ sct) {
+  float tf = atan2f((float)s, (float)c);
+  int k = __float2int_rn(tf * 128.0f);
+  k = min(max(k, 0), TM_SCT_N - 1);
+  double2 g = __ldg(sct + k);
+  double x = s * g.y - c * g.x;
+  double x2 = x * x;
+  double p = x2 * fma(x2, 3.0 / 40.0, 1.0 / 6.0);
+  return fma(x, p, x) + k * (1.0 / 128.0);
+}
+
 // ---- repulsion (src/mesh_repulsion.h:28-79 over the neighbour list) -------
 __device__ __forceinline__ unsigned long long cell_hash(long long key) {
   unsigned long long z = (unsigned long long)key + 0x9E3779B97F4A7C15ull;

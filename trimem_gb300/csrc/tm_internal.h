@@ -92,6 +92,9 @@ struct NLGeom {
   long long stride[3];
 };
 constexpr int TM_NEAR_CAP = 48;  // near-row capacity per vertex
+// grid of dihedral angles k/128, k < TM_SCT_N (covers [0, pi]), whose sine
+// and cosine each energy handle keeps on the device
+constexpr int TM_SCT_N = 404;
 
 struct NLView {
   int kind;  // 0 cell list, 1 Verlet list
@@ -208,6 +211,13 @@ struct tm_energy {
   tmg::DevBuf<int> slow;  // vertices that left their build cell (+ count)
   tmg::DevBuf<float> pos32, poslo;
   tmg::DevBuf<tmg::Globals> glob;
+  tmg::DevBuf<double2> sct;  // {sin, cos}(k / 128), k < TM_SCT_N
+  // flip-sweep workspace, kept between sweeps (grown on demand)
+  tmg::DevBuf<int> fw_owner, fw_limit;
+  tmg::DevBuf<long long> fw_win, fw_pend;
+  tmg::DevBuf<unsigned char> fw_winner, fw_okf, fw_acc, fw_state;
+  tmg::DevBuf<double> fw_part, fw_dpn;
+  tmg::DevBuf<float> fw_dpf;
   cudaStream_t stream = nullptr;
   // second stream: the repulsion pass runs there, concurrent with the
   // edge kernels, between a fork and a join event

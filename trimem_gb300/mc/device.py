@@ -22,7 +22,7 @@ class DeviceChain:
     of shape (n_vertices, 3)) of ``mesh``/``energy`` (capi handles)."""
 
     def __init__(self, mesh, energy, x, mass=1.0, dt=5e-5, n_leapfrog=20, temperature=1.0, flip_ratio=0.2,
-                 flip_mode=1, flip_batch=1024, refresh=1, seed=0, stream=None, force=None):
+                 flip_mode=1, flip_batch=4096, refresh=1, seed=0, stream=None, force=None):
         from .. import capi
 
         self.capi = capi
