@@ -64,18 +64,21 @@ def config(extra=None):
 
 
 def read_traffic():
-    """DRAM bytes per launch of each evaluation stage from the committed ncu
-    summary (profiles/eval_kernels_L7_fp64_sections.md)."""
-    out = {}
+    """DRAM bytes per launch of each evaluation stage, and the FP64 pipe
+    activity of its main kernel, from the committed ncu summary
+    (profiles/eval_kernels_L7_fp64_sections.md)."""
+    out, fp64 = {}, {}
     path = os.path.join(ROOT, "profiles", "eval_kernels_L7_fp64_sections.md")
     try:
         for line in open(path):
             parts = line.split()
             if len(parts) == 2 and parts[0].startswith("k_") and parts[1].isdigit():
                 out[parts[0]] = int(parts[1])
-    except OSError:
+            if len(parts) == 3 and parts[0] == "fp64" and parts[1].startswith("k_"):
+                fp64[parts[1]] = float(parts[2])
+    except (OSError, ValueError):
         pass
-    return out
+    return out, fp64
 
 
 def read_peaks():
@@ -528,7 +531,8 @@ def main():
     hbm = hbm or 6800.0
     dname = names[dom]
     achieved = kbytes[dname] / (kms[dom] * 1e-3) / 1e9
-    traffic = read_traffic().get(dname)
+    traffic_all, fp64_active = read_traffic()
+    traffic = traffic_all.get(dname)
     # whole evaluation: 132 algorithmic bytes per vertex
     eval_bytes = 132 * V
     roofline = {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
@@ -537,7 +541,12 @@ def main():
                 "eval_ms_cold": round(float(kms[4]), 5),
                 "eval_algorithmic_bytes": eval_bytes,
                 "eval_frac": round(eval_bytes / (kms[4] * 1e-3) / 1e9 / hbm, 5),
-                "algorithmic_bytes": kbytes[dname]}
+                "algorithmic_bytes": kbytes[dname],
+                # what bounds the FP64 stencils instead of HBM: FP64 issue
+                "issue_bound": {"pipe": "fp64", "kernel": dname,
+                                "pipe_active_frac": (round(fp64_active[dname] / 100.0, 3)
+                                                     if dname in fp64_active else None),
+                                "source": "ncu sm__pipe_fp64_cycles_active, profiles/eval_kernels_L7_fp64_sections.md"}}
 
     # ---- FP32-stencil variant: speed and error against FP64 ---------------
     g64 = g.clone()

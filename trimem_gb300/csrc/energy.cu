@@ -130,6 +130,7 @@ __global__ void k_bond_short(const double* __restrict__ P, Topo t, EdgeD* __rest
   }
 }
 
+constexpr int VG = 6;  // ring slots loaded together by k_vertex
 template <bool VPROPS>
 __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__ fd, const EdgeD* __restrict__ ed,
                                               const double* __restrict__ ebond, const double* __restrict__ reppot,
@@ -142,15 +143,15 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__
   if (v < t.nv) {
     int d = t.val[v];
     double A = 0, V = 0, LT = 0, T = 0;
-    // slots in groups of four: all loads of a group are issued before the
-    // sums, which keep the slot order
-    for (int m0 = 0; m0 < d; m0 += 4) {
-      int4 s[4];
+    // slots in groups of six (one group at the usual valence): all loads of
+    // a group are issued before the sums, which keep the slot order
+    for (int m0 = 0; m0 < d; m0 += VG) {
+      int4 s[VG];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) s[k] = m0 + k < d ? t.slot[(size_t)(m0 + k) * t.nv + v] : make_int4(0, -1, 0, 0);
-      double fa[4], fv[4], lt[4], tb[4];
+      for (int k = 0; k < VG; ++k) s[k] = m0 + k < d ? t.slot[(size_t)(m0 + k) * t.nv + v] : make_int4(0, -1, 0, 0);
+      double fa[VG], fv[VG], lt[VG], tb[VG];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < VG; ++k) {
         int f = slot_face(s[k].y);
         fa[k] = fv[k] = lt[k] = tb[k] = 0.0;
         if (f >= 0) {
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__
         }
       }
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < VG; ++k) {
         if (slot_face(s[k].y) < 0) continue;
         A += fa[k];
         V += fv[k];

@@ -82,6 +82,7 @@ __device__ __forceinline__ double flip_u_of(unsigned long long seed, long long p
 struct FlipState {
   double props[8];
   double e0;
+  float sq[4];  // float-filter constants of props (filter_state)
   long long next_new;  // first proposal not yet in a window
   long long nn_next;   // next_new after the current window (committed by k_metro)
   long long nflips;
@@ -257,7 +258,7 @@ __device__ __forceinline__ int metro_filter(const FlipEF& g, const float* q, con
   float S = fabsf(g.ka * ta) * (fabsf(ta) + 2.0f * fabsf(q[0])) + fabsf(g.kv * tv) * (fabsf(tv) + 2.0f * fabsf(q[1])) +
             fabsf(g.kc * tc) * (fabsf(tc) + 2.0f * fabsf(q[2])) + fabsf(g.kt * f8[4]) + fabsf(g.kr * f8[5]) +
             fabsf(g.kb * f8[3]);
-  float m = 1e-4f * S + q[3] + 1e-6f * fabsf(f8[6]);
+  float m = 1e-4f * S + q[3] + 1e-6f * fabsf(f8[6]) + 2e-7f;  // f8[6]: -log u in float
   float d = ((xa + xv) + xc - xl) - f8[6];
   if (d < -m) return 1;
   if (d > m) return 0;
@@ -268,6 +269,7 @@ __global__ void k_flip_init(FlipE fe, const Globals* g, long long nflips, FlipSt
   if (threadIdx.x || blockIdx.x) return;
   for (int k = 0; k < 6; ++k) st->props[k] = g->props[k];
   st->e0 = flip_energy(fe, st->props);
+  filter_state(fe, st->props, st->sq);
   st->next_new = 0;
   st->nn_next = 0;
   st->nflips = nflips;
@@ -425,19 +427,20 @@ __device__ bool repulsion_near8(int v, d3 xv, const double* P, const EP& ep, con
 // of vertex_properties (src/mesh_properties.cpp:12-49) in parallel, and one
 // worker sums them in ring order while
 // another computes the repulsion.
-__global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
+__global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
                                               const long long* win, const unsigned char* winner, const int* limit,
-                                              const double* P, EP ep, FlipE fe, NLView nl, double* part,
-                                              unsigned char* okf, double* dpn, float* dpf,
+                                              const double* P, EP ep, FlipE fe, FlipEF fg, NLView nl,
+                                              double* part, unsigned char* okf, double* dpn, float* dpf,
                                               const double2* __restrict__ sct) {
   __shared__ int sr[8][TM_MAXVAL + 1];
   __shared__ unsigned char sf[8][TM_MAXVAL + 1];
   __shared__ int sn[8];
-  __shared__ double term[8][TM_MAXVAL + 1][4];
   __shared__ long long rkey[8][NEAR_HITS];
   __shared__ double rval[8][NEAR_HITS], rterm[8][NEAR_HITS];
   const int s = blockIdx.x;
   const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
+  const int gbase = threadIdx.x & 24;            // warp lane of the variant's lane 0
+  const unsigned gmask = 0xffu << gbase;         // the variant's 8 lanes
   if (s >= st->W) return;
   if (s >= *limit || !winner[s]) {
     if (threadIdx.x == 0) {
@@ -459,24 +462,129 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
   if (!ok) return;
   const Quad q = quad_of(t, e);
   const int v = quad_vertex(q, sub & 3);
-  if (w8 == 0) {
-    Ring R;
-    if (sub < 4)
-      load_ring(t, v, R);
-    else
-      ring_after(t, q, v, R);
-    sn[sub] = R.n;
-    for (int m = 0; m < R.n; ++m) {
-      sr[sub][m] = R.r[m];
-      sf[sub][m] = R.f[m] ? 1 : 0;
+  // ring of the variant, loaded by its 8 lanes (slot m by lane m mod 8);
+  // after the virtual flip (ring_after): va0 / vb0 lose vb0 / va0, va1 / vb1
+  // gain vb1 / va1 right before vb0 / va0
+  {
+    const int n0 = t.val[v];
+    int x = -1, y = -1;
+    if (sub >= 4) {
+      if (v == q.va0) x = q.vb0;
+      else if (v == q.vb0) x = q.va0;
+      else if (v == q.va1) x = q.vb0, y = q.vb1;
+      else x = q.va0, y = q.va1;
+    }
+    int rr[4];
+    bool ff[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int m = w8 + 8 * i;
+      rr[i] = -1;
+      ff[i] = false;
+      if (m < n0) {
+        int4 sl = t.slot[(size_t)m * t.nv + v];
+        rr[i] = sl.x;
+        ff[i] = sl.y != -1;
+      }
+    }
+    int p = n0;  // position of x (n0: absent)
+    if (x >= 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const unsigned b = __ballot_sync(gmask, rr[i] == x && w8 + 8 * i < n0) >> gbase;
+        if (b && p == n0) p = 8 * i + __ffs(b) - 1;
+      }
+    }
+    const bool ins = y >= 0;
+    const int n = x < 0 ? n0 : (ins ? n0 + 1 : (p < n0 ? n0 - 1 : n0));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int m = w8 + 8 * i;
+      if (m >= n0) continue;
+      int dst = m;
+      if (x >= 0 && m >= p) {
+        if (ins) dst = m + 1;
+        else if (m == p) continue;
+        else dst = m - 1;
+      }
+      sr[sub][dst] = rr[i];
+      sf[sub][dst] = ff[i] ? 1 : 0;
+    }
+    if (w8 == 0) {
+      if (ins) {
+        sr[sub][p] = y;
+        sf[sub][p] = 1;
+      }
+      sn[sub] = n;
     }
   }
   __syncthreads();
   const int n = sn[sub];
   const d3 xv = ld3(P, v);
-  for (int m = w8; m < n; m += 8) {
-    double tc = 0.0, ta = 0.0, tv = 0.0, tt = 0.0;
-    if (sf[sub][m]) {
+  // per ring position m (face (v, r_m, r_m-1), edge (v, r_m)): half edge
+  // length x angle, face area, face volume, bond.  With n <= 8 every lane
+  // holds one position and the normal of the next face comes from the next
+  // lane (the same cross product: (x_r(m+1) - x_v) x (x_r(m) - x_v)).
+  double sc = 0.0, sa = 0.0, sv = 0.0, stt = 0.0;
+  auto terms = [&](d3 xj, d3 xk, d3 ev, double el, double il, double n0s, double r0, const d3& N0, bool have1,
+                   const d3& N1, double n1s, double r1) {
+    double th = 0.0;
+    if (have1 && n0s != 0.0 && n1s != 0.0) {
+      // dihedral angle from cosine and signed sine (N0 x N1 lies along the
+      // edge; its sign is the reference's test (N0 x N1) . e >= 0)
+      double inv = r0 * r1;
+      double sd = dot(cross(N0, N1), ev) * (inv * il);
+      double a = angle_sc(fabs(sd), dot(N0, N1) * inv, sct);
+      th = sd >= 0.0 ? a : -a;
+    }
+    double fa = 0.5 * (n0s * r0);
+    double tt = 0.0;
+    if (ep.btype == 0) {
+      int r = ep.r;
+      if (el > ep.lc0)
+        tt = ipow((double)r, r + 1) * ipow(el - ep.lc0, r);
+      else if (el < ep.lc1)
+        tt = exp(el / (el - ep.lc1)) / ipow(el, r);
+    } else {
+      double qa = fa / ep.a0 - 1.0;
+      tt = qa * qa;
+    }
+    sc += 0.5 * el * th;
+    sa += fa;
+    sv += dot(cross(xj, xk), xv) * (1.0 / 6.0);
+    stt += tt;
+  };
+  if (n <= 8) {
+    // lanes past the ring and positions without a face compute nothing; the
+    // next face's normal is used only where that face exists, and then its
+    // lane has computed it
+    const int m = w8 < n ? w8 : 0;
+    const int mn = m + 1 == n ? 0 : m + 1;
+    const bool act = w8 < n && sf[sub][m];
+    d3 xj = mk(0, 0, 0), xk = xj, ev = xj, N0 = xj;
+    double il = 0.0, el = 0.0, n0s = 0.0, r0 = 0.0;
+    if (act) {
+      xj = ld3(P, sr[sub][m]);
+      xk = ld3(P, sr[sub][m == 0 ? n - 1 : m - 1]);
+      ev = xj - xv;
+      double l2 = dot(ev, ev);
+      il = rsqrt(l2);
+      el = l2 * il;
+      N0 = cross(ev, xk - xv);
+      n0s = dot(N0, N0);
+      r0 = rsqrt(n0s);
+    }
+    const int src = gbase + mn;
+    d3 N1;
+    N1.x = __shfl_sync(gmask, N0.x, src);
+    N1.y = __shfl_sync(gmask, N0.y, src);
+    N1.z = __shfl_sync(gmask, N0.z, src);
+    const double n1s = __shfl_sync(gmask, n0s, src);
+    const double r1 = __shfl_sync(gmask, r0, src);
+    if (act) terms(xj, xk, ev, el, il, n0s, r0, N0, sf[sub][mn] != 0, N1, n1s, r1);
+  } else {
+    for (int m = w8; m < n; m += 8) {
+      if (!sf[sub][m]) continue;
       int j = sr[sub][m], k = sr[sub][m == 0 ? n - 1 : m - 1];
       int mn = m + 1 == n ? 0 : m + 1;
       d3 xj = ld3(P, j), xk = ld3(P, k);
@@ -487,65 +595,38 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
       d3 N0 = cross(ev, xk - xv);
       double n0s = dot(N0, N0);
       double r0 = rsqrt(n0s);
-      double fa = 0.5 * (n0s * r0);
-      double th = 0.0;
-      if (sf[sub][mn]) {
-        d3 xn = ld3(P, sr[sub][mn]);
-        d3 N1 = cross(xn - xv, ev);
-        double n1s = dot(N1, N1);
-        if (n0s != 0.0 && n1s != 0.0) {
-          // dihedral angle from cosine and signed sine (N0 x N1 lies along
-          // the edge; its sign is the reference's test (N0 x N1) . e >= 0)
-          double inv = r0 * rsqrt(n1s);
-          double sd = dot(cross(N0, N1), ev) * (inv * il);
-          double a = angle_sc(fabs(sd), dot(N0, N1) * inv, sct);
-          th = sd >= 0.0 ? a : -a;
-        }
+      d3 N1 = mk(0, 0, 0);
+      double n1s = 0.0, r1 = 0.0;
+      const bool have1 = sf[sub][mn] != 0;
+      if (have1) {
+        N1 = cross(ld3(P, sr[sub][mn]) - xv, ev);
+        n1s = dot(N1, N1);
+        r1 = rsqrt(n1s);
       }
-      tc = 0.5 * el * th;
-      ta = fa;
-      tv = dot(cross(xj, xk), xv) * (1.0 / 6.0);
-      if (ep.btype == 0) {
-        int r = ep.r;
-        if (el > ep.lc0)
-          tt = ipow((double)r, r + 1) * ipow(el - ep.lc0, r);
-        else if (el < ep.lc1)
-          tt = exp(el / (el - ep.lc1)) / ipow(el, r);
-      } else {
-        double qa = fa / ep.a0 - 1.0;
-        tt = qa * qa;
-      }
+      terms(xj, xk, ev, el, il, n0s, r0, N0, have1, N1, n1s, r1);
     }
-    term[sub][m][0] = tc;
-    term[sub][m][1] = ta;
-    term[sub][m][2] = tv;
-    term[sub][m][3] = tt;
   }
-  __syncthreads();
+  // sums over the ring: a butterfly over the 8 lanes (every lane ends with
+  // the same sums)
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) {
+    sc += __shfl_xor_sync(gmask, sc, o);
+    sa += __shfl_xor_sync(gmask, sa, o);
+    sv += __shfl_xor_sync(gmask, sv, o);
+    stt += __shfl_xor_sync(gmask, stt, o);
+  }
   double* o = part + 8 * 8 * (size_t)s + 8 * sub;
   if (w8 == 0) {
-    double A = 0, V = 0, C = 0, T = 0;
-    for (int m = 0; m < n; ++m) {
-      if (!sf[sub][m]) continue;
-      C += term[sub][m][0];
-      A += term[sub][m][1];
-      V += term[sub][m][2];
-      T += term[sub][m][3];
-    }
-    A /= 3;
-    V /= 3;
-    C /= 2;
-    T /= ep.tdiv;
+    const double A = sa * (1.0 / 3.0), C = 0.5 * sc;
     o[0] = A;
-    o[1] = V;
+    o[1] = sv * (1.0 / 3.0);
     o[2] = C;
     o[3] = 2 * C * C / A;
-    o[4] = T;
+    o[4] = stt * (1.0 / ep.tdiv);
   }
   // repulsion: the near row shared by the variant's 8 lanes, else one lane
   // walks the cell list
   {
-    const unsigned gmask = 0xffu << (threadIdx.x & 24);
     double pot = 0.0;
     bool near;
     if (sub < 4) {
@@ -562,23 +643,39 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
   __syncthreads();
   // the property change of the flip (before - after, in the summation orders
   // of edge_vertex_properties before (va0, va1, vb0, vb1) and after the flip
-  // (va1, vb0, vb1, va0)), -log(u) and the eligibility flag
-  if (threadIdx.x == 0) {
+  // (va1, vb0, vb1, va0)): lane k of warp 0 takes property k
+  if (threadIdx.x < 32) {
     const double* op = part + 64 * (size_t)s;
-    double* o8 = dpn + 8 * (size_t)s;
-    for (int k = 0; k < 6; ++k) {
+    double dk = 0.0;
+    if (threadIdx.x < 6) {
+      const int k = threadIdx.x;
       double before = ((op[k] + op[8 + k]) + op[16 + k]) + op[24 + k];
       double after = ((op[40 + k] + op[48 + k]) + op[56 + k]) + op[32 + k];
-      o8[k] = before - after;
+      dk = before - after;
+      dpn[8 * (size_t)s + k] = dk;
+      dpf[8 * (size_t)s + k] = (float)dk;
     }
-    o8[6] = -log(flip_u_of(seed, win[s]));
-    // the Metropolis test on the state at the start of the window (the
-    // first round of k_metro): 2 = accepted there, 1 = rejected there
-    double trial[6];
-    for (int k = 0; k < 6; ++k) trial[k] = st->props[k] - o8[k];
-    o8[7] = flip_energy(fe, trial) - st->e0 <= o8[6] ? 2.0 : 1.0;
-    float* f8 = dpf + 8 * (size_t)s;
-    for (int k = 0; k < 8; ++k) f8[k] = (float)o8[k];
+    float f8[7];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f8[k] = (float)__shfl_sync(0xffffffffu, dk, k);
+    if (threadIdx.x == 0) {
+      // -log(u) in float, and the Metropolis test on the state at the start
+      // of the window (the first round of k_metro) by the float filter; the
+      // FP64 test when the filter cannot decide.  2 = accepted there,
+      // 1 = rejected there.
+      const double u = flip_u_of(seed, win[s]);
+      const float uf = (float)u;
+      f8[6] = uf > 1e-30f ? -logf(uf) : 0.0f;
+      int fd = uf > 1e-30f ? metro_filter(fg, st->sq, f8) : -1;
+      if (fd < 0) {
+        double trial[6];
+        for (int k = 0; k < 6; ++k) trial[k] = st->props[k] - dpn[8 * (size_t)s + k];
+        fd = flip_energy(fe, trial) - st->e0 <= -log(u) ? 1 : 0;
+      }
+      dpn[8 * (size_t)s + 7] = fd ? 2.0 : 1.0;
+      dpf[8 * (size_t)s + 6] = f8[6];
+      dpf[8 * (size_t)s + 7] = fd ? 2.0f : 1.0f;
+    }
   }
 }
 
@@ -590,8 +687,9 @@ __global__ void __launch_bounds__(64, 16) k_delta(TopoW t, const FlipState* st, 
 // same decisions as a walk in slot order.  Then the deferred proposals are
 // compacted in order for the next window.
 constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread
-__global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsigned char* winner,
-                                             const double* dpn, const float* dpf, FlipE fe, FlipEF fg,
+__global__ void __launch_bounds__(MB) k_metro(unsigned long long seed, const long long* win,
+                                             const unsigned char* winner, const double* dpn, const float* dpf,
+                                             FlipE fe, FlipEF fg,
                                              FlipState* st, const int* limit, unsigned char* accepted,
                                              long long* pend) {
   __shared__ double sP[6], se0;
@@ -633,7 +731,7 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
           const double* o8 = dpn + 8 * (size_t)s;
           double trial[6];
           for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
-          acc_s = flip_energy(fe, trial) - se0 <= o8[6];
+          acc_s = flip_energy(fe, trial) - se0 <= -log(flip_u_of(seed, win[s]));
         }
       }
       if (acc_s) {
@@ -681,6 +779,7 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
   if (tid == MB - 1) st->npend = scan[MB - 1];
   if (tid == 0) {
     for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
+    for (int k = 0; k < 4; ++k) st->sq[k] = sq[k];
     st->e0 = se0;
     st->acc = sacc;
     st->next_new = st->nn_next;
@@ -804,10 +903,10 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, mode, seed, win.get(), owner.get(), winner.get(),
                                              limit.get());
       TM_LAUNCH();
-      k_delta<<<B, 64, 0, s>>>(t, st, seed, win.get(), winner.get(), limit.get(), P, ep, fe, nlv,
+      k_delta<<<B, 64, 0, s>>>(t, st, seed, win.get(), winner.get(), limit.get(), P, ep, fe, fg, nlv,
                                part.get(), okf.get(), dpn.get(), dpf.get(), e->sct.get());
       TM_LAUNCH();
-      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(),
+      k_metro<<<1, MB, 0, s>>>(seed, win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(),
                                acc.get(), pend.get());
       TM_LAUNCH();
       k_commit<<<B, 32, 0, s>>>(t, seed, win.get(), acc.get(), st);

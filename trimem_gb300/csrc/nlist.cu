@@ -430,8 +430,13 @@ __global__ void k_cand(int nv, NLView nl, const int* vcoord, int pass, int* cnt,
 // table (the cells that meet the ball of radius rn), with a flag for pairs
 // excluded on the current topology.  A row longer than TM_NEAR_CAP marks the
 // rows unusable (flag[3]).
-__global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, double rn, double rn2, int* flag,
-                       int* ncnt, int* nent, double* xb, const EP* eps) {
+constexpr int NB = 128;  // threads per block of k_near
+__global__ void __launch_bounds__(NB) k_near(int nv, const double* P, NLView nl, Topo t, int excl, double rn,
+                                             double rn2, int* flag, int* ncnt, int* nent, double* xb,
+                                             const EP* eps) {
+  // the row of each thread, staged in shared memory (stride 49: no bank
+  // conflicts) while the exclusion flags are set
+  __shared__ int srow[NB][TM_NEAR_CAP + 1];
   if (flag[1] == 0) return;  // rows still valid
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nv) return;
@@ -448,24 +453,30 @@ __global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, dou
   d3 pa = ld3(P, a);
   const double* pp = &pa.x;
   int lo[3], hi[3];
+  // position in cell units (float) for the box-distance pruning; a cell is
+  // skipped only when it is farther than rn after every axis distance is
+  // shortened by 1e-3 cell widths plus 8 float ulps of the coordinate, far
+  // above the float rounding of the cell coordinate
+  float u[3], rlf[3], mg[3];
   for (int k = 0; k < 3; ++k) {
     lo[k] = max(0, (int)floor((pp[k] - rn - G.bmin[k]) * G.inv_rl[k]) - 1);
     hi[k] = min(G.shape[k] - 1, (int)floor((pp[k] + rn - G.bmin[k]) * G.inv_rl[k]) + 1);
+    u[k] = (float)((pp[k] - G.bmin[k]) * G.inv_rl[k]);
+    rlf[k] = (float)G.rl[k];
+    mg[k] = 1e-3f + 9.6e-7f * fabsf(u[k]);
   }
+  const float rnf2 = (float)rn2 * 1.0001f;
+  int* row = srow[threadIdx.x];
   int n = 0;
-  int* row = nent + (size_t)a * TM_NEAR_CAP;
-  for (int ii = lo[0]; ii <= hi[0]; ++ii)
-    for (int jj = lo[1]; jj <= hi[1]; ++jj)
+  for (int ii = lo[0]; ii <= hi[0]; ++ii) {
+    float dx = fmaxf(fmaxf((float)ii - u[0], u[0] - (float)(ii + 1)) - mg[0], 0.0f) * rlf[0];
+    for (int jj = lo[1]; jj <= hi[1]; ++jj) {
+      float dy = fmaxf(fmaxf((float)jj - u[1], u[1] - (float)(jj + 1)) - mg[1], 0.0f) * rlf[1];
+      float gxy = dx * dx + dy * dy;
+      if (gxy > rnf2) continue;
       for (int kk = lo[2]; kk <= hi[2]; ++kk) {
-        // skip cells whose box is farther than rn
-        double g2 = 0.0;
-        const int cc[3] = {ii, jj, kk};
-        for (int k = 0; k < 3; ++k) {
-          double c0 = G.bmin[k] + cc[k] * G.rl[k], c1 = c0 + G.rl[k];
-          double dd = pp[k] < c0 ? c0 - pp[k] : (pp[k] > c1 ? pp[k] - c1 : 0.0);
-          g2 += dd * dd;
-        }
-        if (g2 > rn2 * 1.000001) continue;
+        float dz = fmaxf(fmaxf((float)kk - u[2], u[2] - (float)(kk + 1)) - mg[2], 0.0f) * rlf[2];
+        if (gxy + dz * dz > rnf2) continue;
         long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
         int st = 0;
         int c = cell_lookup(nl, cell_key(cid, rep), &st);
@@ -475,12 +486,36 @@ __global__ void k_near(int nv, const double* P, NLView nl, Topo t, int excl, dou
           d3 pb = ld3(P, b);
           double ex = pa.x - pb.x, ey = pa.y - pb.y, ez = pa.z - pb.z;
           if (ex * ex + ey * ey + ez * ez >= rn2) continue;
-          if (n < TM_NEAR_CAP) row[n] = nl_excluded(t, excl, a, b) ? (int)(0x80000000u | (unsigned)b) : b;
+          if (n < TM_NEAR_CAP) row[n] = b;
           ++n;
         }
       }
+    }
+  }
   if (n > TM_NEAR_CAP) atomicOr(&flag[3], 1);
-  ncnt[a] = min(n, TM_NEAR_CAP);
+  n = min(n, TM_NEAR_CAP);
+  // exclusion flags (nl_excluded): an entry is excluded when it is in the
+  // ring of a or, at level 2, in the ring of a ring vertex of a; the rings
+  // are walked once and their vertices looked up in the row
+  if (excl > 0 && n > 0) {
+    const int d = t.val[a];
+    for (int m = 0; m < d; ++m) {
+      const int w = t.nbr[(size_t)m * t.nv + a];
+      for (int e = 0; e < n; ++e)
+        if (row[e] == w) row[e] |= (int)0x80000000u;
+      if (excl > 1) {
+        const int dw = t.val[w];
+        for (int q = 0; q < dw; ++q) {
+          const int x = t.nbr[(size_t)q * t.nv + w];
+          for (int e = 0; e < n; ++e)
+            if ((row[e] & 0x7fffffff) == x) row[e] |= (int)0x80000000u;
+        }
+      }
+    }
+  }
+  int* out = nent + (size_t)a * TM_NEAR_CAP;
+  for (int e = 0; e < n; ++e) out[e] = row[e];
+  ncnt[a] = n;
   xb[3 * a] = pa.x;
   xb[3 * a + 1] = pa.y;
   xb[3 * a + 2] = pa.z;
@@ -679,7 +714,7 @@ static void refresh_near(tm_nlist* nl, tm_mesh* m, NLView& V, const double* P, d
   int* flag = nl->nflag.get();
   k_near_check<<<nblk(nv, 256), 256, 0, s>>>(nv, P, nl->xb.get(), nl->near_move2, flag, V.vrep, eps);
   TM_LAUNCH();
-  k_near<<<nblk(nv, 128), 128, 0, s>>>(nv, P, V, t, V.excl, rn, rn * rn * (1.0 + 1e-12), flag, nl->ncnt.get(),
+  k_near<<<nblk(nv, NB), NB, 0, s>>>(nv, P, V, t, V.excl, rn, rn * rn * (1.0 + 1e-12), flag, nl->ncnt.get(),
                                        nl->nent.get(), nl->xb.get(), eps);
   TM_LAUNCH();
   k_near_done<<<1, 32, 0, s>>>(flag, m->d_topo_ver.get());
