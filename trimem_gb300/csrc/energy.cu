@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <vector>
 
 #include "tm_internal.h"
 #include "tm_math.cuh"
@@ -111,7 +112,7 @@ __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __rest
   // k_bond_short so that whole warps do not wait on a few lanes
   double val = 0.0, fac = 0.0;
   bool shortb = ep.btype == 0 && l < ep.lc1;
-  if (ep.btype == 0 && !shortb && l > ep.lc0) edge_bond(ep, l, &val, &fac);
+  if (ep.btype == 0 && !shortb && l > ep.lc0) edge_bond(ep, l, il, &val, &fac);
   warp_append(shortb, e, blist, bcnt);  o.db = fac;
   ed[e] = o;
   ebond[e] = val;
@@ -124,7 +125,8 @@ __global__ void k_bond_short(const double* __restrict__ P, Topo t, EdgeD* __rest
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int e = blist[i];
     double val, fac;
-    edge_bond(ep, ed[e].l, &val, &fac);
+    const EdgeD E = ed[e];
+    edge_bond(ep, E.l, fabs(E.il), &val, &fac);
     ed[e].db = fac;
     ebond[e] = val;
   }
@@ -319,6 +321,7 @@ inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 EP make_ep(const tm_energy* e) {
   const tm_params& p = e->prm;
   EP ep;
+  std::memset(&ep, 0, sizeof ep);  // padding too: evaluation graphs compare EP bytes
   ep.kb = p.kappa_b;
   ep.ka = p.kappa_a;
   ep.kv = p.kappa_v;
@@ -346,8 +349,102 @@ void energy_eval(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool
   energy_eval_marked(e, m, P, want_grad, want_vprops, d_grad, s, nullptr);
 }
 
+static void eval_fp64_launches(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool want_vprops,
+                               double* d_grad, cudaStream_t s, cudaEvent_t* ev);
+
+// the launches of one evaluation in the energy's stencil precision
+static void eval_launches(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, double* d_grad,
+                          cudaStream_t s) {
+  if (e->stencil == 1)
+    energy_eval32(e, m, P, want_grad, false, d_grad, s, nullptr);
+  else if (e->stencil == 2)
+    energy_eval_df(e, m, P, want_grad, d_grad, s, nullptr);
+  else
+    eval_fp64_launches(e, m, P, want_grad, false, d_grad, s, nullptr);
+}
+
+// What the launches of an evaluation depend on besides device memory:
+// arguments, stencil precision, buffers, parameters and the neighbour-list
+// view.  Equal keys mean a captured graph replays the same launches.
+static std::vector<unsigned char> eval_key(tm_energy* e, tm_mesh* m, const double* P, bool want_grad,
+                                           double* d_grad, cudaStream_t s) {
+  std::vector<unsigned char> k;
+  auto add = [&k](const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    k.insert(k.end(), b, b + n);
+  };
+  const void* ptrs[] = {P, d_grad, s, e->face.get(), e->edge.get(), e->ebond.get(), e->rho.get(), e->repg.get(),
+                        e->reppot.get(), e->slow.get(), e->pos32.get(), e->poslo.get(), e->partials.get(),
+                        e->glob.get(), e->sct.get(), e->aux, e->ev_fork, e->ev_join, e->nl.xb.get()};
+  add(ptrs, sizeof ptrs);
+  const Topo t = m->topo();
+  const int sizes[] = {t.nv, t.ne, t.nf, want_grad ? 1 : 0, e->stencil, e->nl.near_nv};
+  add(sizes, sizeof sizes);
+  const void* tp[] = {t.to, t.next, t.face, t.vout, t.fhe, t.slot, t.nbr, t.val, t.fv, t.edge};
+  add(tp, sizeof tp);
+  const double nd[] = {e->nl.near_lc1, e->nl.near_move2};
+  add(nd, sizeof nd);
+  const EP ep = make_ep(e);
+  add(&ep, sizeof ep);
+  add(&e->nl.view, sizeof(NLView));
+  return k;
+}
+
+// Evaluation replayed from a CUDA graph: the launch sequence (about a dozen
+// kernels, memsets and the fork/join of the repulsion stream) is captured
+// per key and then issued as one graph launch, which removes the gaps
+// between the short kernels.  On a miss the launches run directly first
+// (any allocation they make happens outside a capture), then they are
+// captured for the next call.  A few graphs are kept (with and without the
+// gradient, several buffers), the least recently used is replaced.
+static void eval_graph(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, double* d_grad, cudaStream_t s) {
+  constexpr size_t MAX_GRAPHS = 4;
+  std::vector<unsigned char> key = eval_key(e, m, P, want_grad, d_grad, s);
+  for (auto& g : e->eval_graphs)
+    if (g.exec && g.key == key) {
+      g.used = ++e->eval_tick;
+      TM_CUDA(cudaGraphLaunch(g.exec, s));
+      return;
+    }
+  eval_launches(e, m, P, want_grad, d_grad, s);
+  key = eval_key(e, m, P, want_grad, d_grad, s);
+  cudaGraph_t g = nullptr;
+  TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  try {
+    eval_launches(e, m, P, want_grad, d_grad, s);
+  } catch (...) {
+    cudaStreamEndCapture(s, &g);  // leave capture mode before reporting
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    throw;
+  }
+  TM_CUDA(cudaStreamEndCapture(s, &g));
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t rc = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  TM_CUDA(rc);
+  tm_energy::EvalGraph* slot = nullptr;
+  if (e->eval_graphs.size() < MAX_GRAPHS) {
+    e->eval_graphs.emplace_back();
+    slot = &e->eval_graphs.back();
+  } else {
+    slot = &e->eval_graphs[0];
+    for (auto& c : e->eval_graphs)
+      if (c.used < slot->used) slot = &c;
+    cudaGraphExecDestroy(slot->exec);
+  }
+  slot->exec = exec;
+  slot->key.swap(key);
+  slot->used = ++e->eval_tick;
+}
+
 void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool want_vprops, double* d_grad,
                         cudaStream_t s, cudaEvent_t* ev) {
+  // graphs need a capturable stream (not the legacy default stream)
+  if (!ev && !want_vprops && s != nullptr && e->use_graphs) {
+    eval_graph(e, m, P, want_grad, d_grad, s);
+    return;
+  }
   if (e->stencil == 1 && !want_vprops) {
     energy_eval32(e, m, P, want_grad, want_vprops, d_grad, s, ev);
     return;
@@ -356,6 +453,11 @@ void energy_eval_marked(tm_energy* e, tm_mesh* m, const double* P, bool want_gra
     energy_eval_df(e, m, P, want_grad, d_grad, s, ev);
     return;
   }
+  eval_fp64_launches(e, m, P, want_grad, want_vprops, d_grad, s, ev);
+}
+
+static void eval_fp64_launches(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bool want_vprops,
+                               double* d_grad, cudaStream_t s, cudaEvent_t* ev) {
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
   e->ensure(m->nv, m->ne, m->nf);
   Topo t = m->topo();
@@ -439,6 +541,8 @@ void tm_energy::to_host(double* dst, const double* src, size_t n) {
 }
 
 tm_energy::~tm_energy() {
+  for (auto& g : eval_graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
   if (aux) cudaStreamDestroy(aux);

@@ -166,7 +166,8 @@ __global__ void k_bond_short_df(EdgeDF* __restrict__ ed, df* __restrict__ ebond,
       ebond[e] = val;
     } else {  // non-positive exponents: FP64
       double val, fac;
-      edge_bond(ep, df_to(ed[e].l), &val, &fac);
+      const double l = df_to(ed[e].l);
+      edge_bond(ep, l, 1.0 / l, &val, &fac);
       ed[e].db = df_from(fac);
       ebond[e] = df_from(val);
     }

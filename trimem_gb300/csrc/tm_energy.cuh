@@ -349,7 +349,9 @@ __device__ __forceinline__ void warp_append(bool need, int idx, int* list, int* 
 
 // Flat-bottom edge penalty and its derivative dB/dl
 // (src/mesh_tether.h:29-85) for an edge of length l.
-__device__ __forceinline__ void edge_bond(const EP& ep, double l, double* val, double* fac) {
+// il = 1/l; below the flat bottom one division (1/(l - lc1)) and powers of
+// il replace the four divisions of the textbook form
+__device__ __forceinline__ void edge_bond(const EP& ep, double l, double il, double* val, double* fac) {
   int r = ep.r;
   double v = 0.0, f = 0.0;
   if (l > ep.lc0) {
@@ -357,11 +359,11 @@ __device__ __forceinline__ void edge_bond(const EP& ep, double l, double* val, d
     f = ipow((double)r, r + 2) * ipow(l - ep.lc0, r - 1);
   }
   if (l < ep.lc1) {
-    double lmc = l - ep.lc1;
-    double ex = exp(l / lmc);
-    double ilr = 1.0 / ipow(l, r);
+    double ilm = 1.0 / (l - ep.lc1);
+    double ex = exp(l * ilm);
+    double ilr = ipow(il, r);
     if (!(l > ep.lc0)) v = ex * ilr;
-    f -= ep.lc1 / (lmc * lmc) + r / l;
+    f -= ep.lc1 * (ilm * ilm) + r * il;
     f *= ilr;
     f *= ex;
   }

@@ -223,6 +223,17 @@ struct tm_energy {
   // edge kernels, between a fork and a join event
   cudaStream_t aux = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // FP64 evaluation graphs (captured launch sequences), each with the key
+  // of what its launches depend on; a few are kept (with and without the
+  // gradient, several position buffers), the least recently used is replaced
+  struct EvalGraph {
+    std::vector<unsigned char> key;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long used = 0;
+  };
+  bool use_graphs = true;
+  std::vector<EvalGraph> eval_graphs;
+  unsigned long long eval_tick = 0;
   void ensure(int nv_, int ne_, int nf_);
   // copies n doubles from device memory to host memory dst and synchronises
   void to_host(double* dst, const double* src, size_t n);
