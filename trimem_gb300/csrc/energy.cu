@@ -543,6 +543,7 @@ void tm_energy::to_host(double* dst, const double* src, size_t n) {
 tm_energy::~tm_energy() {
   for (auto& g : eval_graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (flip_graph.exec) cudaGraphExecDestroy(flip_graph.exec);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
   if (aux) cudaStreamDestroy(aux);

@@ -82,6 +82,7 @@ __device__ __forceinline__ double flip_u_of(unsigned long long seed, long long p
 struct FlipState {
   double props[8];
   double e0;
+  unsigned long long seed;  // proposal stream of the sweep
   float sq[4];  // float-filter constants of props (filter_state)
   long long next_new;  // first proposal not yet in a window
   long long nn_next;   // next_new after the current window (committed by k_metro)
@@ -226,19 +227,15 @@ __device__ __forceinline__ double flip_energy(const FlipE& f, const double* p) {
   return tot;
 }
 
-// Float filter of the Metropolis test E(props - dp) - E(props) <= -log u:
-// the energy change is written without cancellation (quadratic penalties
-// as k t (t - 2 d0), d0 = props/ref - 1 of the current state, t = dp/ref;
-// the linear terms as -k dp) and evaluated from float copies.  A decision
-// is taken only when it is farther from the threshold than a bound on the
-// float error (relative 1e-4 of the terms' magnitudes), the FP64 rounding
-// of the exact test (1e-12 of |E|) and the float rounding of -log u;
-// otherwise (rare) the exact FP64 test decides.
+// Float filter of the Metropolis test E(props - dp) - E(props) <= -log u
+// (k_metro): the energy change is written without cancellation (quadratic
+// penalties as k t (t - 2 d0), d0 = props/ref - 1 of the current state,
+// t = dp/ref; the linear terms as -k dp) and evaluated from float copies.
 struct FlipEF {
   float irA, irV, irC, ka, kv, kc, kt, kr, kb;
 };
 // per-state constants of the filter: d0 of area, volume, curvature and the
-// FP64 rounding bound
+// FP64 rounding bound of the exact test (1e-12 of the energy's magnitude)
 __device__ __forceinline__ void filter_state(const FlipE& f, const double* p, float* q) {
   double da = p[0] * f.irA - 1.0, dv = p[1] * f.irV - 1.0, dc = p[2] * f.irC - 1.0;
   double mag = fabs(f.ka * da * da) + fabs(f.kv * dv * dv) + fabs(f.kc * dc * dc) + fabs(f.kt * p[4]) +
@@ -248,25 +245,10 @@ __device__ __forceinline__ void filter_state(const FlipE& f, const double* p, fl
   q[2] = (float)dc;
   q[3] = (float)(1e-12 * mag);
 }
-// 1 accept, 0 reject, -1 too close to call in float
-__device__ __forceinline__ int metro_filter(const FlipEF& g, const float* q, const float* f8) {
-  float ta = f8[0] * g.irA, tv = f8[1] * g.irV, tc = f8[2] * g.irC;
-  float xa = g.ka * ta * (ta - 2.0f * q[0]);
-  float xv = g.kv * tv * (tv - 2.0f * q[1]);
-  float xc = g.kc * tc * (tc - 2.0f * q[2]);
-  float xl = g.kt * f8[4] + g.kr * f8[5] + g.kb * f8[3];
-  float S = fabsf(g.ka * ta) * (fabsf(ta) + 2.0f * fabsf(q[0])) + fabsf(g.kv * tv) * (fabsf(tv) + 2.0f * fabsf(q[1])) +
-            fabsf(g.kc * tc) * (fabsf(tc) + 2.0f * fabsf(q[2])) + fabsf(g.kt * f8[4]) + fabsf(g.kr * f8[5]) +
-            fabsf(g.kb * f8[3]);
-  float m = 1e-4f * S + q[3] + 1e-6f * fabsf(f8[6]) + 2e-7f;  // f8[6]: -log u in float
-  float d = ((xa + xv) + xc - xl) - f8[6];
-  if (d < -m) return 1;
-  if (d > m) return 0;
-  return -1;  // also for NaN and overflow
-}
 
-__global__ void k_flip_init(FlipE fe, const Globals* g, long long nflips, FlipState* st) {
+__global__ void k_flip_init(FlipE fe, const Globals* g, long long nflips, unsigned long long seed, FlipState* st) {
   if (threadIdx.x || blockIdx.x) return;
+  st->seed = seed;
   for (int k = 0; k < 6; ++k) st->props[k] = g->props[k];
   st->e0 = flip_energy(fe, st->props);
   filter_state(fe, st->props, st->sq);
@@ -312,7 +294,8 @@ __device__ __forceinline__ void for_ring_edges(const TopoW& t, int v, F&& fn) {
   }
 }
 
-__global__ void k_claim(TopoW t, const FlipState* st, unsigned long long seed, const long long* win, int* owner) {
+__global__ void k_claim(TopoW t, const FlipState* st, const long long* win, int* owner) {
+  const unsigned long long seed = st->seed;
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   int s = g >> 2, k = g & 3;
   const int W = st->W, wid = st->wid;
@@ -322,8 +305,9 @@ __global__ void k_claim(TopoW t, const FlipState* st, unsigned long long seed, c
   for_ring_edges(t, quad_vertex(q, k), [&](int x) { atomicMax(&owner[x], tag); });
 }
 
-__global__ void k_winner(TopoW t, const FlipState* st, int mode, unsigned long long seed, const long long* win,
-                         const int* owner, unsigned char* winner, int* limit) {
+__global__ void k_winner(TopoW t, const FlipState* st, int mode, const long long* win, const int* owner,
+                         unsigned char* winner, int* limit) {
+  const unsigned long long seed = st->seed;
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   int s = g >> 2, k = g & 3;
   const int W = st->W, wid = st->wid;
@@ -427,16 +411,16 @@ __device__ bool repulsion_near8(int v, d3 xv, const double* P, const EP& ep, con
 // of vertex_properties (src/mesh_properties.cpp:12-49) in parallel, and one
 // worker sums them in ring order while
 // another computes the repulsion.
-__global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, unsigned long long seed,
-                                              const long long* win, const unsigned char* winner, const int* limit,
-                                              const double* P, EP ep, FlipE fe, FlipEF fg, NLView nl,
-                                              double* part, unsigned char* okf, double* dpn, float* dpf,
-                                              const double2* __restrict__ sct) {
+__global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, const long long* win,
+                                              const unsigned char* winner, const int* limit, const double* P,
+                                              EP ep, NLView nl, double* part, unsigned char* okf, double* dpn,
+                                              float* dpf, const double2* __restrict__ sct) {
   __shared__ int sr[8][TM_MAXVAL + 1];
   __shared__ unsigned char sf[8][TM_MAXVAL + 1];
   __shared__ int sn[8];
   __shared__ long long rkey[8][NEAR_HITS];
   __shared__ double rval[8][NEAR_HITS], rterm[8][NEAR_HITS];
+  const unsigned long long seed = st->seed;
   const int s = blockIdx.x;
   const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
   const int gbase = threadIdx.x & 24;            // warp lane of the variant's lane 0
@@ -655,133 +639,182 @@ __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, 
       dpn[8 * (size_t)s + k] = dk;
       dpf[8 * (size_t)s + k] = (float)dk;
     }
-    float f8[7];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) f8[k] = (float)__shfl_sync(0xffffffffu, dk, k);
     if (threadIdx.x == 0) {
-      // -log(u) in float, and the Metropolis test on the state at the start
-      // of the window (the first round of k_metro) by the float filter; the
-      // FP64 test when the filter cannot decide.  2 = accepted there,
-      // 1 = rejected there.
-      const double u = flip_u_of(seed, win[s]);
-      const float uf = (float)u;
-      f8[6] = uf > 1e-30f ? -logf(uf) : 0.0f;
-      int fd = uf > 1e-30f ? metro_filter(fg, st->sq, f8) : -1;
-      if (fd < 0) {
-        double trial[6];
-        for (int k = 0; k < 6; ++k) trial[k] = st->props[k] - dpn[8 * (size_t)s + k];
-        fd = flip_energy(fe, trial) - st->e0 <= -log(u) ? 1 : 0;
-      }
-      dpn[8 * (size_t)s + 7] = fd ? 2.0 : 1.0;
-      dpf[8 * (size_t)s + 6] = f8[6];
-      dpf[8 * (size_t)s + 7] = fd ? 2.0f : 1.0f;
+      // -log(u) in float for k_metro's filter (NaN below float range: the
+      // FP64 test decides) and the eligibility flag
+      const float uf = (float)flip_u_of(seed, win[s]);
+      dpn[8 * (size_t)s + 7] = 1.0;
+      dpf[8 * (size_t)s + 6] = uf > 1e-30f ? -logf(uf) : __int_as_float(0x7fc00000);
+      dpf[8 * (size_t)s + 7] = 1.0f;
     }
   }
 }
 
 // Metropolis with T = 1 in slot order (flips.cpp:142-160): slot s is tried on
 // the state left by the accepted slots before it, trial = props - dp, and is
-// accepted when E(trial) - E <= -log(u).  Acceptances are rare, so one block
-// tries all remaining slots against the current state at once, takes the
-// first accepted one, updates the state and repeats from the next slot: the
-// same decisions as a walk in slot order.  Then the deferred proposals are
-// compacted in order for the next window.
-constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread
-__global__ void __launch_bounds__(MB) k_metro(unsigned long long seed, const long long* win,
-                                             const unsigned char* winner, const double* dpn, const float* dpf,
-                                             FlipE fe, FlipEF fg,
-                                             FlipState* st, const int* limit, unsigned char* accepted,
-                                             long long* pend) {
-  __shared__ double sP[6], se0;
-  __shared__ float sq[4];
-  __shared__ int sfirst, sstart, sacc;
-  __shared__ int scan[MB];
-  const int tid = threadIdx.x;
+// accepted when E(trial) - E <= -log(u).  The state moves only by the dp of
+// accepted slots, and the energy change of slot s depends on the state only
+// through the area, volume and curvature penalties, linearly in the state's
+// normalised deviations d0: D = k t (t - 2 d0) + ... .  So the first phase
+// bounds, for every slot at once, how far any set of earlier acceptances can
+// move its D (2 k |t| times the sum of |dp|/ref over the window's eligible
+// slots) and decides it by the float filter against the window's starting
+// state when the decision survives that shift: robustly accepted or
+// rejected.  The second phase walks, in slot order, only the robustly
+// accepted slots (state update) and the undecided ones (the FP64 test on the
+// current state, then the update when accepted): the same decisions and the
+// same FP64 state updates as a walk over every slot.  Then the deferred
+// proposals are compacted in order for the next window.
+constexpr int MB = 1024, MS = MAXB / MB;  // threads, slots per thread (consecutive)
+
+// exclusive scan of two counters over the block (1,024 threads); returns the
+// totals
+__device__ __forceinline__ int2 block_scan2(int a, int b, int* ea, int* eb, int2* wsum) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int ta = __shfl_up_sync(0xffffffffu, ia, o), tb = __shfl_up_sync(0xffffffffu, ib, o);
+    if (lane >= o) {
+      ia += ta;
+      ib += tb;
+    }
+  }
+  if (lane == 31) wsum[w] = make_int2(ia, ib);
+  __syncthreads();
+  if (w == 0) {
+    int2 v = wsum[lane];
+    int xa = v.x, xb = v.y;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int ta = __shfl_up_sync(0xffffffffu, xa, o), tb = __shfl_up_sync(0xffffffffu, xb, o);
+      if (lane >= o) {
+        xa += ta;
+        xb += tb;
+      }
+    }
+    wsum[lane] = make_int2(xa, xb);  // inclusive over warps
+  }
+  __syncthreads();
+  const int2 before = w ? wsum[w - 1] : make_int2(0, 0);
+  *ea = before.x + ia - a;
+  *eb = before.y + ib - b;
+  return wsum[31];
+}
+
+__global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsigned char* winner, const double* dpn,
+                                             const float* dpf, FlipE fe, FlipEF fg, FlipState* st, const int* limit,
+                                             unsigned char* accepted, long long* pend) {
+  constexpr unsigned char SKIP = 0, REJECT = 1, ACCEPT = 2, OPEN = 3;
+  __shared__ int lst[MAXB];
+  __shared__ int2 wsum[32];
+  __shared__ float sb[3][32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int W = st->W;
-  __syncthreads();  // every thread has read W before thread 0 may write the state
-  if (tid == 0) {
-    for (int k = 0; k < 6; ++k) sP[k] = st->props[k];
-    se0 = st->e0;
-    sacc = st->acc;
-    sstart = 0;
-    filter_state(fe, sP, sq);
-  }
+  const unsigned long long seed = st->seed;
+  float q[4];
+  for (int k = 0; k < 4; ++k) q[k] = st->sq[k];
+  // window-wide bound of the state's movement: sum of |dp|/ref of the
+  // eligible slots (area, volume, curvature)
+  float ba = 0.0f, bv = 0.0f, bc = 0.0f;
   for (int k = 0; k < MS; ++k) {
-    int s = tid * MS + k;
-    if (s < W) accepted[s] = 0;
+    const int s = tid * MS + k;
+    if (s >= W) break;
+    accepted[s] = 0;
+    const float* f8 = dpf + 8 * (size_t)s;
+    if (f8[7] == 0.0f) continue;
+    ba += fabsf(f8[0] * fg.irA);
+    bv += fabsf(f8[1] * fg.irV);
+    bc += fabsf(f8[2] * fg.irC);
   }
-  __syncthreads();
-  for (int round = 0; round <= W; ++round) {
-    if (tid == 0) sfirst = INT_MAX;
-    __syncthreads();
-    const int start = sstart;
-    for (int k = 0; k < MS; ++k) {
-      int s = k * MB + tid;  // strided: every thread has a slot in small windows
-      if (s < start || s >= W) continue;
-      const float* f8 = dpf + 8 * (size_t)s;
-      if (f8[7] == 0.0f) continue;
-      bool acc_s;
-      if (round == 0) {  // decided by k_delta on this same state
-        acc_s = f8[7] == 2.0f;
-      } else {
-        int fd = metro_filter(fg, sq, f8);
-        if (fd >= 0) {
-          acc_s = fd == 1;
-        } else {
-          const double* o8 = dpn + 8 * (size_t)s;
-          double trial[6];
-          for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
-          acc_s = flip_energy(fe, trial) - se0 <= -log(flip_u_of(seed, win[s]));
-        }
-      }
-      if (acc_s) {
-        atomicMin(&sfirst, s);
-        break;  // later slots of this thread cannot be first
-      }
-    }
-    __syncthreads();
-    const int first = sfirst;
-    if (first == INT_MAX) break;
-    if (tid == first % MB) {
-      const double* o8 = dpn + 8 * (size_t)first;
-      double trial[6];
-      for (int q = 0; q < 6; ++q) trial[q] = sP[q] - o8[q];
-      double en = flip_energy(fe, trial);
-      for (int q = 0; q < 6; ++q) sP[q] = trial[q];
-      se0 = en;
-      filter_state(fe, sP, sq);
-      sacc += 1;
-      accepted[first] = 1;
-      sstart = first + 1;
-    }
-    __syncthreads();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ba += __shfl_xor_sync(0xffffffffu, ba, o);
+    bv += __shfl_xor_sync(0xffffffffu, bv, o);
+    bc += __shfl_xor_sync(0xffffffffu, bc, o);
   }
-  // deferred proposals (outside the limit or not winners), in slot order
+  if (lane == 0) {
+    sb[0][w] = ba;
+    sb[1][w] = bv;
+    sb[2][w] = bc;
+  }
+  __syncthreads();  // also: every thread has read W before thread 0 may write the state
+  ba = bv = bc = 0.0f;
+  for (int k = 0; k < 32; ++k) {  // same order in every thread
+    ba += sb[0][k];
+    bv += sb[1][k];
+    bc += sb[2][k];
+  }
+  ba *= 1.001f;  // float rounding of the sums
+  bv *= 1.001f;
+  bc *= 1.001f;
+  // phase 1: classify this thread's slots
+  unsigned char cls[MS];
+  int nopen = 0;
+  for (int k = 0; k < MS; ++k) {
+    const int s = tid * MS + k;
+    cls[k] = SKIP;
+    if (s >= W) continue;
+    const float* f8 = dpf + 8 * (size_t)s;
+    if (f8[7] == 0.0f) continue;
+    const float ta = f8[0] * fg.irA, tv = f8[1] * fg.irV, tc = f8[2] * fg.irC;
+    const float xa = fg.ka * ta * (ta - 2.0f * q[0]);
+    const float xv = fg.kv * tv * (tv - 2.0f * q[1]);
+    const float xc = fg.kc * tc * (tc - 2.0f * q[2]);
+    const float xl = fg.kt * f8[4] + fg.kr * f8[5] + fg.kb * f8[3];
+    const float S = fabsf(fg.ka * ta) * (fabsf(ta) + 2.0f * fabsf(q[0])) +
+                    fabsf(fg.kv * tv) * (fabsf(tv) + 2.0f * fabsf(q[1])) +
+                    fabsf(fg.kc * tc) * (fabsf(tc) + 2.0f * fabsf(q[2])) + fabsf(fg.kt * f8[4]) +
+                    fabsf(fg.kr * f8[5]) + fabsf(fg.kb * f8[3]);
+    const float shift = 2.0f * (fabsf(fg.ka * ta) * ba + fabsf(fg.kv * tv) * bv + fabsf(fg.kc * tc) * bc);
+    const float m = 1e-4f * S + 2.0f * q[3] + 1e-6f * fabsf(f8[6]) + 2e-7f + 1.01f * shift;
+    const float d = ((xa + xv) + xc - xl) - f8[6];
+    cls[k] = d < -m ? ACCEPT : (d > m ? REJECT : OPEN);  // NaN or overflow: OPEN
+    if (cls[k] >= ACCEPT) ++nopen;
+  }
+  // slots to walk (robustly accepted or open) and deferred proposals, both
+  // in slot order
   const int lim = *limit;
-  int c = 0;
+  int ndef = 0;
   for (int k = 0; k < MS; ++k) {
-    int s = tid * MS + k;
-    if (s < W && (s >= lim || !winner[s])) ++c;
+    const int s = tid * MS + k;
+    if (s < W && (s >= lim || !winner[s])) ++ndef;
   }
-  scan[tid] = c;
+  int ew = 0, ed = 0;
+  const int2 tot = block_scan2(nopen, ndef, &ew, &ed, wsum);
+  for (int k = 0; k < MS; ++k) {
+    const int s = tid * MS + k;
+    if (s >= W) break;
+    if (cls[k] >= ACCEPT) lst[ew++] = cls[k] == ACCEPT ? s : -1 - s;
+    if (s >= lim || !winner[s]) pend[ed++] = win[s];
+  }
   __syncthreads();
-  for (int o = 1; o < MB; o <<= 1) {
-    int v = tid >= o ? scan[tid - o] : 0;
-    __syncthreads();
-    scan[tid] += v;
-    __syncthreads();
-  }
-  int pos = scan[tid] - c;
-  for (int k = 0; k < MS; ++k) {
-    int s = tid * MS + k;
-    if (s < W && (s >= lim || !winner[s])) pend[pos++] = win[s];
-  }
-  if (tid == MB - 1) st->npend = scan[MB - 1];
+  // phase 2: one thread walks the listed slots in order on the FP64 state
   if (tid == 0) {
+    double sP[6];
+    for (int k = 0; k < 6; ++k) sP[k] = st->props[k];
+    double se0 = st->e0;
+    int sacc = st->acc;
+    for (int i = 0; i < tot.x; ++i) {
+      const int c = lst[i];
+      const bool robust = c >= 0;
+      const int s = robust ? c : -1 - c;
+      const double* o8 = dpn + 8 * (size_t)s;
+      double trial[6];
+      for (int k = 0; k < 6; ++k) trial[k] = sP[k] - o8[k];
+      const double en = flip_energy(fe, trial);
+      if (robust || en - se0 <= -log(flip_u_of(seed, win[s]))) {
+        for (int k = 0; k < 6; ++k) sP[k] = trial[k];
+        se0 = en;
+        sacc += 1;
+        accepted[s] = 1;
+      }
+    }
     for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
-    for (int k = 0; k < 4; ++k) st->sq[k] = sq[k];
+    filter_state(fe, sP, st->sq);
     st->e0 = se0;
     st->acc = sacc;
+    st->npend = tot.y;
     st->next_new = st->nn_next;
   }
 }
@@ -789,12 +822,12 @@ __global__ void __launch_bounds__(MB) k_metro(unsigned long long seed, const lon
 // one block of 32 threads per slot (accepted slots only do work): the
 // half-edge rewiring, then the two face rows and five edge rows, then the
 // four ring rows, each stage in parallel
-__global__ void __launch_bounds__(32) k_commit(TopoW t, unsigned long long seed, const long long* win,
-                                               const unsigned char* accepted, FlipState* st) {
+__global__ void __launch_bounds__(32) k_commit(TopoW t, const long long* win, const unsigned char* accepted,
+                                               FlipState* st) {
   const int s = blockIdx.x;
   if (s >= st->W || !accepted[s]) return;
   const int tid = threadIdx.x;
-  const int e = flip_edge_of(seed, win[s], t.ne);
+  const int e = flip_edge_of(st->seed, win[s], t.ne);
   const int a0 = 2 * e, b0 = 2 * e + 1;
   const int a1 = t.next[a0], a2 = t.next[a1], b1 = t.next[b0], b2 = t.next[b1];
   const int va0 = t.to[a0], va1 = t.to[a1], vb0 = t.to[b0], vb1 = t.to[b1];
@@ -886,32 +919,80 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   FlipE fe{1.0 / ep.refA, 1.0 / ep.refV, 1.0 / ep.refC, ep.ka, ep.kv, ep.kc, ep.kt, ep.kr, ep.kb};
   FlipEF fg{(float)fe.irA, (float)fe.irV, (float)fe.irC, (float)fe.ka, (float)fe.kv,
             (float)fe.kc, (float)fe.kt, (float)fe.kr, (float)fe.kb};
-  k_flip_init<<<1, 1, 0, s>>>(fe, e->glob.get(), nflips, st);
+  k_flip_init<<<1, 1, 0, s>>>(fe, e->glob.get(), nflips, seed, st);
   TM_LAUNCH();
   // windows are queued in groups without host round trips; W and the window
   // number live on the device, and a window after the last one is empty
-  // (W = 0: every kernel returns at once)
+  // (W = 0: every kernel returns at once).  A group's 48 launches do not
+  // depend on the sweep (the seed is in the device state), so they are
+  // captured once as a CUDA graph per launch key and replayed.
   const int B = batch;
   constexpr int GROUP = 8;
-  FlipState hs;
-  for (;;) {
+  auto launch_group = [&]() {
     for (int k = 0; k < GROUP; ++k) {
       k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st, win.get(), limit.get());
       TM_LAUNCH();
-      k_claim<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, seed, win.get(), owner.get());
+      k_claim<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, win.get(), owner.get());
       TM_LAUNCH();
-      k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, mode, seed, win.get(), owner.get(), winner.get(),
-                                             limit.get());
+      k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, mode, win.get(), owner.get(), winner.get(), limit.get());
       TM_LAUNCH();
-      k_delta<<<B, 64, 0, s>>>(t, st, seed, win.get(), winner.get(), limit.get(), P, ep, fe, fg, nlv,
-                               part.get(), okf.get(), dpn.get(), dpf.get(), e->sct.get());
+      k_delta<<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get(),
+                               dpn.get(), dpf.get(), e->sct.get());
       TM_LAUNCH();
-      k_metro<<<1, MB, 0, s>>>(seed, win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(),
-                               acc.get(), pend.get());
+      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(), acc.get(),
+                               pend.get());
       TM_LAUNCH();
-      k_commit<<<B, 32, 0, s>>>(t, seed, win.get(), acc.get(), st);
+      k_commit<<<B, 32, 0, s>>>(t, win.get(), acc.get(), st);
       TM_LAUNCH();
     }
+  };
+  cudaGraphExec_t group = nullptr;
+  if (s != nullptr && e->use_graphs) {
+    std::vector<unsigned char> key;
+    auto add = [&key](const void* p, size_t n) {
+      const unsigned char* b = static_cast<const unsigned char*>(p);
+      key.insert(key.end(), b, b + n);
+    };
+    const void* ptrs[] = {s, P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(), part.get(),
+                          okf.get(), dpn.get(), dpf.get(), acc.get(), e->sct.get(), m->d_to.get(),
+                          m->d_next.get(), m->d_face.get(), m->d_vout.get(), m->d_fhe.get(), m->d_slot.get(),
+                          m->d_nbr.get(), m->d_val.get(), m->d_fv.get(), m->d_edge.get()};
+    add(ptrs, sizeof ptrs);
+    const int ints[] = {B, mode, m->nv, m->ne, m->nf};
+    add(ints, sizeof ints);
+    add(&ep, sizeof ep);
+    add(&nlv, sizeof nlv);
+    add(&fe, sizeof fe);
+    add(&fg, sizeof fg);
+    if (!e->flip_graph.exec || e->flip_graph.key != key) {
+      if (e->flip_graph.exec) cudaGraphExecDestroy(e->flip_graph.exec);
+      e->flip_graph.exec = nullptr;
+      e->flip_graph.key.clear();
+      cudaGraph_t g = nullptr;
+      TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        launch_group();
+      } catch (...) {
+        cudaStreamEndCapture(s, &g);  // leave capture mode before reporting
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        throw;
+      }
+      TM_CUDA(cudaStreamEndCapture(s, &g));
+      cudaError_t rc = cudaGraphInstantiate(&e->flip_graph.exec, g, 0);
+      cudaGraphDestroy(g);
+      if (rc != cudaSuccess) e->flip_graph.exec = nullptr;
+      TM_CUDA(rc);
+      e->flip_graph.key.swap(key);
+    }
+    group = e->flip_graph.exec;
+  }
+  FlipState hs;
+  for (;;) {
+    if (group)
+      TM_CUDA(cudaGraphLaunch(group, s));
+    else
+      launch_group();
     TM_CUDA(cudaMemcpyAsync(&hs, st, sizeof(FlipState), cudaMemcpyDeviceToHost, s));
     TM_CUDA(cudaStreamSynchronize(s));
     if (hs.status) fail(TM_ERR_TOPOLOGY, "flip produced a valence above TM_MAXVAL");

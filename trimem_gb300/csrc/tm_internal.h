@@ -234,6 +234,7 @@ struct tm_energy {
   bool use_graphs = true;
   std::vector<EvalGraph> eval_graphs;
   unsigned long long eval_tick = 0;
+  EvalGraph flip_graph;  // one group of flip-sweep windows
   void ensure(int nv_, int ne_, int nf_);
   // copies n doubles from device memory to host memory dst and synchronises
   void to_host(double* dst, const double* src, size_t n);
