@@ -136,7 +136,7 @@ constexpr int VG = 6;  // ring slots loaded together by k_vertex
 template <bool VPROPS>
 __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__ fd, const EdgeD* __restrict__ ed,
                                               const double* __restrict__ ebond, const double* __restrict__ reppot,
-                                              EP ep, double* __restrict__ rho, double* __restrict__ vprops,
+                                              EP ep, double2* __restrict__ rk, double* __restrict__ vprops,
                                               double* __restrict__ partial, Globals* g) {
   __shared__ double red[6][VB];
   __shared__ bool last;
@@ -186,7 +186,8 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__
     pr[3] = 2 * c * c * ia;
     pr[4] = T * (1.0 / ep.tdiv);
     pr[5] = reppot[v];
-    rho[v] = c * ia;
+    const double rho = c * ia;
+    rk[v] = make_double2(ep.kb * rho, (ep.kb * (2.0 / 3.0)) * (rho * rho));
     if (VPROPS)
       for (int k = 0; k < 6; ++k) vprops[6 * (size_t)v + k] = pr[k];
   }
@@ -231,39 +232,46 @@ __global__ void k_assemble_props(EP ep, const double* props6, Globals* g) {
 }
 
 // ---- gradient gather ------------------------------------------------------
+// the sign bit of an edge's il is its boundary flag; tested and cleared as
+// integers (no FP64 compare or absolute value)
+__device__ __forceinline__ bool interior_edge(double il) { return __double_as_longlong(il) >= 0; }
+__device__ __forceinline__ double abs_bits(double x) {
+  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+}
+// rk[v] = (kb rho_v, 2/3 kb rho_v^2), written by k_vertex
 __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd,
-                                             const EdgeD* __restrict__ ed, const double* __restrict__ rho,
+                                             const EdgeD* __restrict__ ed, const double2* __restrict__ rk,
                                              const double* __restrict__ repg, const Globals* __restrict__ g, EP ep,
                                              double* __restrict__ grad) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= t.nv) return;
   const double gA = g->gA, gV = g->gV, gC = g->gC;
-  const double kb = ep.kb;
   const double hgC = 0.5 * gC;
-  const double kb23 = kb * (2.0 / 3.0);
   d3 xi = ld3(P, i);
-  double ri = rho[i];
+  const double2 qi = rk[i];
+  const double ai = gA - qi.y;   // alpha = gA - 2/3 kb (rho_i^2 + rho_j^2 + rho_k^2)
+  const double wi = hgC + qi.x;  // w = gC/2 + kb (rho_i + rho_j)
   d3 acc = ep.kr * ld3(repg, i);
   int d = t.val[i];
   if (d > 0) {
     const size_t nv = t.nv;
     int4 sp = t.slot[(size_t)(d - 1) * nv + i];
     d3 xk = ld3(P, sp.x);
-    double rk = rho[sp.x];
+    double2 qk = rk[sp.x];
     int4 sc = t.slot[i];
     d3 xj = ld3(P, sc.x);
-    double rj = rho[sc.x];
+    double2 qj = rk[sc.x];
     FaceD Fc;
     int fcur = slot_face(sc.y);
     if (fcur >= 0) Fc = fd[fcur];
     const double gV6 = gV * (1.0 / 6.0);
-    const double ri2 = ri * ri;
-    double rk2 = rk * rk, rj2 = rj * rj;
     // scalar multiples of face normals are summed per face: the dihedral
     // term of edge (i, j) reaches the normal of the next face, so its part
     // is carried to the next slot (the last one wraps to the first face)
     double carry = 0.0;
     d3 n0 = mk(0, 0, 0);
+    // length terms s_j (x_j - x_i): sum s_j x_j here, - (sum s_j) x_i at the end
+    double ssum = 0.0;
     for (int m = 0; m < d; ++m) {
       int4 sn = t.slot[(size_t)((m + 1) == d ? 0 : m + 1) * nv + i];
       int fnx = slot_face(sn.y);
@@ -278,7 +286,7 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
         if (m == 0) n0 = n;
         // face (i, j, k): area and volume terms, (alpha/2) n x (x_k - x_j)
         // + (gV/6) x_j x x_k = ((alpha/2) n + (gV/6) x_j) x (x_k - x_j)
-        double alpha = gA - kb23 * (ri2 + rj2 + rk2);
+        double alpha = (ai - qj.y) - qk.y;
         if (ep.btype == 1) alpha += ep.kt * 2.0 * (Fc.A / ep.a0 - 1.0) / ep.a0;
         d3 u = (0.5 * alpha) * n + gV6 * xj;
         d3 e = xk - xj;
@@ -287,36 +295,43 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
         acc.z = fma(u.x, e.y, fma(-u.y, e.x, acc.z));
         // edge (i, j): length and dihedral terms
         EdgeD E = ed[sc.z];
-        double w = hgC + kb * (ri + rj);
+        double w = wi + qj.x;
         double cl = w * E.th + (ep.btype == 0 ? ep.kt * E.db : 0.0);
-        acc += (-cl * fabs(E.il)) * (xj - xi);
+        const double sj = -cl * abs_bits(E.il);
+        ssum += sj;
+        acc.x = fma(sj, xj.x, acc.x);
+        acc.y = fma(sj, xj.y, acc.y);
+        acc.z = fma(sj, xj.z, acc.z);
         double cn = carry;
-        if (E.il > 0.0) {
+        if (interior_edge(E.il)) {
           int cin = slot_corner(sn.y);
           cn += w * cj;
           carry_next = w * cot_at(Fn, cin == 0 ? 2 : cin - 1);
         }
         // edge (j, k) opposite i: dihedral term
-        if (ed[sc.w].il > 0.0) cn -= (hgC + kb * (rj + rk)) * (cj + ck);
+        if (interior_edge(ed[sc.w].il)) cn -= ((hgC + qj.x) + qk.x) * (cj + ck);
         acc += cn * n;
       }
       carry = carry_next;
       xk = xj;
-      rk = rj;
-      rk2 = rj2;
+      qk = qj;
       sc = sn;
       fcur = fnx;
       Fc = Fn;
       xj = ld3(P, sn.x);
-      rj = rho[sn.x];
-      rj2 = rj * rj;
+      qj = rk[sn.x];
     }
     acc += carry * n0;  // the last edge's part on the first face
+    acc.x = fma(-ssum, xi.x, acc.x);
+    acc.y = fma(-ssum, xi.y, acc.y);
+    acc.z = fma(-ssum, xi.z, acc.z);
   }
   st3(grad, i, acc);
 }
 
 inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
+// the FP64 path's per-vertex curvature weights (kb rho, 2/3 kb rho^2)
+inline double2* rk2(tm_energy* e) { return reinterpret_cast<double2*>(e->rho.get()); }
 
 EP make_ep(const tm_energy* e) {
   const tm_params& p = e->prm;
@@ -488,15 +503,15 @@ static void eval_fp64_launches(tm_energy* e, tm_mesh* m, const double* P, bool w
     fork_repulsion(e, m, P, want_grad, s, false);
   int nb = std::max(1, nblk(t.nv, VB));
   if (want_vprops)
-    k_vertex<true><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, e->rho.get(),
+    k_vertex<true><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, rk2(e),
                                      e->vprops.get(), e->partials.get(), e->glob.get());
   else
-    k_vertex<false><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, e->rho.get(), nullptr,
+    k_vertex<false><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, rk2(e), nullptr,
                                       e->partials.get(), e->glob.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
   if (want_grad && t.nv)
-    k_grad<<<nblk(t.nv, 256), 256, 0, s>>>(t, P, fd, ed, e->rho.get(), e->repg.get(), e->glob.get(), ep, d_grad);
+    k_grad<<<nblk(t.nv, 256), 256, 0, s>>>(t, P, fd, ed, rk2(e), e->repg.get(), e->glob.get(), ep, d_grad);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[4], s));
 }
@@ -517,7 +532,7 @@ void tm_energy::ensure(int nv_, int ne_, int nf_) {
   face.ensure(8 * (size_t)std::max(nf, 1));
   edge.ensure(4 * (size_t)std::max(ne, 1));
   ebond.ensure(std::max(ne, 1));
-  rho.ensure(std::max(nv, 1));
+  rho.ensure(2 * (size_t)std::max(nv, 1));  // FP64 path: (kb rho, 2/3 kb rho^2) per vertex
   repg.ensure(3 * (size_t)std::max(nv, 1));
   reppot.ensure(std::max(nv, 1));
   // repulsion slow list (nv + 1) and short-bond edge list (ne + 1)
@@ -816,7 +831,7 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   size_t off_edge = off_face + align256(sizeof(FaceD) * nf);
   size_t off_ebond = off_edge + align256(sizeof(EdgeD) * ne);
   size_t off_rho = off_ebond + align256(sizeof(double) * ne);
-  size_t off_repg = off_rho + align256(sizeof(double) * nv);
+  size_t off_repg = off_rho + align256(sizeof(double2) * nv);
   size_t off_pos32 = off_repg + align256(3 * sizeof(double) * nv);
   size_t off_pot = off_pos32 + align256(3 * sizeof(float) * nv);
   size_t off_slow = off_pot + align256(sizeof(double) * nv);
@@ -827,13 +842,13 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   if (need > (size_t)TM_NOALLOC_SCRATCH_BYTES)
     fail(TM_ERR_ARG, "mesh needs " + std::to_string(need) + " bytes of scratch, more than the " +
                          std::to_string((size_t)TM_NOALLOC_SCRATCH_BYTES) +
-                         " bytes of tm_energy_eval_device_noalloc (about 53,000 vertices)");
+                         " bytes of tm_energy_eval_device_noalloc (about 51,000 vertices)");
   unsigned char* base = noalloc_scratch_for_current_device();
   cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
   FaceD* fd = reinterpret_cast<FaceD*>(base + off_face);
   EdgeD* ed = reinterpret_cast<EdgeD*>(base + off_edge);
   double* ebond = reinterpret_cast<double*>(base + off_ebond);
-  double* rho = reinterpret_cast<double*>(base + off_rho);
+  double2* rho = reinterpret_cast<double2*>(base + off_rho);
   double* repg = reinterpret_cast<double*>(base + off_repg);
   float* pos32 = reinterpret_cast<float*>(base + off_pos32);
   double* reppot = reinterpret_cast<double*>(base + off_pot);
