@@ -522,8 +522,8 @@ def main():
     kbytes = {
         "k_face": 3 * 4 * F + 24 * V + 64 * F,
         "k_edge": 16 * E + 24 * V + 64 * F + 40 * E,
-        "k_vertex": 4 * V + 16 * 2 * E + 64 * F + 40 * E + 24 * V + 8 * V + 24 * V + 16 * V,
-        "k_grad": 4 * V + 16 * 2 * E + 24 * V + 8 * V + 64 * F + 32 * E + 24 * V + 24 * V,
+        "k_vertex": 4 * V + 16 * 2 * E + 64 * F + 40 * E + 24 * V + 16 * V + 24 * V + 16 * V,
+        "k_grad": 4 * V + 16 * 2 * E + 24 * V + 16 * V + 64 * F + 32 * E + 24 * V + 24 * V,
     }
     peaks = read_peaks()
     hbm = peaks.get("hbm_gbs")
