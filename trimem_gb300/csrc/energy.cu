@@ -74,7 +74,8 @@ __global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__
   F.ny = N.y * inv;
   F.nz = N.z * inv;
   F.A = 0.5 * nn;
-  F.V = dot(cross(pa, pb), pc) * (1.0 / 6.0);
+  // (p_a x p_b) . p_c = p_a . ((p_b - p_a) x (p_c - p_a)) = p_a . N
+  F.V = dot(pa, N) * (1.0 / 6.0);
   F.c0 = dot(eab, eac) * inv;
   F.c1 = -dot(eab, ebc) * inv;
   F.c2 = dot(eac, ebc) * inv;
@@ -356,6 +357,13 @@ EP make_ep(const tm_energy* e) {
   ep.rT = sq_threshold(p.rep_lc1);
   ep.rr = p.rep_r;
   ep.tdiv = p.bond_type == 0 ? 2.0 : 3.0;
+  auto ipow_h = [](double x, int n) {  // the device's ipow, on the host
+    double r = 1.0;
+    for (int k = 0; k < std::abs(n); ++k) r *= x;
+    return n < 0 ? 1.0 / r : r;
+  };
+  ep.br1 = ipow_h((double)p.bond_r, p.bond_r + 1);
+  ep.br2 = ipow_h((double)p.bond_r, p.bond_r + 2);
   return ep;
 }
 

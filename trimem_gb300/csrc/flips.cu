@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, 
     if (ep.btype == 0) {
       int r = ep.r;
       if (el > ep.lc0)
-        tt = ipow((double)r, r + 1) * ipow(el - ep.lc0, r);
+        tt = ep.br1 * ipow(el - ep.lc0, r);
       else if (el < ep.lc1)
         tt = exp(el * (1.0 / (el - ep.lc1))) * ipow(il, r);
     } else {

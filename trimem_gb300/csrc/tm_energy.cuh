@@ -15,6 +15,7 @@ struct EP {
   double rlc1, rT;  // repulsion cut-off and its exact squared threshold
   int rr;
   double tdiv;
+  double br1, br2;  // r^(r+1) and r^(r+2) of the flat-bottom bond above lc0
 };
 
 struct __align__(16) FaceD {
@@ -355,8 +356,8 @@ __device__ __forceinline__ void edge_bond(const EP& ep, double l, double il, dou
   int r = ep.r;
   double v = 0.0, f = 0.0;
   if (l > ep.lc0) {
-    v = ipow((double)r, r + 1) * ipow(l - ep.lc0, r);
-    f = ipow((double)r, r + 2) * ipow(l - ep.lc0, r - 1);
+    v = ep.br1 * ipow(l - ep.lc0, r);
+    f = ep.br2 * ipow(l - ep.lc0, r - 1);
   }
   if (l < ep.lc1) {
     double ilm = 1.0 / (l - ep.lc1);
