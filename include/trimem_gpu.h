@@ -80,6 +80,12 @@ int tm_mesh_halfedge(tm_mesh* m, int op, int64_t h, int64_t* out);
 /* Whole topology: to/next/face per halfedge, outgoing halfedge per vertex,
  * halfedge per face (any pointer may be NULL). */
 int tm_mesh_topology(tm_mesh* m, int32_t* to, int32_t* next, int32_t* face, int32_t* vout, int32_t* fhe);
+/* replaces the connectivity by half-edge arrays of the same sizes (as
+ * tm_mesh_topology returns them, e.g. of a flipped mesh saved in a
+ * checkpoint), so that edge and face numbering are restored too; validated
+ * (ranges, triangles, manifold fans, TM_MAXVAL) before anything changes */
+int tm_mesh_set_topology(tm_mesh* m, const int32_t* to, const int32_t* next, const int32_t* face,
+                         const int32_t* vout, const int32_t* fhe);
 /* Device-side invariant check: closed 2-manifold fans, valence >= 3, no
  * double edges.  *status = 0 when valid, else a negative code. */
 int tm_mesh_check(tm_mesh* m, int* status);
@@ -100,6 +106,10 @@ int tm_energy_create(tm_mesh* m, const tm_params* p, tm_energy** out);
 int tm_energy_destroy(tm_energy* e);
 int tm_energy_get_params(tm_energy* e, tm_params* out);
 int tm_energy_initial_props(tm_energy* e, double* out6);
+/* restores the initial properties (the reference's EnergyManager computes
+ * them once from the constructing mesh, src/energy.cpp:13-28): a resumed
+ * run keeps the reference properties of the original one */
+int tm_energy_set_initial_props(tm_energy* e, const double* in6);
 int tm_energy_properties(tm_energy* e, tm_mesh* m, double* out6);
 int tm_energy_vertex_properties(tm_energy* e, tm_mesh* m, double* out6v);
 int tm_energy_energy(tm_energy* e, tm_mesh* m, double* energy);

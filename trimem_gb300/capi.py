@@ -109,6 +109,8 @@ _SIGS = {
     "tm_batch_update_repulsion": (_i32, [_p]),
     "tm_batch_hmc": (_i32, [_p, _i32, _i32, _d, _d, _d, ctypes.c_uint64, _i32, _ip]),
     "tm_batch_set_refresh": (_i32, [_p, _i32]),
+    "tm_energy_set_initial_props": (_i32, [_p, _dp]),
+    "tm_mesh_set_topology": (_i32, [_p, _ip, _ip, _ip, _ip, _ip]),
     "tm_minimize_device": (_i32, [_p, _p, _p, _i32, _i32, _d, _d, _ip, _dp, _p]),
     "tm_surrogate_create": (_i32, [_p, ctypes.POINTER(ctypes.c_float), _i64, _pp]),
     "tm_surrogate_destroy": (_i32, [_p]),
@@ -198,6 +200,14 @@ class Mesh:
         check(lib().tm_mesh_topology(self.h, *[_iptr(a) for a in arrs]))
         return dict(zip(["to", "next", "face", "vout", "fhe"], arrs))
 
+    def set_topology(self, topo):
+        """Connectivity from half-edge arrays (the dict ``topology`` returns)."""
+        arrs = [np.ascontiguousarray(topo[k], dtype=np.int32) for k in ["to", "next", "face", "vout", "fhe"]]
+        nv, ne, nf = self.counts()
+        if [len(a) for a in arrs] != [2 * ne] * 3 + [nv, nf]:
+            raise ValueError("topology arrays do not match the mesh sizes")
+        check(lib().tm_mesh_set_topology(self.h, *[_iptr(a) for a in arrs]))
+
     def check(self):
         s = ctypes.c_int32()
         check(lib().tm_mesh_check(self.h, ctypes.byref(s)))
@@ -278,6 +288,17 @@ class Energy:
         check(lib().tm_energy_initial_props(self.h, _dptr(out)))
         return out
 
+    def set_initial_props(self, props6):
+        v = np.ascontiguousarray(props6, dtype=np.float64)
+        if v.shape != (6,):
+            raise ValueError("six initial properties expected")
+        check(lib().tm_energy_set_initial_props(self.h, _dptr(v)))
+
+    def params(self):
+        out = Params()
+        check(lib().tm_energy_get_params(self.h, ctypes.byref(out)))
+        return out
+
     def update_reference_properties(self):
         check(lib().tm_energy_update_reference_properties(self.h))
 
@@ -286,6 +307,7 @@ class Energy:
 
     def set_stencil_precision(self, mode):
         check(lib().tm_energy_set_stencil_precision(self.h, int(mode)))
+        self.stencil = int(mode)
 
     def fd_gradient(self, mesh, eps):
         out = np.empty((mesh.counts()[0], 3))

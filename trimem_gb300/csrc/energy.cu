@@ -53,7 +53,9 @@ using namespace tmg;
 namespace tmg {
 
 // ---- per-face and per-edge quantities ------------------------------------
-__global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__ fd, float* __restrict__ P32) {
+// fav: (area, volume) of each face again, compact, for k_vertex's gathers
+__global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__ fd, float* __restrict__ P32,
+                       double2* __restrict__ fav) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   // the float copy of the positions used by the neighbour prefilter
   for (int v = f; v < t.nv; v += gridDim.x * blockDim.x) {
@@ -80,10 +82,13 @@ __global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__
   F.c1 = -dot(eab, ebc) * inv;
   F.c2 = dot(eac, ebc) * inv;
   fd[f] = F;
+  fav[f] = make_double2(F.A, F.V);
 }
 
+// elt: (l theta, bond value) of each edge, compact, for k_vertex's gathers
+// (the bond value of short edges is filled in by k_bond_short)
 __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd, EdgeD* __restrict__ ed,
-                       double* __restrict__ ebond, EP ep, int* __restrict__ blist, int* __restrict__ bcnt,
+                       double2* __restrict__ elt, EP ep, int* __restrict__ blist, int* __restrict__ bcnt,
                        const double2* __restrict__ sct) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= t.ne) return;
@@ -116,11 +121,11 @@ __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __rest
   if (ep.btype == 0 && !shortb && l > ep.lc0) edge_bond(ep, l, il, &val, &fac);
   warp_append(shortb, e, blist, bcnt);  o.db = fac;
   ed[e] = o;
-  ebond[e] = val;
+  elt[e] = make_double2(o.l * o.th, val);
 }
 
 __global__ void k_bond_short(const double* __restrict__ P, Topo t, EdgeD* __restrict__ ed,
-                             double* __restrict__ ebond, EP ep, const int* __restrict__ blist,
+                             double2* __restrict__ elt, EP ep, const int* __restrict__ blist,
                              const int* __restrict__ bcnt) {
   int n = *bcnt;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -129,14 +134,14 @@ __global__ void k_bond_short(const double* __restrict__ P, Topo t, EdgeD* __rest
     const EdgeD E = ed[e];
     edge_bond(ep, E.l, fabs(E.il), &val, &fac);
     ed[e].db = fac;
-    ebond[e] = val;
+    elt[e].y = val;
   }
 }
 
 constexpr int VG = 6;  // ring slots loaded together by k_vertex
 template <bool VPROPS>
-__global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__ fd, const EdgeD* __restrict__ ed,
-                                              const double* __restrict__ ebond, const double* __restrict__ reppot,
+__global__ void __launch_bounds__(VB) k_vertex(Topo t, const double2* __restrict__ fav,
+                                              const double2* __restrict__ elt, const double* __restrict__ reppot,
                                               EP ep, double2* __restrict__ rk, double* __restrict__ vprops,
                                               double* __restrict__ partial, Globals* g) {
   __shared__ double red[6][VB];
@@ -158,11 +163,11 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const FaceD* __restrict__
         int f = slot_face(s[k].y);
         fa[k] = fv[k] = lt[k] = tb[k] = 0.0;
         if (f >= 0) {
-          fa[k] = fd[f].A;
-          fv[k] = fd[f].V;
-          EdgeD E = ed[s[k].z];
-          lt[k] = E.l * E.th;
-          if (ep.btype == 0) tb[k] = ebond[s[k].z];
+          const double2 av = fav[f], lb = elt[s[k].z];
+          fa[k] = av.x;
+          fv[k] = av.y;
+          lt[k] = lb.x;
+          if (ep.btype == 0) tb[k] = lb.y;
         }
       }
 #pragma unroll
@@ -333,6 +338,9 @@ __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__
 inline int nblk(long n, int b) { return (int)((n + b - 1) / b); }
 // the FP64 path's per-vertex curvature weights (kb rho, 2/3 kb rho^2)
 inline double2* rk2(tm_energy* e) { return reinterpret_cast<double2*>(e->rho.get()); }
+// the FP64 path's compact (area, volume) per face and (l theta, bond) per edge
+inline double2* fav2(tm_energy* e) { return reinterpret_cast<double2*>(e->fav.get()); }
+inline double2* elt2(tm_energy* e) { return reinterpret_cast<double2*>(e->ebond.get()); }
 
 EP make_ep(const tm_energy* e) {
   const tm_params& p = e->prm;
@@ -396,8 +404,8 @@ static std::vector<unsigned char> eval_key(tm_energy* e, tm_mesh* m, const doubl
     const unsigned char* b = static_cast<const unsigned char*>(p);
     k.insert(k.end(), b, b + n);
   };
-  const void* ptrs[] = {P, d_grad, s, e->face.get(), e->edge.get(), e->ebond.get(), e->rho.get(), e->repg.get(),
-                        e->reppot.get(), e->slow.get(), e->pos32.get(), e->poslo.get(), e->partials.get(),
+  const void* ptrs[] = {P, d_grad, s, e->face.get(), e->edge.get(), e->ebond.get(), e->fav.get(), e->rho.get(),
+                        e->repg.get(), e->reppot.get(), e->slow.get(), e->pos32.get(), e->poslo.get(), e->partials.get(),
                         e->glob.get(), e->sct.get(), e->aux, e->ev_fork, e->ev_join, e->nl.xb.get()};
   add(ptrs, sizeof ptrs);
   const Topo t = m->topo();
@@ -490,7 +498,7 @@ static void eval_fp64_launches(tm_energy* e, tm_mesh* m, const double* P, bool w
   NLView nlv = e->nl.view;
   nlv.pos32 = e->pos32.get();
   int nfb = std::max(nblk(std::max(t.nf, t.nv), 256), 1);
-  k_face<<<nfb, 256, 0, s>>>(t, P, fd, e->pos32.get());
+  k_face<<<nfb, 256, 0, s>>>(t, P, fd, e->pos32.get(), fav2(e));
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
   // the repulsion pass needs only the positions: it overlaps the edge kernels
@@ -500,9 +508,9 @@ static void eval_fp64_launches(tm_energy* e, tm_mesh* m, const double* P, bool w
   int* blist = e->slow.get() + std::max(m->nv, 1) + 1;
   int* bcnt = blist + std::max(m->ne, 1);
   TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
-  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, e->ebond.get(), ep, blist, bcnt, e->sct.get());
+  if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, P, fd, ed, elt2(e), ep, blist, bcnt, e->sct.get());
   TM_LAUNCH();
-  if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(P, t, ed, e->ebond.get(), ep, blist, bcnt);
+  if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(P, t, ed, elt2(e), ep, blist, bcnt);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
   if (conc)
@@ -511,10 +519,10 @@ static void eval_fp64_launches(tm_energy* e, tm_mesh* m, const double* P, bool w
     fork_repulsion(e, m, P, want_grad, s, false);
   int nb = std::max(1, nblk(t.nv, VB));
   if (want_vprops)
-    k_vertex<true><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, rk2(e),
+    k_vertex<true><<<nb, VB, 0, s>>>(t, fav2(e), elt2(e), e->reppot.get(), ep, rk2(e),
                                      e->vprops.get(), e->partials.get(), e->glob.get());
   else
-    k_vertex<false><<<nb, VB, 0, s>>>(t, fd, ed, e->ebond.get(), e->reppot.get(), ep, rk2(e), nullptr,
+    k_vertex<false><<<nb, VB, 0, s>>>(t, fav2(e), elt2(e), e->reppot.get(), ep, rk2(e), nullptr,
                                       e->partials.get(), e->glob.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
@@ -539,7 +547,8 @@ void tm_energy::ensure(int nv_, int ne_, int nf_) {
   nf = nf_;
   face.ensure(8 * (size_t)std::max(nf, 1));
   edge.ensure(4 * (size_t)std::max(ne, 1));
-  ebond.ensure(std::max(ne, 1));
+  ebond.ensure(2 * (size_t)std::max(ne, 1));  // FP64 path: (l theta, bond value) per edge
+  fav.ensure(2 * (size_t)std::max(nf, 1));    // FP64 path: (area, volume) per face
   rho.ensure(2 * (size_t)std::max(nv, 1));  // FP64 path: (kb rho, 2/3 kb rho^2) per vertex
   repg.ensure(3 * (size_t)std::max(nv, 1));
   reppot.ensure(std::max(nv, 1));
@@ -641,6 +650,13 @@ int tm_energy_initial_props(tm_energy* e, double* out6) {
   if (!e || !out6) return TM_ERR_ARG;
   std::memcpy(out6, e->initial, sizeof(double) * 6);
   return TM_OK;
+}
+
+int tm_energy_set_initial_props(tm_energy* e, const double* in6) {
+  TM_API_BEGIN
+  if (!e || !in6) fail(TM_ERR_ARG, "NULL argument");
+  std::memcpy(e->initial, in6, sizeof(double) * 6);
+  TM_API_END
 }
 
 int tm_energy_properties(tm_energy* e, tm_mesh* m, double* out6) {
@@ -838,7 +854,8 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   size_t off_face = 0;
   size_t off_edge = off_face + align256(sizeof(FaceD) * nf);
   size_t off_ebond = off_edge + align256(sizeof(EdgeD) * ne);
-  size_t off_rho = off_ebond + align256(sizeof(double) * ne);
+  size_t off_fav = off_ebond + align256(sizeof(double2) * ne);
+  size_t off_rho = off_fav + align256(sizeof(double2) * nf);
   size_t off_repg = off_rho + align256(sizeof(double2) * nv);
   size_t off_pos32 = off_repg + align256(3 * sizeof(double) * nv);
   size_t off_pot = off_pos32 + align256(3 * sizeof(float) * nv);
@@ -850,12 +867,13 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   if (need > (size_t)TM_NOALLOC_SCRATCH_BYTES)
     fail(TM_ERR_ARG, "mesh needs " + std::to_string(need) + " bytes of scratch, more than the " +
                          std::to_string((size_t)TM_NOALLOC_SCRATCH_BYTES) +
-                         " bytes of tm_energy_eval_device_noalloc (about 51,000 vertices)");
+                         " bytes of tm_energy_eval_device_noalloc (about 44,000 vertices)");
   unsigned char* base = noalloc_scratch_for_current_device();
   cudaStream_t s = stream ? (cudaStream_t)stream : e->stream;
   FaceD* fd = reinterpret_cast<FaceD*>(base + off_face);
   EdgeD* ed = reinterpret_cast<EdgeD*>(base + off_edge);
-  double* ebond = reinterpret_cast<double*>(base + off_ebond);
+  double2* ebond = reinterpret_cast<double2*>(base + off_ebond);
+  double2* fav = reinterpret_cast<double2*>(base + off_fav);
   double2* rho = reinterpret_cast<double2*>(base + off_rho);
   double* repg = reinterpret_cast<double*>(base + off_repg);
   float* pos32 = reinterpret_cast<float*>(base + off_pos32);
@@ -872,7 +890,7 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   NLView nlv = e->nl.view;
   nlv.pos32 = pos32;
   int nfb = std::max(nblk(std::max(t.nf, t.nv), 256), 1);
-  k_face<<<nfb, 256, 0, s>>>(t, d_points, fd, pos32);
+  k_face<<<nfb, 256, 0, s>>>(t, d_points, fd, pos32, fav);
   TM_LAUNCH();
   TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
   if (t.ne) k_edge<<<nblk(t.ne, 256), 256, 0, s>>>(t, d_points, fd, ed, ebond, ep, blist, bcnt, e->sct.get());
@@ -880,7 +898,7 @@ extern "C" int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const dou
   if (t.ne) k_bond_short<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(d_points, t, ed, ebond, ep, blist, bcnt);
   TM_LAUNCH();
   repulsion_eval(e, m, d_points, pos32, true, reppot, repg, slow, slow + nv, s);
-  k_vertex<false><<<nb, VB, 0, s>>>(t, fd, ed, ebond, reppot, ep, rho, nullptr, part, g);
+  k_vertex<false><<<nb, VB, 0, s>>>(t, fav, ebond, reppot, ep, rho, nullptr, part, g);
   TM_LAUNCH();
   if (t.nv) k_grad<<<nblk(t.nv, 256), 256, 0, s>>>(t, d_points, fd, ed, rho, repg, g, ep, d_grad);
   TM_LAUNCH();

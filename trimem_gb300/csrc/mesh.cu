@@ -518,6 +518,55 @@ int tm_mesh_topology(tm_mesh* m, int32_t* to, int32_t* next, int32_t* face, int3
   TM_API_END
 }
 
+int tm_mesh_set_topology(tm_mesh* m, const int32_t* to, const int32_t* next, const int32_t* face,
+                         const int32_t* vout, const int32_t* fhe) {
+  TM_API_BEGIN
+  if (!m || !to || !next || !face || !vout || !fhe) fail(TM_ERR_ARG, "NULL argument");
+  const int nh = 2 * m->ne, nv = m->nv, nf = m->nf;
+  // the arrays must describe a valid half-edge mesh of the same size
+  for (int h = 0; h < nh; ++h) {
+    if (to[h] < 0 || to[h] >= nv || next[h] < 0 || next[h] >= nh || face[h] < -1 || face[h] >= nf)
+      fail(TM_ERR_TOPOLOGY, "half-edge index out of range");
+    if (to[h] == to[h ^ 1]) fail(TM_ERR_TOPOLOGY, "degenerate edge");
+  }
+  for (int f = 0; f < nf; ++f) {
+    int h = fhe[f];
+    if (h < 0 || h >= nh || face[h] != f) fail(TM_ERR_TOPOLOGY, "face half-edge mismatch");
+    int h1 = next[h], h2 = next[h1];
+    if (face[h1] != f || face[h2] != f || next[h2] != h) fail(TM_ERR_TOPOLOGY, "face is not a triangle");
+  }
+  std::vector<int> deg(nv, 0);
+  for (int h = 0; h < nh; ++h) deg[to[h ^ 1]]++;
+  for (int v = 0; v < nv; ++v) {
+    const int h0 = vout[v];
+    if (h0 < -1 || h0 >= nh || (h0 >= 0 && to[h0 ^ 1] != v) || (h0 < 0 && deg[v] > 0))
+      fail(TM_ERR_TOPOLOGY, "vertex half-edge mismatch");
+    if (deg[v] > TM_MAXVAL) fail(TM_ERR_TOPOLOGY, "vertex valence exceeds TM_MAXVAL");
+    if (h0 < 0) continue;
+    int c = 0, h = h0;
+    do {
+      ++c;
+      h = next[h ^ 1];
+    } while (h != h0 && c <= deg[v]);
+    if (c != deg[v]) fail(TM_ERR_TOPOLOGY, "non-manifold vertex");
+  }
+  m->h_to.assign(to, to + nh);
+  m->h_next.assign(next, next + nh);
+  m->h_face.assign(face, face + nh);
+  m->h_vout.assign(vout, vout + nv);
+  m->h_fhe.assign(fhe, fhe + nf);
+  m->closed = true;
+  for (int h = 0; h < nh; ++h) m->closed = m->closed && face[h] >= 0;
+  upload_topology(m);
+  m->host_topo_stale = false;
+  // a new topology: exclusion flags kept with neighbour rows are not trusted
+  ++m->topo_version;
+  const int ver = (int)(m->topo_version & 0x7fffffff);
+  TM_CUDA(cudaMemcpyAsync(m->d_topo_ver.get(), &ver, sizeof(int), cudaMemcpyHostToDevice, m->stream));
+  TM_CUDA(cudaStreamSynchronize(m->stream));
+  TM_API_END
+}
+
 int tm_mesh_check(tm_mesh* m, int* status) {
   TM_API_BEGIN
   if (!m || !status) fail(TM_ERR_ARG, "NULL argument");

@@ -207,7 +207,7 @@ struct tm_energy {
   int stencil = 0;  // 0 FP64, 1 FP32
   tm_nlist nl;
   int nv = 0, ne = 0, nf = 0;
-  tmg::DevBuf<double> face, edge, ebond, rho, repg, reppot, vprops, partials, grad, work;
+  tmg::DevBuf<double> face, edge, ebond, fav, rho, repg, reppot, vprops, partials, grad, work;
   tmg::DevBuf<int> slow;  // vertices that left their build cell (+ count)
   tmg::DevBuf<float> pos32, poslo;
   tmg::DevBuf<tmg::Globals> glob;
