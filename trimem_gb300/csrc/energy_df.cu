@@ -68,7 +68,8 @@ __global__ void k_split_df(int n3, const double* __restrict__ P, float* __restri
   lo[i] = (float)(x - (double)h);
 }
 
-__global__ void __launch_bounds__(256) k_face_df(Topo t, PosDF X, FaceDF* __restrict__ fd) {
+// fav: (area, volume) again as (hi, lo, hi, lo), compact for k_vertex_df
+__global__ void __launch_bounds__(256) k_face_df(Topo t, PosDF X, FaceDF* __restrict__ fd, float4* __restrict__ fav) {
   int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= t.nf) return;
   int a = t.fv[3 * f], b = t.fv[3 * f + 1], c = t.fv[3 * f + 2];
@@ -87,10 +88,13 @@ __global__ void __launch_bounds__(256) k_face_df(Topo t, PosDF X, FaceDF* __rest
   F.c1 = -(ddot(eab, ebc) * inv);
   F.c2 = ddot(eac, ebc) * inv;
   fd[f] = F;
+  fav[f] = make_float4(F.A.hi, F.A.lo, F.V.hi, F.V.lo);
 }
 
+// elt: (l theta, bond value) as (hi, lo, hi, lo), compact for k_vertex_df
+// (the bond value of short edges is filled in by k_bond_short_df)
 __global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* __restrict__ fd,
-                                                EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep, EPD epd,
+                                                EdgeDF* __restrict__ ed, float4* __restrict__ elt, EP ep, EPD epd,
                                                 int* __restrict__ blist, int* __restrict__ bcnt) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= t.ne) return;
@@ -128,7 +132,8 @@ __global__ void __launch_bounds__(256) k_edge_df(Topo t, PosDF X, const FaceDF* 
   }
   warp_append(shortb, e, blist, bcnt);
   ed[e] = o;
-  ebond[e] = val;
+  const df lt = o.l * o.th;
+  elt[e] = make_float4(lt.hi, lt.lo, val.hi, val.lo);
 }
 
 // Flat-bottom bond of an edge shorter than lc1 (src/mesh_tether.h:29-85)
@@ -154,7 +159,7 @@ __device__ __forceinline__ void edge_bond_short_df(const EP& ep, const EPD& epd,
   *fac = (f * ilr) * ex;
 }
 
-__global__ void k_bond_short_df(EdgeDF* __restrict__ ed, df* __restrict__ ebond, EP ep, EPD epd,
+__global__ void k_bond_short_df(EdgeDF* __restrict__ ed, float4* __restrict__ elt, EP ep, EPD epd,
                                 const int* __restrict__ blist, const int* __restrict__ bcnt) {
   int n = *bcnt;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -163,19 +168,22 @@ __global__ void k_bond_short_df(EdgeDF* __restrict__ ed, df* __restrict__ ebond,
       df val, fac;
       edge_bond_short_df(ep, epd, ed[e].l, &val, &fac);
       ed[e].db = fac;
-      ebond[e] = val;
+      elt[e].z = val.hi;
+      elt[e].w = val.lo;
     } else {  // non-positive exponents: FP64
       double val, fac;
       const double l = df_to(ed[e].l);
       edge_bond(ep, l, 1.0 / l, &val, &fac);
       ed[e].db = df_from(fac);
-      ebond[e] = df_from(val);
+      const df v = df_from(val);
+      elt[e].z = v.hi;
+      elt[e].w = v.lo;
     }
   }
 }
 
-__global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const FaceDF* __restrict__ fd,
-                                                 const EdgeDF* __restrict__ ed, const df* __restrict__ ebond,
+__global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const float4* __restrict__ fav,
+                                                 const float4* __restrict__ elt,
                                                  const double* __restrict__ reppot, EP ep, EPD epd,
                                                  df* __restrict__ rho, double* __restrict__ partial, Globals* g) {
   __shared__ float2 red[6][VB];
@@ -187,35 +195,35 @@ __global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const FaceDF* __restri
   if (v < t.nv) {
     int d = t.val[v];
     df A = df_make(0.0f), V = df_make(0.0f), LT = df_make(0.0f), T = df_make(0.0f);
-    // slots in groups of four: all loads of a group are issued before the
-    // sums, which keep the slot order
-    for (int m0 = 0; m0 < d; m0 += 4) {
-      int4 s[4];
+    // slots in groups of six (one group at the usual valence): all loads of
+    // a group (16-byte compact records) are issued before the sums, which
+    // keep the slot order
+    constexpr int G = 6;
+    for (int m0 = 0; m0 < d; m0 += G) {
+      int4 s[G];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) s[k] = m0 + k < d ? t.slot[(size_t)(m0 + k) * t.nv + v] : make_int4(0, -1, 0, 0);
-      df fa[4], fv[4], el[4], eth[4], tb[4];
+      for (int k = 0; k < G; ++k) s[k] = m0 + k < d ? t.slot[(size_t)(m0 + k) * t.nv + v] : make_int4(0, -1, 0, 0);
+      float4 av[G], lb[G];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < G; ++k) {
         int f = slot_face(s[k].y);
-        fa[k] = fv[k] = el[k] = eth[k] = tb[k] = df_make(0.0f);
+        av[k] = lb[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (f >= 0) {
-          fa[k] = fd[f].A;
-          fv[k] = fd[f].V;
-          el[k] = ed[s[k].z].l;
-          eth[k] = ed[s[k].z].th;
-          if (ep.btype == 0) tb[k] = ebond[s[k].z];
+          av[k] = fav[f];
+          lb[k] = elt[s[k].z];
         }
       }
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < G; ++k) {
         if (slot_face(s[k].y) < 0) continue;
-        A += fa[k];
-        V += fv[k];
-        LT += el[k] * eth[k];
+        const df fa = {av[k].x, av[k].y}, fv = {av[k].z, av[k].w}, lt = {lb[k].x, lb[k].y}, tb = {lb[k].z, lb[k].w};
+        A += fa;
+        V += fv;
+        LT += lt;
         if (ep.btype == 0) {
-          T += tb[k];
+          T += tb;
         } else {
-          df q = fa[k] * epd.inv_a0 - df_make(1.0f);
+          df q = fa * epd.inv_a0 - df_make(1.0f);
           T += q * q;
         }
       }
@@ -384,14 +392,15 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   PosDF X{e->pos32.get(), e->poslo.get()};
   FaceDF* fd = reinterpret_cast<FaceDF*>(e->face.get());
   EdgeDF* ed = reinterpret_cast<EdgeDF*>(e->edge.get());
-  df* eb = reinterpret_cast<df*>(e->ebond.get());
+  float4* eb = reinterpret_cast<float4*>(e->ebond.get());  // (l theta, bond) per edge, 16 bytes
+  float4* fav = reinterpret_cast<float4*>(e->fav.get());    // (area, volume) per face, 16 bytes
   df* rho = reinterpret_cast<df*>(e->rho.get());
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
   if (m->nv) k_split_df<<<nblk(3L * m->nv, 256), 256, 0, s>>>(3 * m->nv, P, e->pos32.get(), e->poslo.get());
   TM_LAUNCH();
   const bool conc = ev == nullptr;  // repulsion overlaps the face and edge kernels
   if (conc) fork_repulsion(e, m, P, want_grad, s, true);
-  if (t.nf) k_face_df<<<nblk(t.nf, 256), 256, 0, s>>>(t, X, fd);
+  if (t.nf) k_face_df<<<nblk(t.nf, 256), 256, 0, s>>>(t, X, fd, fav);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
   int* blist = e->slow.get() + std::max(m->nv, 1) + 1;
@@ -407,7 +416,7 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   else
     fork_repulsion(e, m, P, want_grad, s, false);
   int nb = std::max(1, nblk(t.nv, VB));
-  k_vertex_df<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), ep, epd, rho, e->partials.get(), e->glob.get());
+  k_vertex_df<<<nb, VB, 0, s>>>(t, fav, eb, e->reppot.get(), ep, epd, rho, e->partials.get(), e->glob.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[3], s));
   if (want_grad && t.nv)
