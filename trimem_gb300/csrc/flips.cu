@@ -20,14 +20,17 @@
 //             exclusion rings, and reduces them to the property change of
 //             the flip and -log(u)
 //   k_metro   Metropolis with T = 1 in slot order (flips.cpp:142-160): one
-//             block tries all remaining slots on the current state, takes
-//             the first accepted one and repeats from there; losers are
-//             queued for the next window
+//             block decides every slot whose float-filtered decision cannot
+//             be changed by earlier acceptances and walks the rest, with the
+//             robustly accepted ones, in order with the FP64 test; losers
+//             are queued for the next window
 //   k_commit  accepted flips rewrite their six halfedges, two faces, five
 //             edge rows and four ring rows (one block per flip); patches are
 //             disjoint, so commits never touch the same entries
 // Proposals come from a counter-based SplitMix64 stream of (seed, index), so
-// a sweep is reproducible and matches the CPU port of this algorithm.
+// a sweep is reproducible and matches the CPU port of this algorithm.  The
+// seed lives in the sweep state in device memory, so the 48 launches of a
+// group of eight windows are captured once as a CUDA graph and replayed.
 // A flip is also refused when it would raise a valence above TM_MAXVAL.
 #include <algorithm>
 #include <climits>
