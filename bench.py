@@ -523,7 +523,7 @@ def main():
     kbytes = {
         "k_face": 3 * 4 * F + 24 * V + 64 * F,
         "k_edge": 16 * E + 24 * V + 64 * F + 40 * E,
-        "k_vertex": 4 * V + 16 * 2 * E + 64 * F + 40 * E + 24 * V + 16 * V + 24 * V + 16 * V,
+        "k_vertex": 4 * V + 16 * 2 * E + 16 * F + 16 * E + 8 * V + 16 * V,  # valence, slots, (A, V), (l th, bond), pot, rk
         "k_grad": 4 * V + 16 * 2 * E + 24 * V + 16 * V + 64 * F + 32 * E + 24 * V + 24 * V,
     }
     peaks = read_peaks()
