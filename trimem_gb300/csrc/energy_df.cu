@@ -185,7 +185,7 @@ __global__ void k_bond_short_df(EdgeDF* __restrict__ ed, float4* __restrict__ el
 __global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const float4* __restrict__ fav,
                                                  const float4* __restrict__ elt,
                                                  const double* __restrict__ reppot, EP ep, EPD epd,
-                                                 df* __restrict__ rho, double* __restrict__ partial, Globals* g) {
+                                                 float4* __restrict__ rk, double* __restrict__ partial, Globals* g) {
   __shared__ float2 red[6][VB];
   __shared__ double redd[6][VB];
   __shared__ bool last;
@@ -236,7 +236,9 @@ __global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const float4* __restri
     pr[4] = T * epd.inv_tdiv;
     double pot = reppot[v];
     pr[5] = pot == 0.0 ? df_make(0.0f) : df_from(pot);
-    rho[v] = c / a;
+    const df rho = c / a;
+    const df kr = epd.kb * rho, kq = epd.kb23 * (rho * rho);
+    rk[v] = make_float4(kr.hi, kr.lo, kq.hi, kq.lo);  // (kb rho, 2/3 kb rho^2)
   }
   // fixed-order double-float tree over the block, FP64 across blocks
   for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = make_float2(pr[k].hi, pr[k].lo);
@@ -278,8 +280,11 @@ __global__ void __launch_bounds__(VB) k_vertex_df(Topo t, const float4* __restri
 
 __device__ __forceinline__ df cot_df(const FaceDF& F, int c) { return c == 0 ? F.c0 : (c == 1 ? F.c1 : F.c2); }
 
+struct df4 {  // two double-float values
+  df a, b;
+};
 __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* __restrict__ fd,
-                                                const EdgeDF* __restrict__ ed, const df* __restrict__ rho,
+                                                const EdgeDF* __restrict__ ed, const float4* __restrict__ rk,
                                                 const double* __restrict__ repg, const Globals* __restrict__ g,
                                                 EP ep, EPD epd, double* __restrict__ grad) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -287,9 +292,15 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
   const df gA = {g->gdf[0], g->gdf[1]}, gV = {g->gdf[2], g->gdf[3]}, gC = {g->gdf[4], g->gdf[5]};
   const df hgC = ldexp2(gC, 0.5f);
   const df gV6 = gV * sixth();
-  const df kb = epd.kb;
   df3 xi = X.at(i);
-  df ri = rho[i];
+  // per-vertex weights (kb rho, 2/3 kb rho^2) from k_vertex_df:
+  // alpha = gA - 2/3 kb (rho_i^2 + rho_j^2 + rho_k^2), w = gC/2 + kb (rho_i + rho_j)
+  auto q_of = [&](int v) {
+    const float4 q = rk[v];
+    return df4{df{q.x, q.y}, df{q.z, q.w}};
+  };
+  const df4 qi = q_of(i);
+  const df ai = gA - qi.b, wi = hgC + qi.a;
   df3 acc = {df_make(0.0f), df_make(0.0f), df_make(0.0f)};
   // volume term sum_f (x_j x x_k)/6 with x = x_i + d: the x_i x (d_k - d_j)
   // parts telescope around the fan, so only sum d_j x d_k and, for open
@@ -300,10 +311,10 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
     const size_t nv = t.nv;
     int4 sp = t.slot[(size_t)(d - 1) * nv + i];
     df3 dk = X.at(sp.x) - xi;  // x_k - x_i
-    df rk = rho[sp.x];
+    df4 qk = q_of(sp.x);
     int4 sc = t.slot[i];
     df3 dj = X.at(sc.x) - xi;
-    df rj = rho[sc.x];
+    df4 qj = q_of(sc.x);
     int fcur = slot_face(sc.y);
     // scalar multiples of face normals are summed per face: the dihedral
     // term of edge (i, j) reaches the normal of the next face, so its part
@@ -322,7 +333,7 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
         df3 n = {Fc.nx, Fc.ny, Fc.nz};
         if (m == 0) n0 = n;
         // face (i, j, k): area and volume terms
-        df alpha = gA - epd.kb23 * (ri * ri + rj * rj + rk * rk);
+        df alpha = (ai - qj.b) - qk.b;
         if (ep.btype == 1) alpha += ldexp2(epd.kt * (Fc.A * epd.inv_a0 - df_make(1.0f)) * epd.inv_a0, 2.0f);
         df3 dkj = dk - dj;
         acc += ldexp2(alpha, 0.5f) * dcross(n, dkj);
@@ -330,7 +341,7 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
         vtel += dkj;
         // edge (i, j): length and dihedral terms
         const EdgeDF& E = ed[sc.z];
-        df w = hgC + kb * (ri + rj);
+        df w = wi + qj.a;
         df cl = w * E.th;
         if (ep.btype == 0) cl += epd.kt * E.db;
         const df il = E.il.hi < 0.0f ? -E.il : E.il;
@@ -342,16 +353,16 @@ __global__ void __launch_bounds__(256) k_grad_df(Topo t, PosDF X, const FaceDF* 
           carry_next = w * cot_df(fd[fnx], cin == 0 ? 2 : cin - 1);
         }
         // edge (j, k) opposite i: dihedral term
-        if (ed[sc.w].il.hi > 0.0f) cn -= (hgC + kb * (rj + rk)) * (cj + ck);
+        if (ed[sc.w].il.hi > 0.0f) cn -= ((hgC + qj.a) + qk.a) * (cj + ck);
         acc += cn * n;
       }
       carry = carry_next;
       dk = dj;
-      rk = rj;
+      qk = qj;
       sc = sn;
       fcur = fnx;
       dj = X.at(sn.x) - xi;
-      rj = rho[sn.x];
+      qj = q_of(sn.x);
     }
     acc += carry * n0;  // the last edge's part on the first face
   }
@@ -394,7 +405,7 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   EdgeDF* ed = reinterpret_cast<EdgeDF*>(e->edge.get());
   float4* eb = reinterpret_cast<float4*>(e->ebond.get());  // (l theta, bond) per edge, 16 bytes
   float4* fav = reinterpret_cast<float4*>(e->fav.get());    // (area, volume) per face, 16 bytes
-  df* rho = reinterpret_cast<df*>(e->rho.get());
+  float4* rho = reinterpret_cast<float4*>(e->rho.get());  // (kb rho, 2/3 kb rho^2) per vertex
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
   if (m->nv) k_split_df<<<nblk(3L * m->nv, 256), 256, 0, s>>>(3 * m->nv, P, e->pos32.get(), e->poslo.get());
   TM_LAUNCH();
