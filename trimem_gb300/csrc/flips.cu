@@ -86,6 +86,7 @@ struct FlipState {
   double props[8];
   double e0;
   unsigned long long seed;  // proposal stream of the sweep
+  int nacc_win;             // accepted slots of the current window (listed in order)
   float sq[4];  // float-filter constants of props (filter_state)
   long long next_new;  // first proposal not yet in a window
   long long nn_next;   // next_new after the current window (committed by k_metro)
@@ -705,11 +706,13 @@ __device__ __forceinline__ int2 block_scan2(int a, int b, int* ea, int* eb, int2
   return wsum[31];
 }
 
+constexpr int PREF = 256;  // walked slots whose data is prefetched into shared memory
 __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsigned char* winner, const double* dpn,
                                              const float* dpf, FlipE fe, FlipEF fg, FlipState* st, const int* limit,
-                                             unsigned char* accepted, long long* pend) {
+                                             int* accl, long long* pend) {
   constexpr unsigned char SKIP = 0, REJECT = 1, ACCEPT = 2, OPEN = 3;
   __shared__ int lst[MAXB];
+  __shared__ double sdp[PREF][7];  // dp of the walked slots, and -log(u) of the open ones
   __shared__ int2 wsum[32];
   __shared__ float sb[3][32];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -723,7 +726,6 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
   for (int k = 0; k < MS; ++k) {
     const int s = tid * MS + k;
     if (s >= W) break;
-    accepted[s] = 0;
     const float* f8 = dpf + 8 * (size_t)s;
     if (f8[7] == 0.0f) continue;
     ba += fabsf(f8[0] * fg.irA);
@@ -792,27 +794,42 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
     if (s >= lim || !winner[s]) pend[ed++] = win[s];
   }
   __syncthreads();
+  // the walk's data (dp, and -log(u) of the open slots) fetched in parallel
+  if (tid < PREF && tid < tot.x) {
+    const int c = lst[tid];
+    const int s = c >= 0 ? c : -1 - c;
+    for (int k = 0; k < 6; ++k) sdp[tid][k] = dpn[8 * (size_t)s + k];
+    sdp[tid][6] = c >= 0 ? 0.0 : -log(flip_u_of(seed, win[s]));
+  }
+  __syncthreads();
   // phase 2: one thread walks the listed slots in order on the FP64 state
   if (tid == 0) {
     double sP[6];
     for (int k = 0; k < 6; ++k) sP[k] = st->props[k];
     double se0 = st->e0;
-    int sacc = st->acc;
+    int sacc = st->acc, nacc = 0;
     for (int i = 0; i < tot.x; ++i) {
       const int c = lst[i];
       const bool robust = c >= 0;
       const int s = robust ? c : -1 - c;
-      const double* o8 = dpn + 8 * (size_t)s;
+      double o8[7];
+      if (i < PREF) {
+        for (int k = 0; k < 7; ++k) o8[k] = sdp[i][k];
+      } else {
+        for (int k = 0; k < 6; ++k) o8[k] = dpn[8 * (size_t)s + k];
+        o8[6] = robust ? 0.0 : -log(flip_u_of(seed, win[s]));
+      }
       double trial[6];
       for (int k = 0; k < 6; ++k) trial[k] = sP[k] - o8[k];
       const double en = flip_energy(fe, trial);
-      if (robust || en - se0 <= -log(flip_u_of(seed, win[s]))) {
+      if (robust || en - se0 <= o8[6]) {
         for (int k = 0; k < 6; ++k) sP[k] = trial[k];
         se0 = en;
         sacc += 1;
-        accepted[s] = 1;
+        accl[nacc++] = s;
       }
     }
+    st->nacc_win = nacc;
     for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
     filter_state(fe, sP, st->sq);
     st->e0 = se0;
@@ -825,17 +842,17 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
 // one block of 32 threads per slot (accepted slots only do work): the
 // half-edge rewiring, then the two face rows and five edge rows, then the
 // four ring rows, each stage in parallel
-__global__ void __launch_bounds__(32) k_commit(TopoW t, const long long* win, const unsigned char* accepted,
-                                               FlipState* st) {
-  const int s = blockIdx.x;
-  if (s >= st->W || !accepted[s]) return;
+// the flip of proposal p's edge: one warp rewires six half-edges, two face
+// rows, five edge rows and four ring rows (patches of a window's accepted
+// flips are disjoint, so commits never touch the same entries)
+__device__ void commit_one(const TopoW& t, long long p, FlipState* st) {
   const int tid = threadIdx.x;
-  const int e = flip_edge_of(st->seed, win[s], t.ne);
+  const int e = flip_edge_of(st->seed, p, t.ne);
   const int a0 = 2 * e, b0 = 2 * e + 1;
   const int a1 = t.next[a0], a2 = t.next[a1], b1 = t.next[b0], b2 = t.next[b1];
   const int va0 = t.to[a0], va1 = t.to[a1], vb0 = t.to[b0], vb1 = t.to[b1];
   const int fa = t.face[a0], fb = t.face[b0];
-  __syncthreads();  // every thread has read the old wiring
+  __syncwarp();  // every lane has read the old wiring
   if (tid == 0) {
     t.to[a0] = va1;
     t.to[b0] = vb1;
@@ -852,7 +869,7 @@ __global__ void __launch_bounds__(32) k_commit(TopoW t, const long long* win, co
     if (t.vout[va0] == b0) t.vout[va0] = a1;
     if (t.vout[vb0] == a0) t.vout[vb0] = b1;
   }
-  __syncthreads();
+  __syncwarp();
   if (tid == 0) face_row(t, fa);
   if (tid == 1) face_row(t, fb);
   if (tid == 2) edge_row(t, e);
@@ -860,11 +877,19 @@ __global__ void __launch_bounds__(32) k_commit(TopoW t, const long long* win, co
   if (tid == 4) edge_row(t, a2 >> 1);
   if (tid == 5) edge_row(t, b1 >> 1);
   if (tid == 6) edge_row(t, b2 >> 1);
-  __syncthreads();
+  __syncwarp();
   if (tid < 4) {
     const int v = tid == 0 ? va0 : (tid == 1 ? va1 : (tid == 2 ? vb0 : vb1));
     if (!ring_row(t, v)) atomicExch(&st->status, TM_ERR_TOPOLOGY);
   }
+  __syncwarp();
+}
+
+// the window's accepted flips (listed by k_metro), every CB-th per block
+constexpr int CB = 152;
+__global__ void __launch_bounds__(32) k_commit(TopoW t, const long long* win, const int* accl, FlipState* st) {
+  const int nacc = st->nacc_win;
+  for (int i = blockIdx.x; i < nacc; i += gridDim.x) commit_one(t, win[accl[i]], st);
 }
 
 __global__ void k_set_int(int* p, int v) {
@@ -901,7 +926,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   DevBuf<long long>& pend = e->fw_pend;
   DevBuf<unsigned char>& winner = e->fw_winner;
   DevBuf<unsigned char>& okf = e->fw_okf;
-  DevBuf<unsigned char>& acc = e->fw_acc;
+  DevBuf<int>& accl = e->fw_accl;
   DevBuf<double>& part = e->fw_part;
   DevBuf<double>& dpn = e->fw_dpn;
   DevBuf<float>& dpf = e->fw_dpf;
@@ -910,7 +935,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   pend.ensure(MAXB);
   winner.ensure(MAXB);
   okf.ensure(MAXB);
-  acc.ensure(MAXB);
+  accl.ensure(MAXB);
   part.ensure(64 * (size_t)MAXB);
   dpn.ensure(8 * (size_t)MAXB);
   dpf.ensure(8 * (size_t)MAXB);
@@ -942,10 +967,10 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       k_delta<<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get(),
                                dpn.get(), dpf.get(), e->sct.get());
       TM_LAUNCH();
-      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(), acc.get(),
+      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(), accl.get(),
                                pend.get());
       TM_LAUNCH();
-      k_commit<<<B, 32, 0, s>>>(t, win.get(), acc.get(), st);
+      k_commit<<<CB, 32, 0, s>>>(t, win.get(), accl.get(), st);
       TM_LAUNCH();
     }
   };
@@ -957,7 +982,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       key.insert(key.end(), b, b + n);
     };
     const void* ptrs[] = {s, P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(), part.get(),
-                          okf.get(), dpn.get(), dpf.get(), acc.get(), e->sct.get(), m->d_to.get(),
+                          okf.get(), dpn.get(), dpf.get(), accl.get(), e->sct.get(), m->d_to.get(),
                           m->d_next.get(), m->d_face.get(), m->d_vout.get(), m->d_fhe.get(), m->d_slot.get(),
                           m->d_nbr.get(), m->d_val.get(), m->d_fv.get(), m->d_edge.get()};
     add(ptrs, sizeof ptrs);

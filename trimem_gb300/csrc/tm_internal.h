@@ -213,9 +213,9 @@ struct tm_energy {
   tmg::DevBuf<tmg::Globals> glob;
   tmg::DevBuf<double2> sct;  // {sin, cos}(k / 128), k < TM_SCT_N
   // flip-sweep workspace, kept between sweeps (grown on demand)
-  tmg::DevBuf<int> fw_owner, fw_limit;
+  tmg::DevBuf<int> fw_owner, fw_limit, fw_accl;
   tmg::DevBuf<long long> fw_win, fw_pend;
-  tmg::DevBuf<unsigned char> fw_winner, fw_okf, fw_acc, fw_state;
+  tmg::DevBuf<unsigned char> fw_winner, fw_okf, fw_state;
   tmg::DevBuf<double> fw_part, fw_dpn;
   tmg::DevBuf<float> fw_dpf;
   cudaStream_t stream = nullptr;
