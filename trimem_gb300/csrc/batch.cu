@@ -108,13 +108,24 @@ __global__ void k_copy_b(int n, const double* a, double* b) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = a[i];
 }
-__global__ void k_drift_b(int n3, double dt, double m, const double* p, const double* g, double* x) {
+// im = 1/m (no FP64 division per element)
+__global__ void k_drift_b(int n3, double dt, double im, const double* p, const double* g, double* x) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n3) x[i] = x[i] + (p[i] * dt + 0.5 * (-g[i]) * (dt * dt)) / m;
+  if (i < n3) x[i] = x[i] + (p[i] * dt + 0.5 * (-g[i]) * (dt * dt)) * im;
 }
 __global__ void k_kick_b(int n3, double dt, const double* g0, const double* g1, double* p) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n3) p[i] = p[i] + 0.5 * ((-g0[i]) + (-g1[i])) * dt;
+}
+// a kick and the following drift in one pass (same arithmetic)
+__global__ void k_kick_drift_b(int n3, double dt, double im, const double* g0, const double* g1, double* p,
+                               double* x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n3) {
+    const double pn = p[i] + 0.5 * ((-g0[i]) + (-g1[i])) * dt;
+    p[i] = pn;
+    x[i] = x[i] + (pn * dt + 0.5 * (-g1[i]) * (dt * dt)) * im;
+  }
 }
 // p.p per 256-vertex block (blocks never straddle replicas)
 __global__ void k_kin_blocks(int nv, const double* p, double* part) {
@@ -184,10 +195,13 @@ static void batch_hmc_step(tm_batch* b, int L, double dt, double m, double T, un
   double* g1 = b->g1.get();
   batch_eval(b, b->x.get(), g0, s);
   k_collect<<<nblk(b->R, 64), 64, 0, s>>>(b->R, b->rblocks.get(), b->part.get(), b->gs.get(), b->sc.get(), 0);
+  if (L > 0) k_drift_b<<<nblk(n3, B), B, 0, s>>>(n3, dt, 1.0 / m, b->p.get(), g0, b->x.get());
   for (int i = 0; i < L; ++i) {
-    k_drift_b<<<nblk(n3, B), B, 0, s>>>(n3, dt, m, b->p.get(), g0, b->x.get());
     batch_eval(b, b->x.get(), g1, s);
-    k_kick_b<<<nblk(n3, B), B, 0, s>>>(n3, dt, g0, g1, b->p.get());
+    if (i + 1 < L)
+      k_kick_drift_b<<<nblk(n3, B), B, 0, s>>>(n3, dt, 1.0 / m, g0, g1, b->p.get(), b->x.get());
+    else
+      k_kick_b<<<nblk(n3, B), B, 0, s>>>(n3, dt, g0, g1, b->p.get());
     std::swap(g0, g1);
   }
   k_kin_blocks<<<nb, B, 0, s>>>(b->nv, b->p.get(), b->part.get());

@@ -57,17 +57,32 @@ __global__ void k_copy(int n, const double* a, double* b) {
 }
 
 // x += (p dt + 0.5 a dt^2) / m with a = -g
-__global__ void k_drift(int n3, double dt, double m, const double* p, const double* g, double* x) {
+// im = 1/m: an FP64 division per element would dominate the pass (FP64 is
+// GB300's scarce pipe); for the usual m = 1 both forms are exact
+__global__ void k_drift(int n3, double dt, double im, const double* p, const double* g, double* x) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n3) {
     double a = -g[i];
-    x[i] = x[i] + (p[i] * dt + 0.5 * a * (dt * dt)) / m;
+    x[i] = x[i] + (p[i] * dt + 0.5 * a * (dt * dt)) * im;
   }
 }
 // p += 0.5 (a + a') dt
 __global__ void k_kick(int n3, double dt, const double* g0, const double* g1, double* p) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n3) p[i] = p[i] + 0.5 * ((-g0[i]) + (-g1[i])) * dt;
+}
+
+// k_kick followed by the next step's k_drift (the kick's new momentum and
+// the same force), the same arithmetic per element in one pass
+__global__ void k_kick_drift(int n3, double dt, double im, const double* g0, const double* g1, double* p,
+                             double* x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n3) {
+    const double pn = p[i] + 0.5 * ((-g0[i]) + (-g1[i])) * dt;
+    p[i] = pn;
+    const double a = -g1[i];
+    x[i] = x[i] + (pn * dt + 0.5 * a * (dt * dt)) * im;
+  }
 }
 
 // fixed-order dot product p.p into out[slot]
@@ -169,11 +184,17 @@ static void hmc_step(tm_surrogate* sg, tm_energy* e, tm_mesh* m, double* d_x, do
     force(g0);
     record(sc + 0, props);
   }
-  for (int i = 0; i < n_steps; ++i) {
-    k_drift<<<nblk(n3, b), b, 0, s>>>(n3, dt, mass, p, g0, x);
+  // velocity Verlet; each kick is fused with the following drift
+  if (n_steps > 0) {
+    k_drift<<<nblk(n3, b), b, 0, s>>>(n3, dt, 1.0 / mass, p, g0, x);
     TM_LAUNCH();
+  }
+  for (int i = 0; i < n_steps; ++i) {
     force(g1);
-    k_kick<<<nblk(n3, b), b, 0, s>>>(n3, dt, g0, g1, p);
+    if (i + 1 < n_steps)
+      k_kick_drift<<<nblk(n3, b), b, 0, s>>>(n3, dt, 1.0 / mass, g0, g1, p, x);
+    else
+      k_kick<<<nblk(n3, b), b, 0, s>>>(n3, dt, g0, g1, p);
     TM_LAUNCH();
     std::swap(g0, g1);
   }
