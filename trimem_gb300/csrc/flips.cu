@@ -32,6 +32,8 @@
 // seed lives in the sweep state in device memory, so the 48 launches of a
 // group of eight windows are captured once as a CUDA graph and replayed.
 // A flip is also refused when it would raise a valence above TM_MAXVAL.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -325,6 +327,35 @@ __global__ void k_winner(TopoW t, const FlipState* st, int mode, const long long
   if (k == 0) {
     winner[s] = ok ? 1 : 0;
     if (!ok && mode == 0) atomicMin(limit, s);
+  }
+}
+
+// k_claim and k_winner in one cooperative launch: the claims, a grid-wide
+// barrier, then the ownership test on the same edges (read past L1)
+__global__ void __launch_bounds__(64) k_claim_win(TopoW t, const FlipState* st, int mode, const long long* win,
+                                                 int* owner, unsigned char* winner, int* limit) {
+  const unsigned long long seed = st->seed;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = g >> 2, k = g & 3;
+  const int W = st->W, wid = st->wid;
+  const bool act = s < W;  // the four threads of a slot agree
+  int v = 0, tag = 0;
+  if (act) {
+    const Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
+    tag = owner_tag(wid, s);
+    v = quad_vertex(q, k);
+    for_ring_edges(t, v, [&](int x) { atomicMax(&owner[x], tag); });
+  }
+  cooperative_groups::this_grid().sync();
+  if (act) {
+    bool ok = true;
+    for_ring_edges(t, v, [&](int x) { ok = ok && (__ldcg(&owner[x]) == tag); });
+    const unsigned gmask = 0xfu << (threadIdx.x & 28);
+    ok = __all_sync(gmask, ok);
+    if (k == 0) {
+      winner[s] = ok ? 1 : 0;
+      if (!ok && mode == 0) atomicMin(limit, s);
+    }
   }
 }
 
@@ -956,14 +987,42 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   // captured once as a CUDA graph per launch key and replayed.
   const int B = batch;
   constexpr int GROUP = 8;
-  auto launch_group = [&]() {
+  // claim + winner as one cooperative launch when all its blocks fit on the
+  // GPU at once (else, or when the launch is refused, two kernels)
+  const int ncw = nblk(4L * B, 64);
+  if (e->flip_coop == 0) {
+    int per_sm = 0, nsm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_claim_win, 64, 0);
+    e->flip_coop = per_sm * nsm >= (MAXB * 4 + 63) / 64 ? 1 : -1;
+    cudaGetLastError();
+  }
+  auto claim_win = [&](bool coop) {
+    if (coop) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(ncw);
+      cfg.blockDim = dim3(64);
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      TM_CUDA(cudaLaunchKernelEx(&cfg, k_claim_win, t, (const FlipState*)st, mode, (const long long*)win.get(),
+                                 owner.get(), winner.get(), limit.get()));
+    } else {
+      k_claim<<<ncw, 64, 0, s>>>(t, st, win.get(), owner.get());
+      TM_LAUNCH();
+      k_winner<<<ncw, 64, 0, s>>>(t, st, mode, win.get(), owner.get(), winner.get(), limit.get());
+      TM_LAUNCH();
+    }
+  };
+  auto launch_group = [&](bool coop) {
     for (int k = 0; k < GROUP; ++k) {
       k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st, win.get(), limit.get());
       TM_LAUNCH();
-      k_claim<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, win.get(), owner.get());
-      TM_LAUNCH();
-      k_winner<<<nblk(4L * B, 64), 64, 0, s>>>(t, st, mode, win.get(), owner.get(), winner.get(), limit.get());
-      TM_LAUNCH();
+      claim_win(coop);
       k_delta<<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get(),
                                dpn.get(), dpf.get(), e->sct.get());
       TM_LAUNCH();
@@ -997,16 +1056,30 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       e->flip_graph.exec = nullptr;
       e->flip_graph.key.clear();
       cudaGraph_t g = nullptr;
-      TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      try {
-        launch_group();
-      } catch (...) {
-        cudaStreamEndCapture(s, &g);  // leave capture mode before reporting
+      for (int attempt = 0;; ++attempt) {
+        const bool coop = e->flip_coop > 0;
+        TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        bool failed = false;
+        try {
+          launch_group(coop);
+        } catch (...) {
+          if (!coop || attempt > 0) {
+            cudaStreamEndCapture(s, &g);  // leave capture mode before reporting
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            throw;
+          }
+          failed = true;
+        }
+        cudaError_t ec = cudaStreamEndCapture(s, &g);
+        if (!failed && ec == cudaSuccess) break;
+        // a cooperative launch that cannot be captured: two kernels instead
         if (g) cudaGraphDestroy(g);
+        g = nullptr;
         cudaGetLastError();
-        throw;
+        if (!coop || attempt > 0) TM_CUDA(ec);
+        e->flip_coop = -1;
       }
-      TM_CUDA(cudaStreamEndCapture(s, &g));
       cudaError_t rc = cudaGraphInstantiate(&e->flip_graph.exec, g, 0);
       cudaGraphDestroy(g);
       if (rc != cudaSuccess) e->flip_graph.exec = nullptr;
@@ -1020,7 +1093,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     if (group)
       TM_CUDA(cudaGraphLaunch(group, s));
     else
-      launch_group();
+      launch_group(e->flip_coop > 0);
     TM_CUDA(cudaMemcpyAsync(&hs, st, sizeof(FlipState), cudaMemcpyDeviceToHost, s));
     TM_CUDA(cudaStreamSynchronize(s));
     if (hs.status) fail(TM_ERR_TOPOLOGY, "flip produced a valence above TM_MAXVAL");

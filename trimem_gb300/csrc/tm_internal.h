@@ -235,6 +235,7 @@ struct tm_energy {
   std::vector<EvalGraph> eval_graphs;
   unsigned long long eval_tick = 0;
   EvalGraph flip_graph;  // one group of flip-sweep windows
+  int flip_coop = 0;     // claim + winner as one cooperative launch: 0 unknown, 1 yes, -1 no
   void ensure(int nv_, int ne_, int nf_);
   // copies n doubles from device memory to host memory dst and synchronises
   void to_host(double* dst, const double* src, size_t n);
