@@ -13,7 +13,8 @@
 //             that the lowest slot of the current window wins
 //   k_winner  a proposal whose patch it owns entirely is a winner; in
 //             serial mode the window is cut at the first loser, so proposals
-//             are decided in proposal order
+//             are decided in proposal order (k_claim_win does both in one
+//             cooperative launch with a grid barrier when it fits)
 //   k_delta   one block per winner evaluates the vertex properties of the
 //             four quad vertices before and after a virtual flip (the mesh is
 //             not touched), including the repulsion with the post-flip
@@ -29,7 +30,7 @@
 //             disjoint, so commits never touch the same entries
 // Proposals come from a counter-based SplitMix64 stream of (seed, index), so
 // a sweep is reproducible and matches the CPU port of this algorithm.  The
-// seed lives in the sweep state in device memory, so the 48 launches of a
+// seed lives in the sweep state in device memory, so the 40 launches of a
 // group of eight windows are captured once as a CUDA graph and replayed.
 // A flip is also refused when it would raise a valence above TM_MAXVAL.
 #include <cooperative_groups.h>
@@ -982,7 +983,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   TM_LAUNCH();
   // windows are queued in groups without host round trips; W and the window
   // number live on the device, and a window after the last one is empty
-  // (W = 0: every kernel returns at once).  A group's 48 launches do not
+  // (W = 0: every kernel returns at once).  A group's 40 launches do not
   // depend on the sweep (the seed is in the device state), so they are
   // captured once as a CUDA graph per launch key and replayed.
   const int B = batch;
