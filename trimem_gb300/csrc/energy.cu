@@ -53,6 +53,21 @@ using namespace tmg;
 namespace tmg {
 
 // ---- per-face and per-edge quantities ------------------------------------
+// Sign tests and absolute values as integer operations on the bits (no
+// FP64 compare or absolute value: FP64 is GB300's scarce pipe).  The sign
+// bit of an edge's il is its boundary flag; for non-negative doubles the
+// bit patterns order like the values, so a length l >= 0 is compared with
+// a threshold by its bits (NaN lengths compare as above every threshold).
+__device__ __forceinline__ bool interior_edge(double il) { return __double_as_longlong(il) >= 0; }
+__device__ __forceinline__ double abs_bits(double x) {
+  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool len_below(double l, double c) {
+  return __double_as_longlong(l) < __double_as_longlong(c);
+}
+__device__ __forceinline__ bool len_above(double l, double c) {
+  return __double_as_longlong(l) > __double_as_longlong(c);
+}
 // fav: (area, volume) of each face again, compact, for k_vertex's gathers
 __global__ void k_face(Topo t, const double* __restrict__ P, FaceD* __restrict__ fd, float* __restrict__ P32,
                        double2* __restrict__ fav) {
@@ -109,17 +124,23 @@ __global__ void k_edge(Topo t, const double* __restrict__ P, const FaceD* __rest
     // along it: its projection on the unit edge is the signed sine, whose
     // sign is the reference's sign test (n0 x n1) . e >= 0
     double sd = dot(cross(n0, n1), ev) * il;
-    double a = angle_sc(fabs(sd), dot(n0, n1), sct);
+    double a = angle_sc(abs_bits(sd), dot(n0, n1), sct);
     o.th = sd >= 0.0 ? a : -a;
     o.il = il;
   }
-  // flat-bottom edge penalty: above the flat bottom inline (products only);
-  // edges below it (exp and divisions in FP64) go to a list handled by
-  // k_bond_short so that whole warps do not wait on a few lanes
+  // flat-bottom edge penalty: above the flat bottom inline (products only,
+  // edge_bond's l > lc0 branch); edges below it (exp and a division in
+  // FP64) go to a list handled by k_bond_short so that whole warps do not
+  // wait on a few lanes
   double val = 0.0, fac = 0.0;
-  bool shortb = ep.btype == 0 && l < ep.lc1;
-  if (ep.btype == 0 && !shortb && l > ep.lc0) edge_bond(ep, l, il, &val, &fac);
-  warp_append(shortb, e, blist, bcnt);  o.db = fac;
+  const bool shortb = ep.btype == 0 && len_below(l, ep.lc1);
+  if (ep.btype == 0 && !shortb && len_above(l, ep.lc0)) {
+    const double d = l - ep.lc0;
+    val = ep.br1 * ipow(d, ep.r);
+    fac = ep.br2 * ipow(d, ep.r - 1);
+  }
+  warp_append(shortb, e, blist, bcnt);
+  o.db = fac;
   ed[e] = o;
   elt[e] = make_double2(o.l * o.th, val);
 }
@@ -238,12 +259,6 @@ __global__ void k_assemble_props(EP ep, const double* props6, Globals* g) {
 }
 
 // ---- gradient gather ------------------------------------------------------
-// the sign bit of an edge's il is its boundary flag; tested and cleared as
-// integers (no FP64 compare or absolute value)
-__device__ __forceinline__ bool interior_edge(double il) { return __double_as_longlong(il) >= 0; }
-__device__ __forceinline__ double abs_bits(double x) {
-  return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
-}
 // rk[v] = (kb rho_v, 2/3 kb rho_v^2), written by k_vertex
 __global__ void __launch_bounds__(256) k_grad(Topo t, const double* __restrict__ P, const FaceD* __restrict__ fd,
                                              const EdgeD* __restrict__ ed, const double2* __restrict__ rk,
