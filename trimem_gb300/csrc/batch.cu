@@ -225,9 +225,14 @@ static void upload_eps(tm_batch* b) {
   TM_CUDA(cudaStreamSynchronize(b->stream));
 }
 
-static void rebuild_nlist(tm_batch* b) {
+// near_rows: also (re)build the near rows (their build only runs when some
+// vertex has moved half a cut-off).  The rebuilds between HMC steps skip
+// them: members that move that far within a step leave the rows stale at
+// once, and the cells' candidate rows, rebuilt every time, serve instead
+// (the rows never depend on the cells, and stale rows are never used).
+static void rebuild_nlist(tm_batch* b, bool near_rows = true) {
   // near rows when every replica's cells are at least its repulsion cut-off
-  bool near = true;
+  bool near = near_rows;
   for (const tm_params& p : b->prm) near = near && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1;
   nlist_make_batch(&b->en->nl, b->mesh.get(), b->R, b->vrep.get(), b->rblocks.get(), b->rlist.get(),
                    b->prm[0].exclusion_level, b->x.get(), b->stream, b->eps.get(), near);
@@ -445,7 +450,7 @@ int tm_batch_hmc(tm_batch* b, int n_steps, int n_leapfrog, double dt, double mas
       batch_hmc_step(b, n_leapfrog, dt, mass, temperature, seed, s);
     }
     ++b->steps_done;
-    if (b->refresh > 0 && b->steps_done % b->refresh == 0) rebuild_nlist(b);
+    if (b->refresh > 0 && b->steps_done % b->refresh == 0) rebuild_nlist(b, false);
   }
   if (accepted)
     TM_CUDA(cudaMemcpyAsync(accepted, b->acc.get(), sizeof(int) * b->R, cudaMemcpyDeviceToHost, s));

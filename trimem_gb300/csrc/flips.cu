@@ -561,9 +561,10 @@ __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, 
     double tt = 0.0;
     if (ep.btype == 0) {
       int r = ep.r;
-      if (el > ep.lc0)
+      // threshold tests on the length's bits (l >= 0 orders like its bits)
+      if (__double_as_longlong(el) > __double_as_longlong(ep.lc0))
         tt = ep.br1 * ipow(el - ep.lc0, r);
-      else if (el < ep.lc1)
+      else if (__double_as_longlong(el) < __double_as_longlong(ep.lc1))
         tt = exp(el * (1.0 / (el - ep.lc1))) * ipow(il, r);
     } else {
       double qa = fa / ep.a0 - 1.0;
