@@ -499,12 +499,9 @@ def main():
     dev_ms = sum(a.elapsed_time(b) for evs in all_evs for a, b in evs)
     rebuild_ms = sum(evs[0][0].elapsed_time(evs[0][1]) for evs in all_evs) / args.steps
     eval_ms = (dev_ms / args.steps - rebuild_ms) / EVALS_PER_STEP
-    if world > 1:
-        t = torch.tensor([dev_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    dev_ms = max_over_ranks(dev_ms, world, "cuda")
     ms_per_step = dev_ms / args.steps
-    value = world * EVALS_PER_STEP * args.steps / (dev_ms / 1e3)
+    value = job_rate(world, EVALS_PER_STEP * args.steps, dev_ms)
 
     # ---- per-kernel times of one evaluation (cold L2) for the roofline -----
     import ctypes
@@ -666,6 +663,23 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def max_over_ranks(x, world, device):
+    """The largest x over the ranks of the process group (x itself alone)."""
+    if world <= 1:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_rank, ms):
+    """Whole-job throughput: every rank processes units_per_rank (replicas,
+    weak scaling) within the slowest rank's ms."""
+    return world * units_per_rank / (ms / 1e3)
 
 
 def ctypes_ptr(t):

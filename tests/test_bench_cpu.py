@@ -23,3 +23,40 @@ def test_reference_arm_prints_one_json_line(built):
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert "workload" in d["config"]
+
+
+def _rank_main(rank, world, port, q):
+    import torch.distributed as dist
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms = bench.max_over_ranks(10.0 + rank, world, "cpu")  # rank 1 is the slower one
+    q.put((rank, ms, bench.job_rate(world, 100, ms)))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_multi_rank_timing_takes_the_slowest_rank():
+    """world_size 2 over gloo: both ranks see the slower rank's time, and the
+    job rate counts both ranks' work (replicas, weak scaling)."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert [o[1] for o in out] == [11.0, 11.0]
+    assert all(abs(o[2] - 2 * 100 / 0.011) < 1e-6 for o in out)
