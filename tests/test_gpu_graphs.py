@@ -63,3 +63,29 @@ def test_graph_replays_match_direct_launches(built, stencil):
         assert e_only == e_graph, it
         seen.append(e_graph)
     assert np.all(np.isfinite(seen)) and len(set(seen)) == len(seen)
+
+
+def test_graph_replays_on_other_streams(built):
+    """A graph captured on one stream replays on another: alternating
+    streams give the results of the direct launches."""
+    import torch
+
+    from trimem_gb300 import capi
+
+    L = capi.lib()
+    p, f = meshgen.jittered_icosphere(4, seed=5)
+    mesh = capi.Mesh(p, f)
+    en = capi.Energy(mesh, capi.params(**workload_params(p, f)))
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    g, g_direct = torch.empty_like(x), torch.empty_like(x)
+    ms5 = (ctypes.c_float * 5)()
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    for it in range(4):
+        x += 1e-4 * (it + 1) * torch.ones_like(x)
+        st = streams[it % 2]
+        st.wait_stream(torch.cuda.current_stream())
+        capi.check(L.tm_energy_eval_device(en.h, mesh.h, _ptr(x), _ptr(g), None, ctypes.c_void_p(st.cuda_stream)))
+        torch.cuda.synchronize()
+        capi.check(L.tm_energy_eval_timed(en.h, mesh.h, _ptr(x), _ptr(g_direct), ms5, None))
+        torch.cuda.synchronize()
+        assert torch.equal(g, g_direct), it

@@ -413,13 +413,14 @@ static void eval_launches(tm_energy* e, tm_mesh* m, const double* P, bool want_g
 // arguments, stencil precision, buffers, parameters and the neighbour-list
 // view.  Equal keys mean a captured graph replays the same launches.
 static std::vector<unsigned char> eval_key(tm_energy* e, tm_mesh* m, const double* P, bool want_grad,
-                                           double* d_grad, cudaStream_t s) {
+                                           double* d_grad) {
   std::vector<unsigned char> k;
   auto add = [&k](const void* p, size_t n) {
     const unsigned char* b = static_cast<const unsigned char*>(p);
     k.insert(k.end(), b, b + n);
   };
-  const void* ptrs[] = {P, d_grad, s, e->face.get(), e->edge.get(), e->ebond.get(), e->fav.get(), e->rho.get(),
+  // (the launch stream is not part of the key: a graph replays on any stream)
+  const void* ptrs[] = {P, d_grad, e->face.get(), e->edge.get(), e->ebond.get(), e->fav.get(), e->rho.get(),
                         e->repg.get(), e->reppot.get(), e->slow.get(), e->pos32.get(), e->poslo.get(), e->partials.get(),
                         e->glob.get(), e->sct.get(), e->aux, e->ev_fork, e->ev_join, e->nl.xb.get()};
   add(ptrs, sizeof ptrs);
@@ -445,7 +446,7 @@ static std::vector<unsigned char> eval_key(tm_energy* e, tm_mesh* m, const doubl
 // gradient, several buffers), the least recently used is replaced.
 static void eval_graph(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, double* d_grad, cudaStream_t s) {
   constexpr size_t MAX_GRAPHS = 4;
-  std::vector<unsigned char> key = eval_key(e, m, P, want_grad, d_grad, s);
+  std::vector<unsigned char> key = eval_key(e, m, P, want_grad, d_grad);
   for (auto& g : e->eval_graphs)
     if (g.exec && g.key == key) {
       g.used = ++e->eval_tick;
@@ -453,7 +454,7 @@ static void eval_graph(tm_energy* e, tm_mesh* m, const double* P, bool want_grad
       return;
     }
   eval_launches(e, m, P, want_grad, d_grad, s);
-  key = eval_key(e, m, P, want_grad, d_grad, s);
+  key = eval_key(e, m, P, want_grad, d_grad);
   cudaGraph_t g = nullptr;
   TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   try {

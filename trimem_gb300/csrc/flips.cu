@@ -1042,7 +1042,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       const unsigned char* b = static_cast<const unsigned char*>(p);
       key.insert(key.end(), b, b + n);
     };
-    const void* ptrs[] = {s, P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(), part.get(),
+    const void* ptrs[] = {P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(), part.get(),
                           okf.get(), dpn.get(), dpf.get(), accl.get(), e->sct.get(), m->d_to.get(),
                           m->d_next.get(), m->d_face.get(), m->d_vout.get(), m->d_fhe.get(), m->d_slot.get(),
                           m->d_nbr.get(), m->d_val.get(), m->d_fv.get(), m->d_edge.get()};
