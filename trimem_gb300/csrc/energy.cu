@@ -159,29 +159,6 @@ __global__ void k_bond_short(const double* __restrict__ P, Topo t, EdgeD* __rest
   }
 }
 
-// Sums v[0..5] over the VB threads of the block into thread 0's v, in a
-// fixed order (shuffles within each warp, then the warp sums by warp 0):
-// two barriers instead of a shared-memory tree's eight
-__device__ __forceinline__ void block_sum6(double* v, double (*red)[VB]) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < 6; ++k)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-  if (lane == 0)
-    for (int k = 0; k < 6; ++k) red[k][w] = v[k];
-  __syncthreads();
-  if (w == 0) {
-    for (int k = 0; k < 6; ++k) {
-      double x = lane < VB / 32 ? red[k][lane] : 0.0;
-#pragma unroll
-      for (int o = 4; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      v[k] = x;
-    }
-  }
-  __syncthreads();  // red may be reused after the call
-}
-
 constexpr int VG = 6;  // ring slots loaded together by k_vertex
 template <bool VPROPS>
 __global__ void __launch_bounds__(VB) k_vertex(Topo t, const double2* __restrict__ fav,
@@ -241,9 +218,15 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const double2* __restrict
     if (VPROPS)
       for (int k = 0; k < 6; ++k) vprops[6 * (size_t)v + k] = pr[k];
   }
-  block_sum6(pr, red);  // thread 0 holds the block's sums, in a fixed order
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = pr[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 6; ++k) partial[8 * (size_t)blockIdx.x + k] = pr[k];
+    for (int k = 0; k < 6; ++k) partial[8 * (size_t)blockIdx.x + k] = red[k][0];
     __threadfence();
     unsigned int tk = atomicAdd(&g->ticket, 1u);
     last = (tk == gridDim.x - 1);
@@ -255,9 +238,15 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const double2* __restrict
   double acc[6] = {0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < (int)gridDim.x; b += VB)
     for (int k = 0; k < 6; ++k) acc[k] += ((volatile double*)partial)[8 * (size_t)b + k];
-  block_sum6(acc, red);
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int o = VB / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 6; ++k) g->props[k] = acc[k];
+    for (int k = 0; k < 6; ++k) g->props[k] = red[k][0];
     assemble(ep, g);
     g->ticket = 0;
   }
