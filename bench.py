@@ -649,7 +649,6 @@ def main():
     # starts 1, scatter 1, sort 1, near-row check / build / done 3); the
     # displacement and L2-flush kernels are torch's
     launches_per_step = 8 * EVALS_PER_STEP + 14
-    peaks_fp64 = {"fp64_gflops_measured_probe": 1196.0}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -658,7 +657,7 @@ def main():
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(), "fp32_stencil": fp32, "df64_stencil": df64,
             "batch_replicas": batch,
             "hmc_chain": chain,
-            "gpu_launches": launches_per_step * args.steps, "notes": peaks_fp64}
+            "gpu_launches": launches_per_step * args.steps}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
