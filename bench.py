@@ -274,23 +274,66 @@ def chain_start():
 DT_CANDIDATES = (5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6, 5e-7, 2e-7)
 
 
-def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=200, weights=None):
+def _chain_handles(state, stencil):
+    """Mesh (the state's flipped topology with its edge numbering), energy
+    (the relaxed state's area / volume targets) and positions of a chain
+    state."""
+    import torch
+
+    from trimem_gb300 import capi
+
+    mesh = capi.Mesh(state["x"], state["faces"])
+    if state.get("topo") is not None:
+        mesh.set_topology(state["topo"])
+    en = capi.Energy(mesh, capi.params(**state["prm"]))
+    if state.get("initial") is not None:
+        en.set_initial_props(state["initial"])
+    en.set_stencil_precision(stencil)
+    x = torch.tensor(state["x"], dtype=torch.float64, device="cuda").contiguous()
+    return mesh, en, x
+
+
+def chain_warm(stream, start, n_warm=300):
+    """The chains' common start: the relaxed membrane heated to T 1 by an
+    FP64 chain of n_warm steps (the same moves as the measured chains, time
+    step tuned at the relaxed state), so that the measured traces start
+    close to equilibrium instead of climbing from the energy minimum."""
+    import torch
+
+    from trimem_gb300.mc.device import DeviceChain, tune_dt
+
+    x0, f, prm, info = start
+    state = {"x": x0, "faces": f, "prm": prm}
+    mesh, en, x = _chain_handles(state, 0)
+    initial = en.initial_props()
+    dt, _ = tune_dt(mesh, en, x, candidates=DT_CANDIDATES, stream=stream)
+    ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=5, stream=stream)
+    t0 = time.perf_counter()
+    trace = ch.run(n_warm)
+    torch.cuda.synchronize()
+    bend = prm["kappa_b"] * trace[:, 3]
+    q = np.array_split(bend, 4)
+    info = dict(info, warm_steps=n_warm, warm_dt=dt, warm_seconds=round(time.perf_counter() - t0, 3),
+                warm_bending_quarter_means=[round(float(b.mean()), 1) for b in q])
+    return {"x": ch.x.cpu().numpy(), "faces": mesh.fv_indices(), "topo": mesh.topology(), "initial": initial,
+            "prm": prm, "info": info}
+
+
+def chain_leg(stream, state, stencil, dt=None, n_burn=20, n_steps=500, weights=None):
     """ESS/s of the bending energy of a device chain: per step one HMC move
     (20 velocity-Verlet steps, m 1, T 1) and one flip sweep (ratio 0.2,
     98,304 attempts), neighbour list rebuilt every step.  dt: the largest of
     DT_CANDIDATES (from 5e-5, the large-mesh runs' step) with pilot
-    acceptance >= 0.5 unless given."""
+    acceptance >= 0.5 unless given.  The trace's quarter means show whether
+    it is still drifting (an ESS of a drifting trace is a lower bound)."""
     import torch
 
     from trimem_gb300 import capi
     from trimem_gb300.mc.device import DeviceChain, tune_dt
     from trimem_gb300.mc.ess import ess
 
-    x0, f, prm, _ = start
-    mesh = capi.Mesh(x0, f)
-    en = capi.Energy(mesh, capi.params(**prm))
-    en.set_stencil_precision(stencil)
-    x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
+    prm = state["prm"]
+    mesh, en, x = _chain_handles(state, stencil)
     sg = capi.Surrogate(mesh, weights) if weights is not None else None
     pilot = None
     if dt is None:
@@ -316,6 +359,7 @@ def chain_leg(stream, start, stencil, dt=None, n_burn=20, n_steps=200, weights=N
             "flip_attempts_per_s": round(int(0.2 * mesh.counts()[1]) * n_steps / max(ch.seconds["flip"] - sec0["flip"], 1e-9), 1),
             "ess_bending": round(e, 2), "ess_per_s": round(e / (t1 - t0), 3),
             "bending_mean": float(bend.mean()), "bending_sd": float(bend.std()),
+            "bending_quarter_means": [round(float(b.mean()), 1) for b in np.array_split(bend, 4)],
             "ess_reduced_volume": round(e_rv, 2), "ess_reduced_volume_per_s": round(e_rv / (t1 - t0), 3),
             "reduced_volume_mean": float(rv.mean())}
 
@@ -624,16 +668,16 @@ def main():
 
     chain = {}
     try:
-        start = chain_start()
-        chain["start"] = start[3]
-        plain = chain_leg(stream, start, 0)
+        warm = chain_warm(stream, chain_start())
+        chain["start"] = warm["info"]
+        plain = chain_leg(stream, warm, 0)
         chain["plain_fp64"] = plain
-        chain["plain_df64"] = chain_leg(stream, start, 2, dt=plain["dt"])
+        chain["plain_df64"] = chain_leg(stream, warm, 2, dt=plain["dt"])
         from trimem_gb300 import surrogate as S
 
         if os.path.exists(S.WEIGHTS_L7):
             # the surrogate chain tunes its own step on the same rule
-            chain["surrogate"] = chain_leg(stream, start, 0, weights=np.load(S.WEIGHTS_L7))
+            chain["surrogate"] = chain_leg(stream, warm, 0, weights=np.load(S.WEIGHTS_L7))
         else:
             chain["surrogate"] = {"error": "no trained weights"}
     except Exception as exc:
