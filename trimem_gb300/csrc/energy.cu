@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(VB) k_vertex(Topo t, const double2* __restrict
     pr[1] = V * (1.0 / 3.0);
     pr[2] = c;
     pr[3] = 2 * c * c * ia;
-    pr[4] = T * (1.0 / ep.tdiv);
+    pr[4] = T * ep.itdiv;
     pr[5] = reppot[v];
     const double rho = c * ia;
     rk[v] = make_double2(ep.kb * rho, (ep.kb * (2.0 / 3.0)) * (rho * rho));
@@ -380,6 +380,7 @@ EP make_ep(const tm_energy* e) {
   ep.rT = sq_threshold(p.rep_lc1);
   ep.rr = p.rep_r;
   ep.tdiv = p.bond_type == 0 ? 2.0 : 3.0;
+  ep.itdiv = 1.0 / ep.tdiv;
   auto ipow_h = [](double x, int n) {  // the device's ipow, on the host
     double r = 1.0;
     for (int k = 0; k < std::abs(n); ++k) r *= x;

@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, 
     o[1] = sv * (1.0 / 3.0);
     o[2] = C;
     o[3] = 2 * C * C / A;
-    o[4] = stt * (1.0 / ep.tdiv);
+    o[4] = stt * ep.itdiv;
   }
   // repulsion: the near row shared by the variant's 8 lanes, else one lane
   // walks the cell list

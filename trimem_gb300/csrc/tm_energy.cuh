@@ -15,6 +15,7 @@ struct EP {
   double rlc1, rT;  // repulsion cut-off and its exact squared threshold
   int rr;
   double tdiv;
+  double itdiv;  // 1 / tdiv, correctly rounded (what a device division gives)
   double br1, br2;  // r^(r+1) and r^(r+2) of the flat-bottom bond above lc0
 };
 
