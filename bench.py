@@ -357,6 +357,7 @@ def chain_leg(stream, state, stencil, dt=None, n_burn=20, n_steps=500, weights=N
             "flips_accepted_per_sweep": round((ch.flips - f0) / n_steps, 1),
             "ms_per_move": {k: round((ch.seconds[k] - sec0[k]) * 1e3 / n_steps, 3) for k in sec0},
             "flip_attempts_per_s": round(int(0.2 * mesh.counts()[1]) * n_steps / max(ch.seconds["flip"] - sec0["flip"], 1e-9), 1),
+            "flips_accepted_per_s": round((ch.flips - f0) / max(ch.seconds["flip"] - sec0["flip"], 1e-9), 1),
             "ess_bending": round(e, 2), "ess_per_s": round(e / (t1 - t0), 3),
             "bending_mean": float(bend.mean()), "bending_sd": float(bend.std()),
             "bending_quarter_means": [round(float(b.mean()), 1) for b in np.array_split(bend, 4)],
@@ -634,6 +635,43 @@ def main():
             "energy_rel_err": abs(e32 - e64) / abs(e64),
             "grad_rel_err": float(torch.linalg.norm(g - g64) / torch.linalg.norm(g64))}
 
+    # ---- surrogate force: speed against the exact one, tensor-core share ---
+    surrogate = None
+    try:
+        from trimem_gb300 import surrogate as S
+
+        if os.path.exists(S.WEIGHTS_L7):
+            sg = capi.Surrogate(mesh, np.load(S.WEIGHTS_L7))
+            gs = torch.empty_like(x)
+
+            def surrogate_force():
+                capi.check(L.tm_surrogate_gradient_device(sg.h, en.h, mesh.h, ctypes_ptr(x), ctypes_ptr(gs),
+                                                          ctypes_ptr_s(stream)))
+
+            for _ in range(3):
+                surrogate_force()
+            sms = []
+            for _ in range(10):
+                a, b = timed(surrogate_force)
+                torch.cuda.synchronize()
+                sms.append(a.elapsed_time(b))
+            s_ms = float(np.median(sms))
+            # three message-passing rounds, each a (V x 128) @ (128 x 64) bf16
+            # product on the tensor cores (k_dense); the rest is gathers
+            dense_flop = 3 * 2 * V * 128 * 64
+            bf16 = peaks.get("bf16_tflops")
+            surrogate = {"force_ms_cold": round(s_ms, 5), "forces_per_s_cold": round(1e3 / s_ms, 1),
+                         "vs_exact_fp64": round(float(kms[4]) / s_ms, 3),
+                         "vs_exact_df64": round(df64["eval_ms_cold"] / s_ms, 3),
+                         "dense_gflop": round(dense_flop / 1e9, 3),
+                         "dense_tflops_over_whole_force": round(dense_flop / (s_ms * 1e-3) / 1e12, 2),
+                         "bf16_peak_tflops": bf16, "peak_source": "of measured" if bf16 else None,
+                         "frac": round(dense_flop / (s_ms * 1e-3) / 1e12 / bf16, 5) if bf16 else None,
+                         "note": "tensor FLOP over the whole force time (a lower bound on k_dense's own rate); "
+                                 "the force is bound by the gathers around the dense layers"}
+    except Exception as exc:  # the headline line is printed either way
+        surrogate = {"error": f"{type(exc).__name__}: {exc}"}
+
     # ---- end to end through the public API ---------------------------------
     cm = core.TriMesh(p, f)
     ep = core.EnergyParams()
@@ -699,6 +737,7 @@ def main():
             "config": config({"eval_ms": round(eval_ms, 5), "rebuild_ms": round(rebuild_ms, 5),
                               "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4)}),
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(), "fp32_stencil": fp32, "df64_stencil": df64,
+            "surrogate_force": surrogate,
             "batch_replicas": batch,
             "hmc_chain": chain,
             "gpu_launches": launches_per_step * args.steps}
