@@ -167,6 +167,51 @@ def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400):
                       f"N(0,1e-4)) of the 163,842-vertex workload, {t:.1f} s, OpenMP {O.get_threads()} threads"}
 
 
+def cpu_chain_step(state, n_steps=2, n_leapfrog=20, dt=5e-6, ratio=0.2):
+    """Chain steps of the chains' workload on the host cores with the oracle
+    (the reference algorithm restated, all threads): per step a neighbour-list
+    rebuild, an HMC move of n_leapfrog velocity-Verlet steps (m 1, T 1: 21
+    gradients and 2 energies, the reference's integrator) and a parallel flip
+    sweep (the reference's pflip restated, OpenMP with try-locks)."""
+    from oracle import oracle as O
+
+    O.set_threads(os.cpu_count() or 1)
+    mo = O.Mesh(state["x"], state["faces"])
+    eo = O.Energy(mo, O.default_params(**state["prm"]))
+    x = mo.points()  # a view of the oracle mesh's positions
+    rng = np.random.default_rng(3)
+    t_hmc = t_flip = 0.0
+    acc = flips = 0
+    for _ in range(n_steps):
+        t0 = time.perf_counter()
+        eo.update_repulsion(mo)
+        x0 = x.copy()
+        pm = rng.standard_normal(x.shape)
+        h0 = eo.energy(mo) + 0.5 * float((pm * pm).sum())
+        a = -eo.gradient(mo)
+        for _ in range(n_leapfrog):
+            x += pm * dt + (0.5 * dt * dt) * a
+            a1 = -eo.gradient(mo)
+            pm += (0.5 * dt) * (a + a1)
+            a = a1
+        h1 = eo.energy(mo) + 0.5 * float((pm * pm).sum())
+        if rng.random() <= np.exp(min(0.0, h0 - h1)):
+            acc += 1
+        else:
+            x[:] = x0
+        t1 = time.perf_counter()
+        flips += O.flip_parallel(mo, eo, ratio, int(rng.integers(1 << 31)))
+        t_flip += time.perf_counter() - t1
+        t_hmc += t1 - t0
+    sec = t_hmc + t_flip
+    return {"steps": n_steps, "seconds": round(sec, 3), "steps_per_s": round(n_steps / sec, 4),
+            "ms_per_move": {"hmc": round(t_hmc * 1e3 / n_steps, 1), "flip": round(t_flip * 1e3 / n_steps, 1)},
+            "acceptance": acc / n_steps, "flips_accepted_per_sweep": flips / n_steps,
+            "cores": O.get_threads(), "kind": "port",
+            "sample": f"{n_steps} chain steps (HMC move of {n_leapfrog} velocity-Verlet steps at dt {dt:g} + pflip "
+                      f"sweep ratio {ratio}) from the chains' warmed 163,842-vertex state"}
+
+
 def batch_members(n_per_level=16, levels=(3, 4, 5, 6)):
     """The 64 membranes of the batch configuration: (points, faces, params)."""
     from trimem_gb300 import meshgen
@@ -705,6 +750,7 @@ def main():
         batch = {"error": f"{type(exc).__name__}: {exc}"}
 
     chain = {}
+    warm = None
     try:
         warm = chain_warm(stream, chain_start())
         chain["start"] = warm["info"]
@@ -724,6 +770,17 @@ def main():
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(p, f, prm)
+        if warm is not None:
+            try:
+                cc = cpu_chain_step(warm)
+                pl = chain.get("plain_fp64", {})
+                if "ess_bending" in pl:
+                    # same moves and the same algorithm: the GPU chain's ESS
+                    # per step at the CPU's step rate
+                    cc["ess_per_s_at_gpu_ess_per_step"] = round(pl["ess_bending"] / pl["steps"] * cc["steps_per_s"], 5)
+                cb["chain_step"] = cc
+            except Exception as exc:
+                cb["chain_step"] = {"error": f"{type(exc).__name__}: {exc}"}
 
     # this library's kernels per step: 8 per FP64 evaluation (k_face, k_edge,
     # k_bond_short, k_moved, k_rep_fast, k_rep_slow, k_vertex, k_grad) and 14
