@@ -121,3 +121,41 @@ def test_surrogate_hmc_step_uses_the_exact_hamiltonian(C):
     mesh.points()[:] = x.cpu().numpy()
     assert out4[3] == pytest.approx(en.energy(mesh), rel=1e-12)
     assert np.isfinite(out4[1]) and np.isfinite(out4[2])
+
+
+def test_trained_network_lowers_the_force_error(C):
+    """What the trained network gains over the leapfrog without it: on a
+    state of the 163,842-vertex benchmark membrane (relaxed by the device
+    L-BFGS, then a few chain steps at T 1), the surrogate gradient
+    g_local - F_nn is far closer to the exact FP64 gradient than g_local
+    alone (the same integrator with no learned force)."""
+    import torch
+
+    from trimem_gb300 import surrogate as S
+    from trimem_gb300.mc.device import DeviceChain, relaxed_state
+    from trimem_gb300.workloads import workload_params as wp
+
+    if not __import__("os").path.exists(S.WEIGHTS_L7):
+        pytest.skip("no trained weights")
+    p, f = meshgen.jittered_icosphere(7, seed=0)
+    prm = dict(wp(p, f, kappa_b=20.0, vfrac=0.65), cont_lambda=0.0)
+    x0, _ = relaxed_state(p, f, prm)
+    mesh = C.Mesh(x0, f)
+    en = C.Energy(mesh, C.params(**prm))
+    x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
+    DeviceChain(mesh, en, x, dt=5e-6, n_leapfrog=20, flip_ratio=0.0, seed=3).run(5)
+    L = C.lib()
+    C.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, _p(x), None))
+    g_exact = torch.empty_like(x)
+    C.check(L.tm_energy_eval_device(en.h, mesh.h, _p(x), _p(g_exact), None, None))
+    sg = C.Surrogate(mesh, np.load(S.WEIGHTS_L7))
+    g_sur = torch.empty_like(x)
+    C.check(L.tm_surrogate_gradient_device(sg.h, en.h, mesh.h, _p(x), _p(g_sur), None))
+    inp = S.Inputs(sg, en, mesh, x, 16)
+    torch.cuda.synchronize()
+    ref = float(torch.linalg.norm(g_exact))
+    err_net = float(torch.linalg.norm(g_sur - g_exact)) / ref
+    err_none = float(torch.linalg.norm(inp.gloc - g_exact)) / ref
+    print(f"relative gradient error: surrogate {err_net:.3e}, without the network {err_none:.3e}")
+    assert err_none > 0.02, err_none  # bending and repulsion: a sizeable part of the force here
+    assert err_net < 0.25 * err_none, (err_net, err_none)
