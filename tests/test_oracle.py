@@ -119,3 +119,30 @@ def test_parallel_flip_ratio_above_one_raises():
     m, e = _flip_setup()
     with pytest.raises(ValueError):
         O.flip_parallel(m, e, 1.5, 1)
+
+
+def test_windowed_sweep_accepts_like_the_serial_sweep():
+    """The device sweep's algorithm (decided in windows, conflicting
+    proposals deferred; the device matches this port bit for bit) against
+    the reference's serial sweep (src/flips.cpp:22-73): from the same state,
+    over independent seeds, the accepted flips and the energy after one
+    sweep have the same mean (z <= 4.5 with the seeds' standard errors)."""
+    m0, e = _flip_setup()
+    n = 30
+    res = {"serial": ([], []), "windowed": ([], [])}
+    for s in range(n):
+        for name in res:
+            m = m0.clone()
+            if name == "serial":
+                acc = O.flip_serial(m, e, 0.3, 1000 + s)
+            else:
+                acc = O.flip_windowed(m, e, 0.3, 5000 + s, 1, 512)
+            assert m.check() == 0
+            res[name][0].append(acc)
+            res[name][1].append(e.energy(m))
+    for k in range(2):
+        a, b = (np.asarray(res[name][k], dtype=np.float64) for name in ("serial", "windowed"))
+        se = np.hypot(a.std(ddof=1), b.std(ddof=1)) / np.sqrt(n)
+        z = abs(a.mean() - b.mean()) / se
+        assert z <= 4.5, (k, a.mean(), b.mean(), z)
+    assert np.mean(res["serial"][0]) > 100
