@@ -137,15 +137,16 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400):
-    """Oracle (reference algorithm on the host cores, all threads)."""
+def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400, warmup=1):
+    """Oracle (reference algorithm on the host cores, all threads): warmup
+    untimed evaluations, then evaluations until max_evals or budget_s."""
     from oracle import oracle as O
 
     nthreads = os.cpu_count() or 1
     O.set_threads(nthreads)
     mo = O.Mesh(p, f)
     eo = O.Energy(mo, O.default_params(**prm))
-    eo.time_energy_gradient(mo, 1)  # warm-up
+    eo.time_energy_gradient(mo, max(int(warmup), 1))  # untimed warm-up evaluations
     n, t = 0, 0.0
     rng = np.random.default_rng(1)
     x = mo.points()
@@ -415,9 +416,9 @@ def run_reference(args):
     if rank != 0:
         return
     p, f, prm = workload()
-    for _ in range(max(args.warmup, 0)):
-        pass
-    cb = cpu_baseline(p, f, prm, budget_s=max(20.0, 5.0 * args.steps), max_evals=max(3, args.steps * 2))
+    # a bounded sample: two evaluations per step, at most two minutes
+    cb = cpu_baseline(p, f, prm, budget_s=min(max(20.0, 5.0 * args.steps), 120.0),
+                      max_evals=max(3, args.steps * 2), warmup=args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(),
