@@ -213,6 +213,58 @@ def cpu_chain_step(state, n_steps=2, n_leapfrog=20, dt=5e-6, ratio=0.2):
                       f"sweep ratio {ratio}) from the chains' warmed 163,842-vertex state"}
 
 
+def level6_leg(stream, flush, n_evals=100, cpu=True):
+    """The 40,962-vertex evaluation loop (level-6 icosphere, kb 30, volume
+    target 0.8, the other parameters as the headline workload): FP64
+    energy+gradient evaluations with an N(0, 1e-4) displacement before each
+    and a cell-list rebuild every 10, each evaluation timed with CUDA events
+    after an L2 flush; beside it the CPU restatement on the host cores."""
+    import ctypes
+
+    import torch
+
+    from trimem_gb300 import capi, meshgen
+    from trimem_gb300.workloads import workload_params
+
+    p6, f6 = meshgen.jittered_icosphere(6, seed=0)
+    prm6 = workload_params(p6, f6)
+    mesh = capi.Mesh(p6, f6)
+    en = capi.Energy(mesh, capi.params(**prm6))
+    L = capi.lib()
+    x = torch.tensor(p6, dtype=torch.float64, device="cuda").contiguous()
+    g = torch.empty_like(x)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(66)
+    disp = [1e-4 * torch.randn(tuple(x.shape), dtype=torch.float64, device="cuda", generator=gen)
+            for _ in range(EVALS_PER_STEP)]
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+    sp = ctypes.c_void_p(stream)
+    ms = []
+    for i in range(n_evals + 10):
+        if i % EVALS_PER_STEP == 0:
+            capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ptr(x), sp))
+        x.add_(disp[i % EVALS_PER_STEP], alpha=1.0 if (i // EVALS_PER_STEP) % 2 == 0 else -1.0)
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        capi.check(L.tm_energy_eval_device(en.h, mesh.h, ptr(x), ptr(g), None, sp))
+        b.record()
+        if i >= 10:  # the first ten are warm-up
+            ms.append((a, b))
+    torch.cuda.synchronize()
+    eval_ms = sum(a.elapsed_time(b) for a, b in ms) / len(ms)
+    out = {"workload": "icosphere L6 (40962 vertices), FP64 energy+gradient, displacement N(0,1e-4) per eval, "
+                       "cell-list rebuild every 10 evals, L2 flushed before each",
+           "vertices": len(p6), "evals": n_evals, "eval_ms": round(eval_ms, 5),
+           "gpu_evals_per_s": round(1e3 / eval_ms, 1)}
+    if cpu:
+        cb = cpu_baseline(p6, f6, prm6, budget_s=8.0, max_evals=200)
+        out.update(cpu_evals_per_s=round(cb["value"], 3), cpu_cores=cb["cores"],
+                   gpu_over_cpu=round(1e3 / eval_ms / cb["value"], 1))
+    return out
+
+
 def batch_members(n_per_level=16, levels=(3, 4, 5, 6)):
     """The 64 membranes of the batch configuration: (points, faces, params)."""
     from trimem_gb300 import meshgen
@@ -746,6 +798,11 @@ def main():
            "api": "np.copyto(TriMesh.points(), x); EnergyManager.energy_gradient(mesh); update_repulsion every 10"}
 
     try:
+        level6 = level6_leg(stream, flush, cpu=(rank == 0 and not args.no_cpu))
+    except Exception as exc:  # the headline line is printed either way
+        level6 = {"error": f"{type(exc).__name__}: {exc}"}
+
+    try:
         batch = batch_leg(stream)
     except Exception as exc:  # the headline line is printed either way
         batch = {"error": f"{type(exc).__name__}: {exc}"}
@@ -796,6 +853,7 @@ def main():
                               "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4)}),
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(), "fp32_stencil": fp32, "df64_stencil": df64,
             "surrogate_force": surrogate,
+            "level6": level6,
             "batch_replicas": batch,
             "hmc_chain": chain,
             "gpu_launches": launches_per_step * args.steps}
