@@ -343,3 +343,38 @@ def test_fp32_stencil_error_bounds(C):
     for k in range(6):
         assert abs(p32[k] - p64[k]) <= 1e-5 * max(abs(p64[k]), 1e-12), k
     assert rel(g32, g64) < 1e-4
+
+
+def test_annealing_run_with_continuation(C):
+    """A continuation (annealing) run on the device, as the reference's
+    HMC callback drives it (src/trimem/mc/hmc.py:174-177, src/energy.cpp:30-55):
+    a device chain with flips, the reference properties advanced every five
+    steps until lambda reaches 1, area difference on (kc 10).  At the end the
+    device energy and gradient of the final (moved and flipped) membrane
+    match the oracle's, whose reference properties come from the same
+    initial state and the same number of continuation updates."""
+    import torch
+
+    from trimem_gb300.mc.device import DeviceChain
+
+    p, f = meshgen.jittered_icosphere(3, seed=6)
+    prm = workload_params(p, f, vfrac=0.8)
+    prm.update(cont_delta=0.1, cont_lambda=0.0, area_frac=0.95, curvature_frac=0.9, kappa_c=10.0)
+    mg = C.Mesh(p, f)
+    eg = C.Energy(mg, C.params(**prm))
+    mo0 = O.Mesh(p, f)
+    eo = O.Energy(mo0, O.default_params(**prm))
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    ch = DeviceChain(mg, eg, x, dt=1e-6, n_leapfrog=10, flip_ratio=0.2, seed=8)
+    for _ in range(12):
+        ch.run(5)
+        eg.update_reference_properties()
+        eo.update_reference_properties()
+    assert eg.params().cont_lambda >= 1.0 and ch.flips > 0
+    xf = ch.x.cpu().numpy()
+    mg.points()[:] = xf
+    mo = O.Mesh(xf, mg.fv_indices())
+    eo.update_repulsion(mo)
+    eg.update_repulsion(mg)
+    assert abs(eg.energy(mg) - eo.energy(mo)) <= RTOL * abs(eo.energy(mo))
+    assert rel(eg.gradient(mg), eo.gradient(mo)) < RTOL
