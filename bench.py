@@ -21,7 +21,20 @@ e2e:    the same evaluations through the public API (trimem_gb300.core:
 cpu_baseline / --impl reference: the reference algorithm restated on the
         host cores (the reference itself cannot be built: its OpenMesh
         submodule is empty), all threads, energy() + gradient() per
-        evaluation like the reference's Python drivers.
+        evaluation like the reference's Python drivers; chain_step: chain
+        steps of the same restatement from the chains' warmed state.
+
+Secondary objects on the same line (measured after the timed region):
+roofline        per-kernel times of one cold evaluation (CUDA events inside
+                the library), algorithmic bytes, DRAM traffic and FP64 pipe
+                activity from the committed ncu summary
+fp32_stencil, df64_stencil   the other stencil precisions: time and error
+surrogate_force the learned force: time, and its tensor-core FLOP rate
+level6          the 40,962-vertex evaluation loop, GPU and CPU
+batch_replicas  64 membranes of 642-40,962 vertices in one batch
+hmc_chain       device chains (HMC move + flip sweep) from a shared warm-up:
+                per-move times, acceptance, ESS/s of the bending energy and
+                the reduced volume, quarter means of the bending trace
 """
 import argparse
 import json

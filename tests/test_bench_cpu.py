@@ -60,3 +60,20 @@ def test_multi_rank_timing_takes_the_slowest_rank():
         assert p.exitcode == 0
     assert [o[1] for o in out] == [11.0, 11.0]
     assert all(abs(o[2] - 2 * 100 / 0.011) < 1e-6 for o in out)
+
+
+def test_cpu_chain_step_runs_the_oracle_chain(built):
+    """The CPU chain-step baseline on a small membrane: HMC moves and
+    parallel flip sweeps of the oracle, a finite rate and a valid
+    acceptance."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from trimem_gb300 import meshgen
+    from trimem_gb300.workloads import workload_params
+
+    p, f = meshgen.jittered_icosphere(2, seed=0)
+    prm = dict(workload_params(p, f, kappa_b=20.0), cont_lambda=0.0)
+    out = bench.cpu_chain_step({"x": p, "faces": f, "prm": prm}, n_steps=2, n_leapfrog=3, dt=1e-6)
+    assert out["steps"] == 2 and out["steps_per_s"] > 0
+    assert 0.0 <= out["acceptance"] <= 1.0 and out["flips_accepted_per_sweep"] >= 0
+    assert out["kind"] == "port" and out["cores"] >= 1
