@@ -52,46 +52,48 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 LEVEL = 7
 EVALS_PER_STEP = 10
+# stencil precision of the headline evaluations (tm_energy_set_stencil_precision)
+HEADLINE_STENCIL = 0
 METRIC = "grad evals/s (FP64 energy+gradient, 163,842-vertex icosphere)"
 UNIT = "evals/s"
 
 
 def workload():
-    from trimem_gb300.workloads import workload_params
-    from trimem_gb300 import meshgen
+    from trimem_gb300.workloads import very_large_mesh
 
-    p, f = meshgen.jittered_icosphere(LEVEL, seed=0)
-    prm = workload_params(p, f, kappa_b=20.0, vfrac=0.65)
-    return p, f, prm
+    return very_large_mesh()
 
 
-def config(extra=None):
-    c = {"workload": "icosphere L7 (163842 vertices), FP64 energy+gradient, cell-list rebuild every 10 evals, "
-                     "N(0,1e-4) displacement between evals (pre-drawn pool of 10, sign alternating per step)",
-         "vertices": 163842, "faces": 327680, "evals_per_step": EVALS_PER_STEP,
-         "l2": "flushed (256 MB write) before every timed evaluation and rebuild",
-         "parallelism": "replicas"}
-    if extra:
-        c.update(extra)
-    return c
+def config():
+    return {"workload": "icosphere L7 (163842 vertices), FP64 energy+gradient, cell-list rebuild every 10 evals, "
+                        "N(0,1e-4) displacement between evals (pre-drawn pool of 10, sign alternating per step)",
+            "vertices": 163842, "faces": 327680, "evals_per_step": EVALS_PER_STEP,
+            "l2": "flushed (256 MB write) before every timed evaluation and rebuild",
+            "parallelism": "replicas"}
+
+
+# the committed ncu summary of the headline evaluation's stages: DRAM bytes
+# per stage and the activity of the pipe that bounds the stencils
+TRAFFIC_PROFILE = "profiles/eval_kernels_L7_fp64_sections.md"
+PIPE_NAME = "fp64"
+PIPE_METRIC = "sm__pipe_fp64_cycles_active"
 
 
 def read_traffic():
-    """DRAM bytes per launch of each evaluation stage, and the FP64 pipe
-    activity of its main kernel, from the committed ncu summary
-    (profiles/eval_kernels_L7_fp64_sections.md)."""
-    out, fp64 = {}, {}
-    path = os.path.join(ROOT, "profiles", "eval_kernels_L7_fp64_sections.md")
+    """DRAM bytes per launch of each evaluation stage, and the pipe activity
+    of its main kernel (percent), from the committed ncu summary
+    TRAFFIC_PROFILE: lines "<stage> <bytes>" and "<pipe> <stage> <pct>"."""
+    out, pipe = {}, {}
     try:
-        for line in open(path):
+        for line in open(os.path.join(ROOT, TRAFFIC_PROFILE)):
             parts = line.split()
             if len(parts) == 2 and parts[0].startswith("k_") and parts[1].isdigit():
                 out[parts[0]] = int(parts[1])
-            if len(parts) == 3 and parts[0] == "fp64" and parts[1].startswith("k_"):
-                fp64[parts[1]] = float(parts[2])
+            if len(parts) == 3 and parts[0] == PIPE_NAME and parts[1].startswith("k_"):
+                pipe[parts[1]] = float(parts[2])
     except (OSError, ValueError):
         pass
-    return out, fp64
+    return out, pipe
 
 
 def read_peaks():
@@ -152,7 +154,9 @@ class Clocks:
 
 def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400, warmup=1):
     """Oracle (reference algorithm on the host cores, all threads): warmup
-    untimed evaluations, then evaluations until max_evals or budget_s."""
+    untimed evaluations, then evaluations until max_evals or budget_s.  The
+    process loads the oracle's timing build (-O3 -fopenmp, the compiler's
+    default FMA contraction) unless TRIMEM_ORACLE_BUILD says otherwise."""
     from oracle import oracle as O
 
     nthreads = os.cpu_count() or 1
@@ -176,9 +180,22 @@ def cpu_baseline(p, f, prm, budget_s=15.0, max_evals=400, warmup=1):
         eo.gradient(mo)
         t += time.perf_counter() - t0
         n += 1
-    return {"value": n / t, "unit": UNIT, "cores": O.get_threads(), "kind": "port",
+    return {"value": n / t, "unit": UNIT, "cores": O.get_threads(), "kind": "port", "build": O.BUILD,
             "sample": f"{n} evaluations (energy + gradient calls, one cell-list rebuild per 10, displacement "
                       f"N(0,1e-4)) of the 163,842-vertex workload, {t:.1f} s, OpenMP {O.get_threads()} threads"}
+
+
+def cpu_baseline_parity_build(budget_s=8.0):
+    """The same CPU sample with the oracle's parity build (no FMA
+    contraction), in a child process; returns its evaluations/s."""
+    env = dict(os.environ, TRIMEM_ORACLE_BUILD="parity")
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-sample", str(budget_s)], env=env,
+                       capture_output=True, text=True, timeout=600)
+    try:
+        out = json.loads(r.stdout.strip().splitlines()[-1])
+        return {"value": out["value"], "unit": UNIT, "build": out["build"], "sample": out["sample"]}
+    except Exception:
+        return {"error": (r.stderr or r.stdout)[-300:]}
 
 
 def cpu_chain_step(state, n_steps=2, n_leapfrog=20, dt=5e-6, ratio=0.2):
@@ -552,13 +569,17 @@ def run_profile(args):
 
 
 def main():
+    # the CPU legs time the oracle's -O3 -fopenmp build (the reference's own
+    # compiler settings); the parity build is timed beside it in a child
+    # process.  Set before this process first loads the oracle.
+    os.environ.setdefault("TRIMEM_ORACLE_BUILD", "timing")
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--e2e-evals", type=int, default=30)
+    ap.add_argument("--e2e-evals", type=int, default=200)
     ap.add_argument("--profile-evals", type=int, default=0,
                     help="only run this many device evaluations (for ncu captures) and exit")
     ap.add_argument("--stencil", type=int, default=0, help="stencil precision of --profile-evals (0, 1, 2)")
@@ -568,7 +589,13 @@ def main():
                     help="only run this many flip sweeps (ratio 0.2) (for ncu captures) and exit")
     ap.add_argument("--profile-batch", type=int, default=0,
                     help="only run this many HMC steps of the 64-replica batch (for ncu captures) and exit")
+    ap.add_argument("--cpu-sample", type=float, default=0.0,
+                    help="only time the CPU sample of the headline workload for this many seconds, print it, exit")
     args = ap.parse_args()
+    if args.cpu_sample:
+        p, f, prm = workload()
+        print(json.dumps(cpu_baseline(p, f, prm, budget_s=args.cpu_sample, max_evals=200)), flush=True)
+        return
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_evals or args.profile_surrogate or args.profile_flips or args.profile_batch:
@@ -593,6 +620,7 @@ def main():
     mesh = capi.Mesh(p, f)
     en = capi.Energy(mesh, capi.params(**prm))
     L = capi.lib()
+    capi.check(L.tm_energy_set_stencil_precision(en.h, HEADLINE_STENCIL))
     # a dedicated stream: the library runs on it and the timing events are
     # recorded on it (the NULL handle would select the library's own stream)
     side = torch.cuda.Stream()
@@ -659,7 +687,11 @@ def main():
     ms_per_step = dev_ms / args.steps
     value = job_rate(world, EVALS_PER_STEP * args.steps, dev_ms)
 
-    # ---- per-kernel times of one evaluation (cold L2) for the roofline -----
+    # ---- roofline of the whole evaluation ----------------------------------
+    # algorithmic bytes of one FP64 energy+gradient evaluation: 132 per
+    # vertex (positions 24, ordered 1-ring CSR 28, flap indices 24, per-vertex
+    # (c, a) written and read back between the passes 32, gradient 24), over
+    # the measured time of one evaluation of the timed loop
     import ctypes
 
     kms = []
@@ -670,40 +702,46 @@ def main():
         kms.append(list(ms5))
     kms = np.median(np.array(kms), axis=0)
     names = ["k_face", "k_edge", "k_vertex", "k_grad"]
-    dom = int(np.argmax(kms[:4]))
     F, E = len(f), 3 * len(f) // 2
-    # unique bytes each kernel must move (inputs + outputs) per launch
-    kbytes = {
+    # the unique bytes each stage's kernels read and write per launch (their
+    # inputs and outputs, including this implementation's face and edge
+    # records), for comparison with the per-stage DRAM traffic
+    stage_bytes = {
         "k_face": 3 * 4 * F + 24 * V + 64 * F,
         "k_edge": 16 * E + 24 * V + 64 * F + 40 * E,
-        "k_vertex": 4 * V + 16 * 2 * E + 16 * F + 16 * E + 8 * V + 16 * V,  # valence, slots, (A, V), (l th, bond), pot, rk
+        "k_vertex": 4 * V + 16 * 2 * E + 16 * F + 16 * E + 8 * V + 16 * V,
         "k_grad": 4 * V + 16 * 2 * E + 24 * V + 16 * V + 64 * F + 32 * E + 24 * V + 24 * V,
     }
     peaks = read_peaks()
     hbm = peaks.get("hbm_gbs")
     peak_note = "of measured" if hbm else "of fallback"
     hbm = hbm or 6800.0
-    dname = names[dom]
-    achieved = kbytes[dname] / (kms[dom] * 1e-3) / 1e9
-    traffic_all, fp64_active = read_traffic()
-    traffic = traffic_all.get(dname)
-    # whole evaluation: 132 algorithmic bytes per vertex
     eval_bytes = 132 * V
-    roofline = {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 5), "traffic": traffic, "peak_source": peak_note,
-                "kernel_ms": {n: round(float(k), 5) for n, k in zip(names, kms[:4])},
+    achieved = eval_bytes / (eval_ms * 1e-3) / 1e9
+    traffic_all, pipe_active = read_traffic()
+    traffic = sum(traffic_all.values()) if len(traffic_all) == 4 else None
+    dom = int(np.argmax(kms[:4]))
+    dname = names[dom]
+    roofline = {"bound": "hbm", "kernel": "one energy+gradient evaluation (all its launches)",
+                "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 5),
+                "traffic": traffic, "peak_source": peak_note,
+                "algorithmic_bytes": eval_bytes, "algorithmic_bytes_per_vertex": 132,
+                "eval_ms": round(eval_ms, 5),
+                "traffic_source": "sum over the evaluation's stages of ncu dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum (cold-cache captures), " + TRAFFIC_PROFILE,
+                "stage_ms_cold": {n: round(float(k), 5) for n, k in zip(names, kms[:4])},
                 "eval_ms_cold": round(float(kms[4]), 5),
-                "eval_algorithmic_bytes": eval_bytes,
-                "eval_frac": round(eval_bytes / (kms[4] * 1e-3) / 1e9 / hbm, 5),
-                "algorithmic_bytes": kbytes[dname],
-                # what bounds the FP64 stencils instead of HBM: FP64 issue
-                "issue_bound": {"pipe": "fp64", "kernel": dname,
-                                "pipe_active_frac": (round(fp64_active[dname] / 100.0, 3)
-                                                     if dname in fp64_active else None),
-                                "source": "ncu sm__pipe_fp64_cycles_active, profiles/eval_kernels_L7_fp64_sections.md"}}
+                "stage_unique_bytes": stage_bytes,
+                # what bounds the stencils instead of HBM: instruction issue on
+                # the arithmetic pipe of the dominant stage
+                "issue_bound": {"pipe": PIPE_NAME, "kernel": dname,
+                                "pipe_active_frac": (round(pipe_active[dname] / 100.0, 3)
+                                                     if dname in pipe_active else None),
+                                "source": "ncu " + PIPE_METRIC + ", " + TRAFFIC_PROFILE}}
 
-    # ---- FP32-stencil variant: speed and error against FP64 ---------------
+    # ---- the stencil precisions: speed and error against FP64 -------------
     g64 = g.clone()
+    capi.check(L.tm_energy_set_stencil_precision(en.h, 0))
     capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes_ptr(x), ctypes_ptr(g64), ctypes_ptr(e_dev),
                                        ctypes_ptr_s(stream)))
     torch.cuda.synchronize()
@@ -720,7 +758,7 @@ def main():
                                            ctypes_ptr_s(stream)))
         torch.cuda.synchronize()
         ev = float(e_dev.item())
-        capi.check(L.tm_energy_set_stencil_precision(en.h, 0))
+        capi.check(L.tm_energy_set_stencil_precision(en.h, HEADLINE_STENCIL))
         ks = np.median(np.array(ks), axis=0)
         return {"eval_ms_cold": round(float(ks[4]), 5), "evals_per_s_cold": round(1e3 / float(ks[4]), 1),
                 "kernel_ms": {n_: round(float(k), 5) for n_, k in zip(names, ks[:4])},
@@ -739,7 +777,7 @@ def main():
                                        ctypes_ptr_s(stream)))
     torch.cuda.synchronize()
     e32 = float(e_dev.item())
-    capi.check(L.tm_energy_set_stencil_precision(en.h, 0))
+    capi.check(L.tm_energy_set_stencil_precision(en.h, HEADLINE_STENCIL))
     k32 = np.median(np.array(k32), axis=0)
     fp32 = {"eval_ms_cold": round(float(k32[4]), 5), "evals_per_s_cold": round(1e3 / float(k32[4]), 1),
             "kernel_ms": {n: round(float(k), 5) for n, k in zip(names, k32[:4])},
@@ -784,6 +822,10 @@ def main():
         surrogate = {"error": f"{type(exc).__name__}: {exc}"}
 
     # ---- end to end through the public API ---------------------------------
+    # the reference's drivers write the positions into TriMesh.points() and
+    # call EnergyManager.energy and EnergyManager.gradient separately
+    # (src/trimem/mc/evaluators.py fun / grad); each call uploads the host
+    # positions and evaluates.  The fused energy_gradient call is timed beside.
     cm = core.TriMesh(p, f)
     ep = core.EnergyParams()
     for k in ["kappa_b", "kappa_a", "kappa_v", "kappa_c", "kappa_t", "kappa_r", "area_frac", "volume_frac",
@@ -792,23 +834,42 @@ def main():
     ep.bond_params.lc0, ep.bond_params.lc1, ep.bond_params.a0 = prm["bond_lc0"], prm["bond_lc1"], prm["bond_a0"]
     ep.repulse_params.lc1, ep.repulse_params.rlist = prm["rep_lc1"], prm["rlist"]
     estore = core.EnergyManager(cm, ep)
+    estore.set_stencil_precision(HEADLINE_STENCIL)
     rng = np.random.default_rng(5)
     host_x = [p + rng.normal(0, 1e-4, size=p.shape) for _ in range(4)]
     pts = cm.points()
     for i in range(3):
         np.copyto(pts, host_x[i % 4])
+        estore.energy(cm)
+        estore.gradient(cm)
         estore.energy_gradient(cm)
     n_e2e = args.e2e_evals
-    t0 = time.perf_counter()
-    for i in range(n_e2e):
-        if i % EVALS_PER_STEP == 0:
-            estore.update_repulsion(cm)
-        np.copyto(pts, host_x[i % 4])
-        en_val, grad = estore.energy_gradient(cm)
-    t1 = time.perf_counter()
-    e2e = {"value": n_e2e / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": EVALS_PER_STEP * 24 * V + 24 * V,
-           "d2h_bytes_per_step": EVALS_PER_STEP * (24 * V + 8),
-           "api": "np.copyto(TriMesh.points(), x); EnergyManager.energy_gradient(mesh); update_repulsion every 10"}
+
+    def e2e_loop(fused):
+        t0 = time.perf_counter()
+        for i in range(n_e2e):
+            if i % EVALS_PER_STEP == 0:
+                estore.update_repulsion(cm)
+            np.copyto(pts, host_x[i % 4])
+            if fused:
+                estore.energy_gradient(cm)
+            else:
+                estore.energy(cm)
+                estore.gradient(cm)
+        return n_e2e / (time.perf_counter() - t0)
+
+    globals_bytes = 184  # the device's global sums and energy terms, read back by energy()
+    e2e = {"value": e2e_loop(False), "unit": UNIT,
+           "h2d_bytes_per_step": EVALS_PER_STEP * 2 * 24 * V + 24 * V,
+           "d2h_bytes_per_step": EVALS_PER_STEP * (24 * V + globals_bytes),
+           "evals": n_e2e,
+           "api": "np.copyto(TriMesh.points(), x); EnergyManager.energy(mesh); EnergyManager.gradient(mesh); "
+                  "update_repulsion every 10 evaluations",
+           "fused": {"value": e2e_loop(True), "unit": UNIT,
+                     "h2d_bytes_per_step": EVALS_PER_STEP * 24 * V + 24 * V,
+                     "d2h_bytes_per_step": EVALS_PER_STEP * (24 * V + 8),
+                     "api": "np.copyto(TriMesh.points(), x); EnergyManager.energy_gradient(mesh) (one call, "
+                            "no counterpart in the reference)"}}
 
     try:
         level6 = level6_leg(stream, flush, cpu=(rank == 0 and not args.no_cpu))
@@ -841,6 +902,7 @@ def main():
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(p, f, prm)
+        cb["parity_build"] = cpu_baseline_parity_build()
         if warm is not None:
             try:
                 cc = cpu_chain_step(warm)
@@ -862,8 +924,10 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config({"eval_ms": round(eval_ms, 5), "rebuild_ms": round(rebuild_ms, 5),
-                              "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4)}),
+            "config": config(),
+            "timing": {"eval_ms": round(eval_ms, 5), "rebuild_ms": round(rebuild_ms, 5),
+                       "wall_ms_per_step_incl_flush": round((w1 - w0) * 1e3 / args.steps, 4),
+                       "stencil": HEADLINE_STENCIL},
             "roofline": roofline, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(), "fp32_stencil": fp32, "df64_stencil": df64,
             "surrogate_force": surrogate,
             "level6": level6,

@@ -143,11 +143,15 @@ int tm_energy_eval_timed(tm_energy* e, tm_mesh* m, const double* d_points, doubl
 #define TM_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
 /* tm_energy_eval_device (FP64 stencil) for callers that must not allocate
  * device memory during the evaluation: the scratch lives in one file-scope
- * device array of TM_NOALLOC_SCRATCH_BYTES (about 53,000 vertices; larger
- * meshes are rejected with TM_ERR_ARG) instead of the energy manager's
- * buffers.  The first call on a device looks up the array's address and must
- * precede any stream capture; calls that overlap on the GPU share the array
- * and race.  No counterpart in the reference. */
+ * device array of TM_NOALLOC_SCRATCH_BYTES (about 380 bytes per vertex, so
+ * about 44,000 vertices; larger meshes are rejected with TM_ERR_ARG) instead
+ * of the energy manager's buffers.  d_grad must not be NULL (TM_ERR_ARG), and
+ * the stencil precision set by tm_energy_set_stencil_precision is ignored:
+ * the stencil is always FP64.  The first call on a device looks up the
+ * array's address and must precede any stream capture; the address is kept
+ * for the life of the process and does not survive cudaDeviceReset.  Calls
+ * that overlap on the GPU share the array and race.  No counterpart in the
+ * reference. */
 int tm_energy_eval_device_noalloc(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad,
                                   double* d_energy, void* stream);
 /* Rebuilds the neighbour list from device-resident positions. */

@@ -1326,6 +1326,10 @@ void om_energy_gradient(void* e, void* m, double* out) { ((Energy*)e)->gradient(
 void om_energy_update_reference(void* e) { ((Energy*)e)->update_reference(); }
 void om_energy_update_repulsion(void* e, void* m) { ((Energy*)e)->update_repulsion(*(Mesh*)m); }
 void om_energy_initial_props(void* e, double* out) { put_props(((Energy*)e)->initial, out); }
+void om_energy_set_initial_props(void* e, const double* p) {
+  Props& q = ((Energy*)e)->initial;
+  q.area = p[0]; q.volume = p[1]; q.curvature = p[2]; q.bending = p[3]; q.tethering = p[4]; q.repulsion = p[5];
+}
 void om_energy_ref_props(void* e, double* out) { put_props(((Energy*)e)->ref_props(), out); }
 double om_energy_lambda(void* e) { return ((Energy*)e)->prm.cont_lambda; }
 

@@ -76,6 +76,9 @@ void om_energy_gradient(void* e, void* m, double* out3v);
 void om_energy_update_reference(void* e);
 void om_energy_update_repulsion(void* e, void* m);
 void om_energy_initial_props(void* e, double* out6);
+/* reference properties of a chain started elsewhere (the reference's
+ * checkpoint restart keeps the original initial properties) */
+void om_energy_set_initial_props(void* e, const double* props6);
 void om_energy_ref_props(void* e, double* out6);
 double om_energy_lambda(void* e);
 

@@ -13,7 +13,15 @@ import subprocess
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(_HERE, "_build", platform.machine(), "liboracle.so")
+# TRIMEM_ORACLE_BUILD selects the build this process loads: "parity" (the
+# default; no FMA contraction, what the tests check against) or "timing"
+# (-O3 -fopenmp with the compiler's default contraction, the timed CPU
+# baseline).  Read once, at the first use.
+BUILD = os.environ.get("TRIMEM_ORACLE_BUILD", "parity")
+if BUILD not in ("parity", "timing"):
+    raise ValueError(f"TRIMEM_ORACLE_BUILD must be 'parity' or 'timing', not {BUILD!r}")
+_LIB_PATH = os.path.join(_HERE, "_build", platform.machine(),
+                         "liboracle.so" if BUILD == "parity" else "liboracle_timing.so")
 _lib = None
 
 _d = ctypes.c_double
@@ -85,6 +93,7 @@ def lib():
             "om_energy_update_reference": (None, [_p]),
             "om_energy_update_repulsion": (None, [_p, _p]),
             "om_energy_initial_props": (None, [_p, _dp]),
+            "om_energy_set_initial_props": (None, [_p, _dp]),
             "om_energy_ref_props": (None, [_p, _dp]),
             "om_energy_lambda": (_d, [_p]),
             "om_nlist_create": (_p, [_p, _i, _i, _d]),
@@ -234,6 +243,10 @@ class Energy:
         lib().om_energy_initial_props(self.h, _ptr(out))
         return out
 
+    def set_initial_props(self, props6):
+        p = np.ascontiguousarray(props6, dtype=np.float64)
+        lib().om_energy_set_initial_props(self.h, _ptr(p))
+
     def ref_props(self):
         out = np.empty(6)
         lib().om_energy_ref_props(self.h, _ptr(out))
@@ -309,3 +322,37 @@ def area(mesh):
 
 def edges_length(mesh):
     return lib().om_edges_length(mesh.h)
+
+
+# ---------------------------------------------------------------------------
+# HMC chain (src/trimem/mc/hmc.py:14-26 velocity Verlet, :138-165 Metropolis
+# step), restated for the checks: numpy's global generator is drawn in the
+# reference's order -- one normal array for the momenta, then one uniform for
+# the acceptance -- so a chain started from np.random.seed(s) reproduces the
+# reference's chain step for step.
+# ---------------------------------------------------------------------------
+def leapfrog(x, p, force, mass, dt, n):
+    """n velocity-Verlet steps in position/momentum form (hmc.py:14-26)."""
+    a = force(x)
+    for _ in range(n):
+        x = x + (p * dt + 0.5 * dt * dt * a) / mass
+        a_new = force(x)
+        p = p + 0.5 * dt * (a + a_new)
+        a = a_new
+    return x, p
+
+
+def hmc_chain(x, energy, gradient, n_steps, dt, n_leapfrog, mass=1.0, temperature=1.0):
+    """n_steps Metropolis-corrected HMC moves at a fixed temperature
+    (hmc.py:138-165).  Returns (final state, number of accepted moves)."""
+    accepted = 0
+    for _ in range(n_steps):
+        p = np.random.normal(size=x.shape) * np.sqrt(mass * temperature)
+        xn, pn = leapfrog(x, p, lambda y: -gradient(y), mass, dt, n_leapfrog)
+        h_new = energy(xn) + 0.5 * float(pn.ravel() @ pn.ravel()) / mass
+        h_old = energy(x) + 0.5 * float(p.ravel() @ p.ravel()) / mass
+        dh = (h_new - h_old) / temperature
+        if np.random.uniform() <= (1.0 if dh <= 0 else np.exp(-dh)):
+            x = xn
+            accepted += 1
+    return x, accepted

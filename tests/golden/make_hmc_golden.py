@@ -9,8 +9,8 @@ x_L = a x_0 + b p, so for each of the 2^10 accept/reject patterns the start
 x_0 follows from ref_hmc by one division.  The pattern whose x_0 rows are the
 twelve unit vectors of an icosahedron and whose forward run (with this
 package's HMC, which recomputes every accept decision) reproduces ref_hmc to
-1e-14 is kept.  Run with the reference mounted at $TRIMEM_REFERENCE
-(default /root/reference).
+1e-14 is kept.  Run with the environment variable TRIMEM_REFERENCE set to
+the root of a trimem checkout (the folder holding tests/test_sampling.py).
 """
 import ast
 import itertools
@@ -24,13 +24,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from trimem_gb300.mc.hmc import HMC  # noqa: E402
+from oracle import oracle as O  # noqa: E402
 from trimem_gb300.meshgen import hull_faces  # noqa: E402
 
-REF = os.environ.get("TRIMEM_REFERENCE", "/root/reference")
+REF = os.environ.get("TRIMEM_REFERENCE")
 
 
 def read_ref_hmc():
+    if not REF:
+        raise SystemExit("set TRIMEM_REFERENCE to the root of a trimem checkout")
     src = open(os.path.join(REF, "tests", "test_sampling.py")).read()
     m = re.search(r"ref_hmc\s*=\s*np\.array\(\s*(\[.*?\])\s*\)", src, flags=re.S)
     return np.array(ast.literal_eval(m.group(1)))
@@ -47,10 +49,9 @@ def vv_map(dt, L):
 
 def run(x0, steps=10):
     np.random.seed(42)
-    h = HMC(x0.copy(), lambda x: 0.5 * x.ravel().dot(x.ravel()), lambda x: x,
-            options={"info_step": 10, "time_step": 1.0e-1})
-    h.run(steps)
-    return h.x
+    x, _ = O.hmc_chain(x0.copy(), lambda x: 0.5 * x.ravel().dot(x.ravel()), lambda x: x,
+                       n_steps=steps, dt=0.1, n_leapfrog=100)
+    return x
 
 
 def main():

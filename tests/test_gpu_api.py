@@ -113,28 +113,6 @@ def test_flips_module(m, fn):
     assert len(np.unique(np.sort(mesh.fv_indices(), axis=1), axis=0)) == mesh.fv_indices().shape[0]
 
 
-def test_mesh_hmc_matches_reference_chain(m):
-    from trimem_gb300.mc.hmc import MeshHMC
-    from trimem_gb300.mc.mesh import Mesh
-
-    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "hmc_icosahedron.json")))
-    np.random.seed(42)
-    mesh = Mesh(np.array(g["x0"]), np.array(g["faces"]))
-
-    def energy(x):
-        mesh.x = x
-        return 0.5 * x.ravel().dot(x.ravel())
-
-    def gradient(x):
-        mesh.x = x
-        return x
-
-    hmc = MeshHMC(mesh, energy, gradient, options={"info_step": 10, "time_step": 1.0e-1})
-    hmc.run(10)
-    assert np.linalg.norm(hmc.x - np.array(g["ref_hmc"])) < 1.0e-14
-    assert np.array_equal(mesh.x, hmc.x)
-
-
 def test_points_view_is_zero_copy(m):
     p, f = meshgen.icosphere(2)
     mesh = m.TriMesh(p, f)

@@ -1,7 +1,7 @@
 """ctypes binding of the C ABI (``include/trimem_gpu.h``).
 
-This is the boundary a non-Python host binds; the tests
-use it to drive the library exactly the way such a host would.
+This is the boundary a non-Python host binds; the tests use it to drive the
+library exactly the way such a host would.
 """
 import ctypes
 import os

@@ -22,3 +22,19 @@ def workload_params(p, f, kappa_b=30.0, vfrac=0.8, bond_type=0, n_search=0, excl
                 bond_lc0=1.15 * l, bond_lc1=0.85 * l, bond_a0=a, bond_r=2, bond_type=bond_type,
                 rep_lc1=rep_scale * l, rep_r=2, n_search=n_search, rlist=rep_scale * l, exclusion_level=excl,
                 cont_delta=0.0, cont_lambda=1.0)
+
+
+def very_large_mesh():
+    """The 163,842-vertex membrane (level-7 icosphere, jitter seed 0) with the
+    very-large-mesh energy: kb 20, reduced-volume target 0.65, the other
+    parameters as workload_params.  Returns (points, faces, params)."""
+    p, f = meshgen.jittered_icosphere(7, seed=0)
+    return p, f, workload_params(p, f, kappa_b=20.0, vfrac=0.65)
+
+
+def small_mesh():
+    """The CPU-sized membrane: level-4 icosphere (2,562 vertices), vertices
+    jittered by N(0, 0.01) (seed 0), workload_params (kb 30, volume target
+    0.8).  Returns (points, faces, params)."""
+    p, f = meshgen.jittered_icosphere(4, seed=0)
+    return p, f, workload_params(p, f)
