@@ -53,7 +53,7 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 LEVEL = 7
 EVALS_PER_STEP = 10
 # stencil precision of the headline evaluations (tm_energy_set_stencil_precision)
-HEADLINE_STENCIL = 0
+HEADLINE_STENCIL = 2
 METRIC = "grad evals/s (FP64 energy+gradient, 163,842-vertex icosphere)"
 UNIT = "evals/s"
 
@@ -834,7 +834,7 @@ def main():
     ep.bond_params.lc0, ep.bond_params.lc1, ep.bond_params.a0 = prm["bond_lc0"], prm["bond_lc1"], prm["bond_a0"]
     ep.repulse_params.lc1, ep.repulse_params.rlist = prm["rep_lc1"], prm["rlist"]
     estore = core.EnergyManager(cm, ep)
-    estore.set_stencil_precision(HEADLINE_STENCIL)
+    estore.set_stencil_precision({0: "fp64", 1: "fp32", 2: "df64"}[HEADLINE_STENCIL])
     rng = np.random.default_rng(5)
     host_x = [p + rng.normal(0, 1e-4, size=p.shape) for _ in range(4)]
     pts = cm.points()

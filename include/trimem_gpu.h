@@ -25,8 +25,7 @@ enum {
   TM_ERR_TOPOLOGY = -3, /* non-manifold input or valence above TM_MAXVAL   */
   TM_ERR_RANGE = -4,    /* std::range_error in the reference (flip ratio)   */
   TM_ERR_TIMEOUT = -5,  /* a bounded device wait gave up                    */
-  TM_ERR_NOMEM = -6,    /* device or pinned allocation failed               */
-  TM_ERR_DEVICE = -7    /* a device-side check recorded a bad index         */
+  TM_ERR_NOMEM = -6     /* device or pinned allocation failed               */
 };
 
 /* Largest vertex valence the device ring tables hold. */
@@ -122,9 +121,10 @@ int tm_energy_components(tm_energy* e, tm_mesh* m, double* out7);
 int tm_energy_gradient(tm_energy* e, tm_mesh* m, double* grad, double* energy);
 int tm_energy_update_reference_properties(tm_energy* e);
 int tm_energy_update_repulsion(tm_energy* e, tm_mesh* m);
-/* Local stencil precision: 0 FP64 (default), 1 FP32 (positions split into
- * float hi/lo parts, FP64 global sums), 2 double-float (pairs of floats on
- * the FP32 pipe, ~48-bit significands; FP64 global sums, exact pair tests).
+/* Local stencil precision: 0 FP64, 1 FP32 (positions split into float
+ * hi/lo parts, FP64 global sums), 2 double-word (the default: pairs of
+ * floats on the FP32 pipe, ~48-bit significands, results within ~1e-13 of
+ * FP64; FP64 global sums, penalty assembly and exact pair tests).
  * Per-vertex properties are always computed with the FP64 stencil. */
 int tm_energy_set_stencil_precision(tm_energy* e, int mode);
 
@@ -244,6 +244,14 @@ int tm_surrogate_hmc_step_device(tm_surrogate* s, tm_energy* e, tm_mesh* m, doub
  * and b float (64). */
 int tm_dense_silu_bf16(const void* d_h, const void* d_m, const void* d_w, const float* d_bias, void* d_out,
                        int64_t rows, void* stream);
+/* tm_dense_silu_bf16 with the poll limit of its two device waits (tile loads,
+ * MMA completion) given.  A wait that gives up makes the call return
+ * TM_ERR_TIMEOUT with the context still usable: the kernel records it,
+ * skips the dependent work, lets its own copies land and frees its tensor
+ * memory.  wait_polls = 0 makes the first wait give up at once; a test aid
+ * for the failure path, no counterpart in the reference. */
+int tm_dense_silu_bf16_bounded(const void* d_h, const void* d_m, const void* d_w, const float* d_bias, void* d_out,
+                               int64_t rows, int wait_polls, void* stream);
 
 /* ---- batches of replicas (no counterpart in the reference: the reference
  * runs one membrane per process) -------------------------------------------

@@ -131,5 +131,24 @@ def test_small_membrane_hybrid_run_matches_the_oracle(built):
             ch.step()
     assert len(checks) == 11
     assert ch.flips > 0
-    print(f"small membrane run: {ch.accepted} of 1000 HMC moves accepted, {ch.flips} flips, "
-          f"largest gradient deviation {max(checks):.1e}")
+    # at dt 1e-4 the jittered membrane's forces reject every HMC move (the
+    # reference's integrator behaves the same); the run continues with the
+    # largest time step that accepts, checked the same way
+    from trimem_gb300.mc.device import tune_dt
+
+    dt, _ = tune_dt(mg, eg, x, candidates=(1e-5, 5e-6, 2e-6, 1e-6, 5e-7, 2e-7))
+    ch2 = DeviceChain(mg, eg, x, dt=dt, n_leapfrog=20, flip_ratio=0.1, flip_mode=1, refresh=1, seed=7)
+    for step in range(1, 301):
+        ch2.step()
+        if step % 100 == 0:
+            xs = x.cpu().numpy()
+            mg.points()[:] = xs
+            mo = O.Mesh(xs, mg.fv_indices())
+            eo = O.Energy(mo, O.default_params(**prm))
+            eo.set_initial_props(initial)
+            eg.update_repulsion(mg)
+            checks.append(_compare_state(eg, mg, eo, mo, f"dt {dt:g} step {step}"))
+            assert mg.check() == 0
+    assert ch2.accepted > 0
+    print(f"small membrane run: {ch.accepted} of 1000 HMC moves accepted at dt 1e-4, {ch.flips} flips; "
+          f"{ch2.accepted} of 300 at dt {dt:g}, {ch2.flips} flips; largest gradient deviation {max(checks):.1e}")

@@ -18,6 +18,8 @@ TM_ERR_ARG = -1
 TM_ERR_CUDA = -2
 TM_ERR_TOPOLOGY = -3
 TM_ERR_RANGE = -4
+TM_ERR_TIMEOUT = -5
+TM_ERR_NOMEM = -6
 TM_MAXVAL = 32
 
 _d = ctypes.c_double
@@ -119,6 +121,7 @@ _SIGS = {
     "tm_surrogate_hmc_step_device": (_i32, [_p, _p, _p, _p, _d, _d, _i32, _d, ctypes.c_uint64, ctypes.c_uint64, _d,
                                             _dp, _dp, _p]),
     "tm_dense_silu_bf16": (_i32, [_p, _p, _p, _p, _p, _i64, _p]),
+    "tm_dense_silu_bf16_bounded": (_i32, [_p, _p, _p, _p, _p, _i64, _i32, _p]),
 }
 
 _lib = None

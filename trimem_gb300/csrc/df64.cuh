@@ -162,4 +162,106 @@ __device__ __forceinline__ bool df_atan2_pos(df y, df x, df* out) {
   return true;
 }
 
+// ---- lighter forms for the stencils ---------------------------------------
+// The positions enter as double-words of about 48 bits, so every quantity of
+// the stencils carries an absolute error of a few u^2 times the magnitudes it
+// is built from.  These forms keep to that absolute error and skip the work
+// that only buys relative accuracy under cancellation:
+//   add_s   SloppyDWPlusDW (Joldes, Muller & Popescu 2017, Algorithm 5),
+//           error a few u^2 (|x| + |y|), 11 operations instead of 20;
+//   mul_s   DWTimesDW without the lo*lo term (below u^2 relative);
+//   dot3 / cross_c   sums of exact products (TwoProd with FMA) in the style
+//           of Ogita, Rump & Oishi's Dot2, one TwoSum per addition and all
+//           error terms collected in one float;
+//   dacc    a running sum whose float lo part gathers the TwoSum errors
+//           (Sum2 of the same paper), renormalised once at the end;
+//   rsqrt_dw / rcp_dw   one Newton step from the float estimate (relative
+//           error about 2^-46).
+__device__ __forceinline__ df add_s(df x, df y) {
+  df s = two_sum(x.hi, y.hi);
+  float c = __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo));
+  return fast_two_sum(s.hi, c);
+}
+__device__ __forceinline__ df sub_s(df x, df y) { return add_s(x, df{-y.hi, -y.lo}); }
+__device__ __forceinline__ df mul_s(df x, df y) {
+  df c = two_prod(x.hi, y.hi);
+  float t = __fmaf_rn(x.hi, y.lo, __fmul_rn(x.lo, y.hi));
+  return fast_two_sum(c.hi, __fadd_rn(c.lo, t));
+}
+__device__ __forceinline__ df neg(df x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ df half(df x) { return {0.5f * x.hi, 0.5f * x.lo}; }
+// x >= 0 test and |x| on the leading part (hi carries the sign)
+__device__ __forceinline__ df dabs(df x) { return x.hi < 0.0f ? neg(x) : x; }
+
+__device__ __forceinline__ df3 sub3(const df3& a, const df3& b) {
+  return {sub_s(a.x, b.x), sub_s(a.y, b.y), sub_s(a.z, b.z)};
+}
+__device__ __forceinline__ df3 scale3(df s, const df3& a) { return {mul_s(s, a.x), mul_s(s, a.y), mul_s(s, a.z)}; }
+
+// a . b
+__device__ __forceinline__ df dot3(const df3& a, const df3& b) {
+  df p0 = two_prod(a.x.hi, b.x.hi), p1 = two_prod(a.y.hi, b.y.hi), p2 = two_prod(a.z.hi, b.z.hi);
+  df s = two_sum(p0.hi, p1.hi);
+  df t = two_sum(s.hi, p2.hi);
+  float lo = __fadd_rn(__fadd_rn(p0.lo, p1.lo), __fadd_rn(p2.lo, __fadd_rn(s.lo, t.lo)));
+  lo = __fmaf_rn(a.x.hi, b.x.lo, lo);
+  lo = __fmaf_rn(a.x.lo, b.x.hi, lo);
+  lo = __fmaf_rn(a.y.hi, b.y.lo, lo);
+  lo = __fmaf_rn(a.y.lo, b.y.hi, lo);
+  lo = __fmaf_rn(a.z.hi, b.z.lo, lo);
+  lo = __fmaf_rn(a.z.lo, b.z.hi, lo);
+  return two_sum(t.hi, lo);
+}
+// a1 b2 - a2 b1 (one component of a cross product)
+__device__ __forceinline__ df cross_c(df a1, df b2, df a2, df b1) {
+  df p = two_prod(a1.hi, b2.hi), q = two_prod(a2.hi, b1.hi);
+  df s = two_sum(p.hi, -q.hi);
+  float lo = __fadd_rn(__fsub_rn(p.lo, q.lo), s.lo);
+  lo = __fmaf_rn(a1.hi, b2.lo, lo);
+  lo = __fmaf_rn(a1.lo, b2.hi, lo);
+  lo = __fmaf_rn(-a2.hi, b1.lo, lo);
+  lo = __fmaf_rn(-a2.lo, b1.hi, lo);
+  return two_sum(s.hi, lo);
+}
+__device__ __forceinline__ df3 cross3(const df3& a, const df3& b) {
+  return {cross_c(a.y, b.z, a.z, b.y), cross_c(a.z, b.x, a.x, b.z), cross_c(a.x, b.y, a.y, b.x)};
+}
+
+struct dacc {
+  float hi, lo;
+};
+__device__ __forceinline__ void acc_add(dacc& a, df x) {
+  df s = two_sum(a.hi, x.hi);
+  a.hi = s.hi;
+  a.lo = __fadd_rn(a.lo, __fadd_rn(s.lo, x.lo));
+}
+__device__ __forceinline__ df acc_val(const dacc& a) { return two_sum(a.hi, a.lo); }
+struct dacc3 {
+  dacc x, y, z;
+};
+__device__ __forceinline__ void acc_add3(dacc3& a, const df3& v) {
+  acc_add(a.x, v.x);
+  acc_add(a.y, v.y);
+  acc_add(a.z, v.z);
+}
+__device__ __forceinline__ df3 acc_val3(const dacc3& a) { return {acc_val(a.x), acc_val(a.y), acc_val(a.z)}; }
+
+// 1 / sqrt(q), q > 0: with q r0^2 = 1 - e (r0 the float estimate, |e| of
+// order 2^-22), 1/sqrt(q) = r0 (1 + e/2 + 3e^2/8 + O(e^3))
+__device__ __forceinline__ df rsqrt_dw(df q) {
+  const float r0 = rsqrtf(q.hi);
+  const df y = mul_s(q, two_prod(r0, r0));
+  const float e = __fsub_rn(__fsub_rn(1.0f, y.hi), y.lo);
+  const float c = __fmul_rn(__fmul_rn(r0, e), __fmaf_rn(0.375f, e, 0.5f));
+  return fast_two_sum(r0, c);
+}
+// 1 / x, x != 0: with x r0 = 1 - e (r0 = 1/x_hi rounded, |e| <= 2^-24 plus
+// x_lo's share), 1/x = r0 (1 + e + e^2 + O(e^3))
+__device__ __forceinline__ df rcp_dw(df x) {
+  const float r0 = __frcp_rn(x.hi);
+  const df p = two_prod(x.hi, r0);
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p.hi), p.lo), __fmul_rn(x.lo, r0));
+  return fast_two_sum(r0, __fmul_rn(__fmul_rn(r0, e), __fadd_rn(1.0f, e)));
+}
+
 }  // namespace tmg

@@ -423,7 +423,8 @@ static std::vector<unsigned char> eval_key(tm_energy* e, tm_mesh* m, const doubl
   // (the launch stream is not part of the key: a graph replays on any stream)
   const void* ptrs[] = {P, d_grad, e->face.get(), e->edge.get(), e->ebond.get(), e->fav.get(), e->rho.get(),
                         e->repg.get(), e->reppot.get(), e->slow.get(), e->pos32.get(), e->poslo.get(), e->partials.get(),
-                        e->glob.get(), e->sct.get(), e->aux, e->ev_fork, e->ev_join, e->nl.xb.get()};
+                        e->glob.get(), e->sct.get(), e->aux, e->ev_fork, e->ev_join, e->nl.xb.get(),
+                        e->posdw.get(), e->sctf.get()};
   add(ptrs, sizeof ptrs);
   const Topo t = m->topo();
   const int sizes[] = {t.nv, t.ne, t.nf, want_grad ? 1 : 0, e->stencil, e->nl.near_nv};
@@ -634,17 +635,33 @@ int tm_energy_create(tm_mesh* m, const tm_params* p, tm_energy** out) {
   TM_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
   {
     std::vector<double2> sc(tmg::TM_SCT_N);
-    for (int k = 0; k < tmg::TM_SCT_N; ++k) sc[k] = make_double2(std::sin(k / 128.0), std::cos(k / 128.0));
+    std::vector<float4> scf(tmg::TM_SCT_N);
+    auto split = [](double x, float* h, float* l) {
+      *h = (float)x;
+      *l = (float)(x - (double)*h);
+    };
+    for (int k = 0; k < tmg::TM_SCT_N; ++k) {
+      sc[k] = make_double2(std::sin(k / 128.0), std::cos(k / 128.0));
+      split(sc[k].x, &scf[k].x, &scf[k].y);
+      split(sc[k].y, &scf[k].z, &scf[k].w);
+    }
     e->sct.ensure(tmg::TM_SCT_N);
+    e->sctf.ensure(tmg::TM_SCT_N);
     TM_CUDA(cudaMemcpyAsync(e->sct.get(), sc.data(), sizeof(double2) * tmg::TM_SCT_N, cudaMemcpyHostToDevice,
+                            e->stream));
+    TM_CUDA(cudaMemcpyAsync(e->sctf.get(), scf.data(), sizeof(float4) * tmg::TM_SCT_N, cudaMemcpyHostToDevice,
                             e->stream));
     TM_CUDA(cudaStreamSynchronize(e->stream));
   }
   m->upload_points(e->stream);
   tmg::nlist_make(&e->nl, m, e->prm, m->d_pts.get(), e->stream);
   // initial properties: the reference properties are still unset (zero) and
-  // only the sums matter here
+  // only the sums matter here; taken with the FP64 stencil whatever the
+  // handle's stencil precision
+  const int stencil = e->stencil;
+  e->stencil = 0;
   tmg::energy_eval(e.get(), m, m->d_pts.get(), false, false, nullptr, e->stream);
+  e->stencil = stencil;
   tmg::Globals g;
   fetch_globals(e.get(), &g);
   for (int k = 0; k < 6; ++k) e->initial[k] = g.props[k];

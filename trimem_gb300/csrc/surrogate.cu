@@ -221,10 +221,16 @@ __global__ void __launch_bounds__(256) k_agg(Topo t, const EdgeF* __restrict__ e
 // h_out = h + SiLU([h | m] W^T + b) for 128 vertices per CTA on the tensor cores
 constexpr int DENSE_SMEM = 1024 + 49152 + 64;
 
+// Every wait is bounded: wait_polls polls for the tile loads and for the MMA
+// completion.  When a wait gives up the CTA records it in *status (1 loads,
+// 2 MMA), skips the work that depended on it, waits (with the long default
+// limit) for the copies and the MMA it did issue to land, and frees its
+// tensor memory before it returns.
+constexpr int WAIT_POLLS = 1 << 22;
 __global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorMap mh,
                                                const __grid_constant__ CUtensorMap mm,
                                                const __grid_constant__ CUtensorMap mw, const float* __restrict__ bias,
-                                               __nv_bfloat16* __restrict__ out, int M, int* status) {
+                                               __nv_bfloat16* __restrict__ out, int M, int* status, int wait_polls) {
   using namespace tmg::tc;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -234,6 +240,7 @@ __global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorM
   uint8_t* B1 = base + 40960;   // W[:, 64:128]
   uint64_t* bars = reinterpret_cast<uint64_t*>(base + 49152);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(base + 49152 + 16);
+  int* issued = reinterpret_cast<int*>(base + 49152 + 20);  // the MMA was issued
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM;
   if (threadIdx.x == 0) {
@@ -243,6 +250,7 @@ __global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorM
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     mbar_fence_init();
+    *issued = 0;
   }
   if (warp == 0) {
     tmem_alloc(tslot, 64);
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorM
     tma_load_2d(A1, &mm, &bars[0], 0, m0);
     tma_load_2d(B0, &mw, &bars[0], 0, 0);
     tma_load_2d(B1, &mw, &bars[0], 64, 0);
-    if (mbar_wait(&bars[0], 0)) {
+    if (mbar_wait(&bars[0], 0, wait_polls)) {
       tc_fence_after();
       constexpr uint32_t idesc = idesc_bf16_f32(BM, H);
 #pragma unroll
@@ -269,12 +277,15 @@ __global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorM
           mma_bf16(tmem, sdesc_sw128(a + 32 * k, 1024), sdesc_sw128(b + 32 * k, 1024), idesc, (kc | k) != 0);
       }
       mma_commit(&bars[1]);
+      *issued = 1;
     } else {
-      atomicExch(status, 1);  // tile loads did not arrive
+      atomicExch(status, 1);  // tile loads did not arrive in time
+      // the copies are still this CTA's: let them land before it exits
+      if (!mbar_wait(&bars[0], 0, WAIT_POLLS)) atomicExch(status, 3);
     }
   }
-  __syncwarp();
-  bool done = __all_sync(0xffffffffu, mbar_wait(&bars[1], 0));
+  __syncthreads();
+  bool done = __all_sync(0xffffffffu, mbar_wait(&bars[1], 0, wait_polls));
   tc_fence_after();
   if (done) {
     const int r = warp * 32 + lane;
@@ -299,8 +310,11 @@ __global__ void __launch_bounds__(128) k_dense(const __grid_constant__ CUtensorM
         *reinterpret_cast<uint4*>(out + (size_t)(m0 + r) * H + c * 8) = ov;
       }
     }
-  } else if (lane == 0) {
-    atomicExch(status, 2);  // the MMA completion did not arrive
+  } else {
+    if (lane == 0) atomicExch(status, 2);  // the MMA completion did not arrive in time
+    // an MMA that was issued still writes the accumulator: wait for it
+    // before the tensor memory is freed
+    if (threadIdx.x == 0 && *issued && !mbar_wait(&bars[1], 0, WAIT_POLLS)) atomicExch(status, 3);
   }
   tc_fence_before();
   __syncthreads();
@@ -407,13 +421,13 @@ void make_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t cols, u
 }
 
 void dense_launch(const CUtensorMap& mh, const CUtensorMap& mm, const CUtensorMap& mw, const float* bias,
-                  __nv_bfloat16* out, int M, int* status, cudaStream_t s) {
+                  __nv_bfloat16* out, int M, int* status, cudaStream_t s, int wait_polls = WAIT_POLLS) {
   static bool attr = false;
   if (!attr) {
     TM_CUDA(cudaFuncSetAttribute(k_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, DENSE_SMEM));
     attr = true;
   }
-  if (M > 0) k_dense<<<nblk(M, BM), BM, DENSE_SMEM, s>>>(mh, mm, mw, bias, out, M, status);
+  if (M > 0) k_dense<<<nblk(M, BM), BM, DENSE_SMEM, s>>>(mh, mm, mw, bias, out, M, status, wait_polls);
   TM_LAUNCH();
 }
 
@@ -561,7 +575,13 @@ int tm_surrogate_inputs_device(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const
 
 int tm_dense_silu_bf16(const void* d_h, const void* d_m, const void* d_w, const float* d_bias, void* d_out,
                        int64_t rows, void* stream) {
+  return tm_dense_silu_bf16_bounded(d_h, d_m, d_w, d_bias, d_out, rows, WAIT_POLLS, stream);
+}
+
+int tm_dense_silu_bf16_bounded(const void* d_h, const void* d_m, const void* d_w, const float* d_bias, void* d_out,
+                               int64_t rows, int wait_polls, void* stream) {
   TM_API_BEGIN
+  if (wait_polls < 0) fail(TM_ERR_ARG, "wait_polls must be >= 0");
   if (!d_h || !d_m || !d_w || !d_bias || !d_out) fail(TM_ERR_ARG, "NULL argument");
   if (rows < 0 || rows > (1LL << 30)) fail(TM_ERR_ARG, "rows out of range");
   cudaStream_t s = (cudaStream_t)stream;
@@ -573,7 +593,7 @@ int tm_dense_silu_bf16(const void* d_h, const void* d_m, const void* d_w, const 
   DevBuf<int> st;
   st.ensure(1);
   TM_CUDA(cudaMemsetAsync(st.get(), 0, sizeof(int), s));
-  dense_launch(mh, mm, mw, d_bias, static_cast<__nv_bfloat16*>(d_out), (int)rows, st.get(), s);
+  dense_launch(mh, mm, mw, d_bias, static_cast<__nv_bfloat16*>(d_out), (int)rows, st.get(), s, wait_polls);
   int hs = 0;
   TM_CUDA(cudaMemcpyAsync(&hs, st.get(), sizeof(int), cudaMemcpyDeviceToHost, s));
   TM_CUDA(cudaStreamSynchronize(s));

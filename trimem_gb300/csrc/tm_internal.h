@@ -204,14 +204,16 @@ struct Globals {
 struct tm_energy {
   tm_params prm{};
   double initial[6] = {0, 0, 0, 0, 0, 0};
-  int stencil = 0;  // 0 FP64, 1 FP32
+  int stencil = 2;  // 0 FP64, 1 FP32, 2 double-word (FP64-accurate, FP32 pipe; the default)
   tm_nlist nl;
   int nv = 0, ne = 0, nf = 0;
   tmg::DevBuf<double> face, edge, ebond, fav, rho, repg, reppot, vprops, partials, grad, work;
   tmg::DevBuf<int> slow;  // vertices that left their build cell (+ count)
   tmg::DevBuf<float> pos32, poslo;
+  tmg::DevBuf<float4> posdw;  // double-word stencils: hi parts [nv], lo parts [nv]
   tmg::DevBuf<tmg::Globals> glob;
   tmg::DevBuf<double2> sct;  // {sin, cos}(k / 128), k < TM_SCT_N
+  tmg::DevBuf<float4> sctf;  // the same as double-words (sin hi, sin lo, cos hi, cos lo)
   // flip-sweep workspace, kept between sweeps (grown on demand)
   tmg::DevBuf<int> fw_owner, fw_limit, fw_accl;
   tmg::DevBuf<long long> fw_win, fw_pend;
