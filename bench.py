@@ -544,21 +544,28 @@ def run_profile(args):
         print("profile surrogate evaluations done:", args.profile_surrogate)
         return
     if args.profile_flips:
-        # the chains' state: relaxed membrane, initial area / volume targets
-        from trimem_gb300.mc.device import relaxed_state
-
+        # sweeps of ratio 0.2 (98,304 proposals, windows of 4,096) on the
+        # benchmark membrane as constructed (area and volume targets at that
+        # state); each sweep timed with CUDA events on its stream
         prm0 = dict(prm, cont_lambda=0.0)
-        x0, _ = relaxed_state(p, f, prm0)
-        mesh = capi.Mesh(x0, f)
+        mesh = capi.Mesh(p, f)
         en = capi.Energy(mesh, capi.params(**prm0))
-        x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
-        capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), None))
+        side = torch.cuda.Stream()
+        sp = ctypes.c_void_p(side.cuda_stream)
+        capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), sp))
+        ms, accs = [], []
         for k in range(args.profile_flips):
             acc = ctypes.c_int32()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(side)
             capi.check(L.tm_flip_device(mesh.h, en.h, ctypes.c_void_p(x.data_ptr()), 0.2, 7 + k, 1, 4096,
-                                        ctypes.byref(acc), None))
-        torch.cuda.synchronize()
-        print("profile flip sweeps done:", args.profile_flips)
+                                        ctypes.byref(acc), sp))
+            b.record(side)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+            accs.append(acc.value)
+        print("profile flip sweeps done:", args.profile_flips, "ms per sweep:", [round(v, 3) for v in ms],
+              "accepted:", accs)
         return
     for _ in range(args.profile_evals):
         x.add_(torch.randn(x.shape, dtype=torch.float64, device="cuda", generator=gen), alpha=1e-4)

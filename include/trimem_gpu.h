@@ -253,6 +253,41 @@ int tm_dense_silu_bf16(const void* d_h, const void* d_m, const void* d_w, const 
 int tm_dense_silu_bf16_bounded(const void* d_h, const void* d_m, const void* d_w, const float* d_bias, void* d_out,
                                int64_t rows, int wait_polls, void* stream);
 
+/* ---- training of the surrogate on the GPU (no counterpart in the
+ * reference) ----------------------------------------------------------------
+ * Hand-written forward and backward kernels of the network and Adam:
+ * activations and dense weights bf16 (the dense layer on the tensor cores,
+ * as in inference), FP32 accumulation and FP32 master parameters.  The
+ * inputs are the device arrays tm_surrogate_inputs_device exports for one
+ * state (u n x 8, normals n x 4, ring neighbours [D][n] int32 with -1
+ * padding, edge features [D][n][4] 16-byte aligned, unit edge directions
+ * [D][n][3]) and the target force n x 3 (float).  The loss is
+ * mean((F - T)^2) / target_rms^2 over the 3 n force components.  Parameter
+ * gradients are reduced in a fixed order: a step is bit-reproducible.
+ * A training state serves meshes of n_vertices and up to max_valence ring
+ * slots; weights use the blob layout of tm_surrogate_create. */
+typedef struct tm_strain tm_strain;
+int tm_surrogate_train_create(int64_t n_vertices, int32_t max_valence, const float* weights, int64_t n_weights,
+                              tm_strain** out);
+int tm_surrogate_train_destroy(tm_strain* t);
+/* current weights (host blob of n_weights floats) */
+int tm_surrogate_train_get_weights(tm_strain* t, float* weights, int64_t n_weights);
+/* forward pass (force into d_force and loss into d_loss, each may be NULL)
+ * and, when d_grad is not NULL, the loss gradient wrt the parameters in
+ * blob order without the 8-float header; synchronises */
+int tm_surrogate_train_grad(tm_strain* t, const float* d_u, const float* d_nrm, const int32_t* d_nbr,
+                            const float* d_ef, const float* d_dirs, const float* d_target, int64_t n_vertices,
+                            int32_t max_valence, float target_rms, float* d_force, float* d_loss, float* d_grad,
+                            void* stream);
+/* one Adam step (Kingma & Ba, with bias correction) on one state; the
+ * loss before the step goes to d_loss (may be NULL); does not synchronise */
+int tm_surrogate_train_step(tm_strain* t, const float* d_u, const float* d_nrm, const int32_t* d_nbr,
+                            const float* d_ef, const float* d_dirs, const float* d_target, int64_t n_vertices,
+                            int32_t max_valence, float target_rms, float lr, float beta1, float beta2, float eps,
+                            float* d_loss, void* stream);
+/* synchronises; TM_ERR_TIMEOUT if a tensor-core wait of a past step gave up */
+int tm_surrogate_train_status(tm_strain* t);
+
 /* ---- batches of replicas (no counterpart in the reference: the reference
  * runs one membrane per process) -------------------------------------------
  * n_rep independent meshes with their own parameters evaluated and sampled

@@ -1,7 +1,6 @@
 """Host side of the learned surrogate (no GPU): the weight blob that
-tm_surrogate_create parses round-trips, and the sparse-product form used for
-training computes the same function as the gather form the CUDA kernels
-restate."""
+tm_surrogate_create parses round-trips, and the torch reference network's
+bf16 emulation stays close to its FP32 form."""
 import numpy as np
 import pytest
 
@@ -45,16 +44,6 @@ def _random_inputs(nv=300, d=6, seed=1):
     inp.ef = torch.randn(d, nv, S.FE, generator=g) * valid
     inp.dirs = torch.randn(d, nv, 3, generator=g) * valid
     return inp
-
-
-def test_sparse_training_form_equals_gather_form():
-    net = _net(2)
-    inp = _random_inputs()
-    with torch.no_grad():
-        f_gather = net(inp.u, inp.nrm, inp.nbr, inp.ef, inp.dirs)
-        f_sparse = net.forward_sparse(S.SparseInputs(inp))
-    rel = float((f_gather - f_sparse).norm() / f_gather.norm())
-    assert rel < 1e-5, rel
 
 
 def test_bf16_emulation_stays_close():

@@ -26,6 +26,7 @@ _d = ctypes.c_double
 _p = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
+_f32 = ctypes.c_float
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
 _i64p = ctypes.POINTER(ctypes.c_int64)
@@ -122,6 +123,13 @@ _SIGS = {
                                             _dp, _dp, _p]),
     "tm_dense_silu_bf16": (_i32, [_p, _p, _p, _p, _p, _i64, _p]),
     "tm_dense_silu_bf16_bounded": (_i32, [_p, _p, _p, _p, _p, _i64, _i32, _p]),
+    "tm_surrogate_train_create": (_i32, [_i64, _i32, _p, _i64, _p]),
+    "tm_surrogate_train_destroy": (_i32, [_p]),
+    "tm_surrogate_train_get_weights": (_i32, [_p, _p, _i64]),
+    "tm_surrogate_train_grad": (_i32, [_p, _p, _p, _p, _p, _p, _p, _i64, _i32, _f32, _p, _p, _p, _p]),
+    "tm_surrogate_train_step": (_i32, [_p, _p, _p, _p, _p, _p, _p, _i64, _i32, _f32, _f32, _f32, _f32, _f32, _p,
+                                       _p]),
+    "tm_surrogate_train_status": (_i32, [_p]),
 }
 
 _lib = None

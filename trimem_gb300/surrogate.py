@@ -1,6 +1,6 @@
-"""Learned surrogate force: the network in torch (training, and the FP32
-reference of the CUDA forward), the weight blob of tm_surrogate_create, and
-the training driver.
+"""Learned surrogate force: the weight blob of tm_surrogate_create, the
+training data (states of plain device HMC chains) and the training driver
+over the library's own training kernels (tm_surrogate_train_*).
 
 The CUDA side (csrc/surrogate.cu) evaluates, per vertex i with ring j,
 
@@ -13,7 +13,11 @@ The CUDA side (csrc/surrogate.cu) evaluates, per vertex i with ring j,
 with d_ij the unit edge direction and N_i the vertex normal; the leapfrog
 gradient is g_local - F, g_local the exact gradient of the local penalty
 terms.  The network is trained on F_target = g_local - g_exact from states
-of a device chain (MSE on forces, Adam).
+of device chains at the reduced volumes of the learned-surrogate
+configuration (MSE on forces, Adam), by hand-written forward and backward
+kernels on the GPU; the training set stays resident in device memory.
+``make_net`` is the same network in torch, the floating-point reference the
+tests check those kernels against.
 
 Run ``python -m trimem_gb300.surrogate --out weights.npy`` on a GPU to train
 the weights for the 163,842-vertex benchmark membrane.
@@ -64,7 +68,7 @@ def make_net():
             F_ = torch.nn.functional
             rnd = (lambda t: t.to(torch.bfloat16).float()) if bf16 else (lambda t: t)
             mask = (nbr >= 0).to(u.dtype)
-            idx = nbr.clamp(min=0)
+            idx = nbr.clamp(min=0).long()
             h = rnd(F_.silu(self.win(u)))
             for r in range(NR):
                 g = self.we[r](ef)
@@ -77,47 +81,7 @@ def make_net():
             F = (c[..., None] * dirs).sum(0) + cn[:, None] * nrm[:, :3]
             return self.scales[2] * F
 
-        def forward_sparse(self, sp):
-            """The same function with the ring sums as sparse products
-            (training): m = sum_k W_e[:, k] * (E_k h) + b_e * (A h), with
-            E_k / A the adjacency weighted by edge feature k / by one, and
-            sum_j c_ij d_ij = ((w_o * h) . (D h)) + b_o D 1 per component."""
-            F_ = torch.nn.functional
-            h = F_.silu(self.win(sp.u))
-            for r in range(NR):
-                Y = [torch.sparse.mm(a, h) for a in sp.E]
-                m = sum(self.we[r].weight[:, k] * Y[k] for k in range(FE)) + self.we[r].bias * Y[FE]
-                h = h + F_.silu(torch.cat([h, m], 1) @ self.dense[r].weight.t() + self.dense[r].bias)
-            hw = h * self.wo
-            F = torch.stack([(hw * torch.sparse.mm(d, h)).sum(1) for d in sp.D], 1) + self.bo * sp.dsum
-            F = F + (h @ self.wn + self.bn)[:, None] * sp.nrm[:, :3]
-            return self.scales[2] * F
-
     return SurrogateNet()
-
-
-class SparseInputs:
-    """Inputs as sparse adjacency matrices (COO, shared pattern): E_0..E_3
-    weighted by the edge features, E_4 by one, D_x, D_y, D_z by the unit
-    edge directions."""
-
-    def __init__(self, inp):
-        torch = _torch()
-        D, nv = inp.nbr.shape
-        sel = inp.nbr >= 0
-        rows = torch.arange(nv, device=inp.nbr.device).expand(D, nv)[sel]
-        cols = inp.nbr[sel]
-        ind = torch.stack([rows, cols])
-
-        def mat(v):
-            return torch.sparse_coo_tensor(ind, v, (nv, nv), check_invariants=False).coalesce()
-
-        self.E = [mat(inp.ef[..., k][sel]) for k in range(FE)] + [mat(torch.ones_like(inp.ef[..., 0][sel]))]
-        self.D = [mat(inp.dirs[..., k][sel]) for k in range(3)]
-        self.dsum = (inp.dirs * sel[..., None]).sum(0)
-        self.u = inp.u
-        self.nrm = inp.nrm
-        self.target = getattr(inp, "target", None)
 
 
 def to_blob(net):
@@ -183,7 +147,8 @@ def mesh_scales(p, f):
 
 
 class Inputs:
-    """Device tensors of one state: network inputs and the exact gradients."""
+    """Device tensors of one state: network inputs, and the exact local and
+    total gradients' difference as the target (float32)."""
 
     def __init__(self, sg, energy, mesh, x, max_valence, stream=0):
         torch = _torch()
@@ -194,110 +159,188 @@ class Inputs:
         self.u = torch.empty(nv, FV, device=dev)
         self.nrm = torch.empty(nv, 4, device=dev)
         nbr = torch.empty(max_valence, nv, dtype=torch.int32, device=dev)
-        self.ef = torch.empty(max_valence, nv, FE, device=dev)
-        self.dirs = torch.empty(max_valence, nv, 3, device=dev)
+        ef = torch.empty(max_valence, nv, FE, device=dev)
+        dirs = torch.empty(max_valence, nv, 3, device=dev)
         self.gloc = torch.empty(nv, 3, dtype=torch.float64, device=dev)
         P = lambda t: ctypes.c_void_p(t.data_ptr())
         capi.check(capi.lib().tm_surrogate_inputs_device(sg.h, energy.h, mesh.h, P(x), max_valence, P(self.u),
-                                                         P(self.nrm), P(nbr), P(self.ef), P(self.dirs), P(self.gloc),
+                                                         P(self.nrm), P(nbr), P(ef), P(dirs), P(self.gloc),
                                                          ctypes.c_void_p(stream)))
         d = int((nbr >= 0).any(dim=1).sum())  # rows past the largest valence hold no neighbour
-        self.nbr = nbr[:d].long()
-        self.ef = self.ef[:d].contiguous()
-        self.dirs = self.dirs[:d].contiguous()
+        self.nbr = nbr[:d].contiguous()
+        self.ef = ef[:d].contiguous()
+        self.dirs = dirs[:d].contiguous()
+
+    @property
+    def D(self):
+        return self.nbr.shape[0]
 
 
-def generate(n_snap, every=2, burn=10, level=7, seed=5, max_valence=16, log=print):
-    """States of the benchmark chain (the 163,842-vertex membrane relaxed by
-    L-BFGS, initial area / volume targets; HMC with 20 velocity-Verlet steps
-    at the tuned time step + a flip sweep of ratio 0.2 per step) with the
-    network inputs and the training target g_local - g_exact."""
+class DeviceTrainer:
+    """The training kernels (tm_surrogate_train_*) for meshes of nv
+    vertices and up to max_valence ring slots, started from a weight blob."""
+
+    def __init__(self, nv, max_valence, blob):
+        from . import capi
+
+        self.capi = capi
+        self.L = capi.lib()
+        self.nv = int(nv)
+        self.blob = np.ascontiguousarray(blob, dtype=np.float32)
+        h = ctypes.c_void_p()
+        capi.check(self.L.tm_surrogate_train_create(self.nv, int(max_valence), self.blob.ctypes.data_as(ctypes.c_void_p),
+                                                    self.blob.size, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.tm_surrogate_train_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _args(self, d):
+        P = lambda t: ctypes.c_void_p(t.data_ptr())
+        return [P(d.u), P(d.nrm), P(d.nbr), P(d.ef), P(d.dirs), P(d.target), self.nv, d.D]
+
+    def grad(self, d, target_rms, want_grad=True, stream=0):
+        """(loss, force, gradient) of one state; gradient in blob order
+        without the header (None unless want_grad)."""
+        torch = _torch()
+        dev = d.u.device
+        F = torch.empty(self.nv, 3, device=dev)
+        loss = torch.empty(1, device=dev)
+        g = torch.empty(BLOB_SIZE - BLOB_HEADER, device=dev) if want_grad else None
+        P = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+        self.capi.check(self.L.tm_surrogate_train_grad(self.h, *self._args(d), float(target_rms), P(F), P(loss), P(g),
+                                                       ctypes.c_void_p(stream)))
+        return float(loss.item()), F, g
+
+    def step(self, d, target_rms, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8, loss_out=None, stream=0):
+        """One Adam step on state d (asynchronous); the loss before the step
+        goes to loss_out (a one-element device tensor) when given."""
+        P = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+        self.capi.check(self.L.tm_surrogate_train_step(self.h, *self._args(d), float(target_rms), float(lr),
+                                                       float(beta1), float(beta2), float(eps), P(loss_out),
+                                                       ctypes.c_void_p(stream)))
+
+    def weights(self):
+        b = np.empty(BLOB_SIZE, np.float32)
+        self.capi.check(self.L.tm_surrogate_train_get_weights(self.h, b.ctypes.data_as(ctypes.c_void_p), b.size))
+        return b
+
+
+VOLUMES = (0.65, 0.75, 0.85)
+
+
+def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, max_valence=16, log=print):
+    """Training states: for each reduced volume, the 163,842-vertex membrane
+    (level-7 icosphere, kb 20, the other parameters of the benchmark)
+    relaxed towards that volume by the device L-BFGS, then a plain device
+    HMC chain (20 velocity-Verlet steps at the tuned time step + a flip sweep
+    of ratio 0.2 per step) whose every `every`-th state gives one snapshot:
+    the network inputs and the target g_local - g_exact.  Everything stays
+    in device memory.  Returns (snapshots, (lbar, abar), per-volume info)."""
     torch = _torch()
     from . import capi, meshgen
     from .mc.device import DeviceChain, relaxed_state, tune_dt
     from .workloads import workload_params
 
     p, f = meshgen.jittered_icosphere(level, seed=0)
-    prm = dict(workload_params(p, f, kappa_b=20.0, vfrac=0.65), cont_lambda=0.0)
-    x0, info = relaxed_state(p, f, prm)
-    log(f"relaxed start: {info}")
-    mesh = capi.Mesh(x0, f)
-    en = capi.Energy(mesh, capi.params(**prm))
-    lbar, abar = mesh_scales(x0, f)
-    net = make_net()
-    with torch.no_grad():
-        net.scales.copy_(torch.tensor([lbar, abar, 1.0]))
-    sg = capi.Surrogate(mesh, to_blob(net))
-    x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
-    dt, pilot = tune_dt(mesh, en, x)
-    log(f"time step {dt} (pilot acceptance {pilot})")
-    ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=seed)
-    ch.run(burn)
+    data, info = [], []
+    scales = None
+    g = None
     L = capi.lib()
-    data = []
-    g = torch.empty_like(x)
-    for k in range(n_snap):
-        ch.run(every)
-        inp = Inputs(sg, en, mesh, x, max_valence)
-        capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(g.data_ptr()),
-                                           None, None))
-        torch.cuda.synchronize()
-        inp.target = (inp.gloc - g).float()
-        del inp.gloc
-        data.append(inp)
-        if log and (k + 1) % 10 == 0:
-            log(f"snapshot {k + 1}/{n_snap}, acceptance so far {ch.accepted / ch.step_index:.2f}")
-    return data, (lbar, abar), dict(prm, dt=dt)
+    for vi, v in enumerate(volumes):
+        prm = workload_params(p, f, kappa_b=20.0, vfrac=v)
+        t0 = time.perf_counter()
+        x0, rinfo = relaxed_state(p, f, prm)
+        mesh = capi.Mesh(x0, f)
+        en = capi.Energy(mesh, capi.params(**prm))
+        if scales is None:
+            scales = mesh_scales(x0, f)
+            net = make_net()
+            with torch.no_grad():
+                net.scales.copy_(torch.tensor([scales[0], scales[1], 1.0]))
+            sg = capi.Surrogate(mesh, to_blob(net))
+        else:
+            sg = capi.Surrogate(mesh, to_blob(net))
+        x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
+        dt, pilot = tune_dt(mesh, en, x)
+        ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=seed + vi)
+        ch.run(burn)
+        if g is None:
+            g = torch.empty_like(x)
+        for k in range(n_per_volume):
+            ch.run(every)
+            inp = Inputs(sg, en, mesh, x, max_valence)
+            capi.check(L.tm_energy_eval_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()),
+                                               ctypes.c_void_p(g.data_ptr()), None, None))
+            torch.cuda.synchronize()
+            inp.target = (inp.gloc - g).float().contiguous()
+            del inp.gloc
+            data.append(inp)
+        info.append({"volume_frac": v, "relax": rinfo, "dt": dt, "pilot": pilot, "steps": ch.step_index,
+                     "acceptance": round(ch.accepted / max(ch.step_index, 1), 3),
+                     "seconds": round(time.perf_counter() - t0, 2)})
+        if log:
+            log(f"volume {v}: {n_per_volume} snapshots, dt {dt}, acceptance {info[-1]['acceptance']}, "
+                f"{info[-1]['seconds']} s")
+    return data, scales, info
 
 
-def train(data, scales, iters=1500, lr=2e-3, seed=0, log=print, budget_s=420.0):
+def train(data, scales, epochs=20, lr=1e-3, seed=0, log=print, n_val=None):
+    """Adam at a constant learning rate over the snapshots (shuffled per
+    epoch), on the GPU with the library's training kernels.  Returns
+    (weights blob, validation relative MSE with the bf16 forward, target
+    rms, seconds, steps)."""
     torch = _torch()
-    torch.manual_seed(seed)
+    rng = np.random.default_rng(seed)
     lbar, abar = scales
     tgt_rms = float(torch.sqrt(torch.stack([(d.target ** 2).mean() for d in data]).mean()))
-    net = make_net().cuda()
+    torch.manual_seed(seed)
+    net = make_net()
     with torch.no_grad():
         net.scales.copy_(torch.tensor([lbar, abar, tgt_rms]))
-    opt = torch.optim.Adam(net.parameters(), lr=lr)
-    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, iters)
-    n_val = max(1, len(data) // 8)
-    train_set, val_set = data[:-n_val], data[-n_val:]
-    sparse = [SparseInputs(d) for d in train_set]
-    t0 = time.time()
-    for it in range(iters):
-        if time.time() - t0 > budget_s:
-            log(f"time budget reached after {it} iterations")
-            break
-        d = sparse[it % len(sparse)]
-        F = net.forward_sparse(d)
-        loss = ((F - d.target) ** 2).mean() / tgt_rms ** 2
-        opt.zero_grad()
-        loss.backward()
-        opt.step()
-        sched.step()
-        if log and (it % 250 == 0 or it == iters - 1):
-            log(f"iter {it} loss {loss.item():.4f} ({time.time() - t0:.0f} s)")
-    with torch.no_grad():
-        errs = []
-        for d in val_set:
-            F = net(d.u, d.nrm, d.nbr, d.ef, d.dirs, bf16=True)
-            errs.append(float(((F - d.target) ** 2).mean() / (d.target ** 2).mean()))
-    return net, float(np.mean(errs)), tgt_rms
+    n_val = n_val if n_val is not None else max(1, len(data) // 10)
+    val_idx = set(range(len(data))[::max(1, len(data) // n_val)][:n_val])
+    train_set = [d for k, d in enumerate(data) if k not in val_idx]
+    val_set = [d for k, d in enumerate(data) if k in val_idx]
+    D = max(d.D for d in data)
+    tr = DeviceTrainer(data[0].u.shape[0], D, to_blob(net))
+    loss = torch.zeros(1, device=data[0].u.device)
+    t0 = time.perf_counter()
+    steps = 0
+    for ep in range(epochs):
+        for k in rng.permutation(len(train_set)):
+            tr.step(train_set[k], tgt_rms, lr=lr, loss_out=loss)
+            steps += 1
+        if log:
+            torch.cuda.synchronize()
+            log(f"epoch {ep + 1}/{epochs}: last loss {float(loss.item()):.4f} ({time.perf_counter() - t0:.1f} s)")
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    val = [tr.grad(d, tgt_rms, want_grad=False)[0] for d in val_set]
+    return tr.weights(), float(np.mean(val)), tgt_rms, secs, steps
 
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--snapshots", type=int, default=48)
-    ap.add_argument("--iters", type=int, default=2000)
+    ap.add_argument("--per-volume", type=int, default=200, help="snapshots per reduced volume")
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default=WEIGHTS_L7)
-    ap.add_argument("--budget", type=float, default=420.0, help="training time limit in seconds")
     args = ap.parse_args()
     log = lambda *a: print(*a, flush=True)
-    data, scales, _ = generate(args.snapshots, log=log)
-    net, val, rms = train(data, scales, iters=args.iters, log=log, budget_s=args.budget)
-    b = to_blob(net.cpu())
-    np.save(args.out, b)
-    print(f"validation relative MSE (bf16 forward) {val:.4f}, target rms {rms:.4g}, weights -> {args.out}")
+    data, scales, info = generate(args.per_volume, log=log)
+    blob, val, rms, secs, steps = train(data, scales, epochs=args.epochs, lr=args.lr, log=log)
+    np.save(args.out, blob)
+    print(f"{steps} Adam steps in {secs:.1f} s ({1e3 * secs / max(steps, 1):.2f} ms each); validation relative MSE "
+          f"{val:.4f}, target rms {rms:.4g}, weights -> {args.out}")
 
 
 if __name__ == "__main__":
