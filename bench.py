@@ -209,6 +209,8 @@ def cpu_chain_step(state, n_steps=2, n_leapfrog=20, dt=5e-6, ratio=0.2):
     O.set_threads(os.cpu_count() or 1)
     mo = O.Mesh(state["x"], state["faces"])
     eo = O.Energy(mo, O.default_params(**state["prm"]))
+    if state.get("initial") is not None:  # the chain's reference properties
+        eo.set_initial_props(state["initial"])
     x = mo.points()  # a view of the oracle mesh's positions
     rng = np.random.default_rng(3)
     t_hmc = t_flip = 0.0
@@ -385,16 +387,14 @@ def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_step
 
 
 def chain_start():
-    """The chains' workload: the 163,842-vertex membrane with area and volume
-    targets at the initial state (continuation lambda 0, so the chain samples
-    around its start instead of collapsing towards the 0.65 reduced volume,
-    which an ESS needs), relaxed to a local energy minimum by the device
-    L-BFGS (the jittered input is far from equilibrium: its short edges give
-    forces no time step survives)."""
+    """The chains' workload: the 163,842-vertex membrane with the
+    very-large-mesh energy (reduced-volume target 0.65), relaxed by the
+    device L-BFGS towards that target before sampling (the jittered input is
+    far from equilibrium: its short edges give forces no time step
+    survives).  The learned surrogate's training volumes include this one."""
     from trimem_gb300.mc.device import relaxed_state
 
     p, f, prm = workload()
-    prm = dict(prm, cont_lambda=0.0)
     x0, info = relaxed_state(p, f, prm)
     return x0, f, prm, info
 
@@ -421,18 +421,19 @@ def _chain_handles(state, stencil):
     return mesh, en, x
 
 
-def chain_warm(stream, start, n_warm=300):
-    """The chains' common start: the relaxed membrane heated to T 1 by an
-    FP64 chain of n_warm steps (the same moves as the measured chains, time
-    step tuned at the relaxed state), so that the measured traces start
-    close to equilibrium instead of climbing from the energy minimum."""
+def chain_warm(stream, start, n_warm=1000):
+    """The chains' common start: the relaxed membrane heated at T 1 by a
+    chain of n_warm steps (the same moves as the measured chains, default
+    stencils, time step tuned at the relaxed state), so that the measured
+    traces start closer to equilibrium instead of climbing from the energy
+    minimum."""
     import torch
 
     from trimem_gb300.mc.device import DeviceChain, tune_dt
 
     x0, f, prm, info = start
     state = {"x": x0, "faces": f, "prm": prm}
-    mesh, en, x = _chain_handles(state, 0)
+    mesh, en, x = _chain_handles(state, 2)
     initial = en.initial_props()
     dt, _ = tune_dt(mesh, en, x, candidates=DT_CANDIDATES, stream=stream)
     ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=5, stream=stream)
@@ -447,7 +448,19 @@ def chain_warm(stream, start, n_warm=300):
             "prm": prm, "info": info}
 
 
-def chain_leg(stream, state, stencil, dt=None, n_burn=20, n_steps=500, weights=None):
+def drift_check(trace):
+    """Stationarity of a trace: the difference of its first and last quarter
+    means over their combined standard error (each quarter's standard error
+    of the mean from its own effective sample size).  |z| < 3 passes."""
+    from trimem_gb300.mc.ess import ess
+
+    q = np.array_split(np.asarray(trace, float), 4)
+    se = [float(b.std(ddof=1) / np.sqrt(max(ess(b), 1.0))) for b in (q[0], q[3])]
+    z = float((q[3].mean() - q[0].mean()) / max(np.hypot(*se), 1e-300))
+    return {"z": round(z, 2), "stationary": bool(abs(z) < 3.0)}
+
+
+def chain_leg(stream, state, stencil, dt=None, n_burn=20, n_steps=2000, weights=None):
     """ESS/s of the bending energy of a device chain: per step one HMC move
     (20 velocity-Verlet steps, m 1, T 1) and one flip sweep (ratio 0.2,
     98,304 attempts), neighbour list rebuilt every step.  dt: the largest of
@@ -489,6 +502,7 @@ def chain_leg(stream, state, stencil, dt=None, n_burn=20, n_steps=500, weights=N
             "ess_bending": round(e, 2), "ess_per_s": round(e / (t1 - t0), 3),
             "bending_mean": float(bend.mean()), "bending_sd": float(bend.std()),
             "bending_quarter_means": [round(float(b.mean()), 1) for b in np.array_split(bend, 4)],
+            "drift": drift_check(bend),
             "ess_reduced_volume": round(e_rv, 2), "ess_reduced_volume_per_s": round(e_rv / (t1 - t0), 3),
             "reduced_volume_mean": float(rv.mean())}
 
@@ -893,14 +907,16 @@ def main():
     try:
         warm = chain_warm(stream, chain_start())
         chain["start"] = warm["info"]
-        plain = chain_leg(stream, warm, 0)
-        chain["plain_fp64"] = plain
-        chain["plain_df64"] = chain_leg(stream, warm, 2, dt=plain["dt"])
+        plain = chain_leg(stream, warm, 2)
+        chain["plain_df64"] = plain
+        # the FP64 stencil on the same moves, shorter: its trace follows the
+        # double-word one (the same accept and flip decisions)
+        chain["plain_fp64"] = chain_leg(stream, warm, 0, dt=plain["dt"], n_steps=500)
         from trimem_gb300 import surrogate as S
 
         if os.path.exists(S.WEIGHTS_L7):
             # the surrogate chain tunes its own step on the same rule
-            chain["surrogate"] = chain_leg(stream, warm, 0, weights=np.load(S.WEIGHTS_L7))
+            chain["surrogate"] = chain_leg(stream, warm, 2, weights=np.load(S.WEIGHTS_L7))
         else:
             chain["surrogate"] = {"error": "no trained weights"}
     except Exception as exc:
@@ -912,8 +928,8 @@ def main():
         cb["parity_build"] = cpu_baseline_parity_build()
         if warm is not None:
             try:
-                cc = cpu_chain_step(warm)
-                pl = chain.get("plain_fp64", {})
+                cc = cpu_chain_step(warm, dt=warm["info"]["warm_dt"])
+                pl = chain.get("plain_df64", {})
                 if "ess_bending" in pl:
                     # same moves and the same algorithm: the GPU chain's ESS
                     # per step at the CPU's step rate

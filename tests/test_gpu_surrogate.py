@@ -125,10 +125,11 @@ def test_surrogate_hmc_step_uses_the_exact_hamiltonian(C):
 
 def test_trained_network_lowers_the_force_error(C):
     """What the trained network gains over the leapfrog without it: on a
-    state of the 163,842-vertex benchmark membrane (relaxed by the device
-    L-BFGS, then a few chain steps at T 1), the surrogate gradient
-    g_local - F_nn is far closer to the exact FP64 gradient than g_local
-    alone (the same integrator with no learned force)."""
+    state of the 163,842-vertex benchmark membrane at reduced-volume target
+    0.65 (one of the training volumes; relaxed by the device L-BFGS, then a
+    few chain steps at T 1), the surrogate gradient g_local - F_nn is far
+    closer to the exact gradient than g_local alone (the same integrator
+    with no learned force)."""
     import torch
 
     from trimem_gb300 import surrogate as S
@@ -138,12 +139,12 @@ def test_trained_network_lowers_the_force_error(C):
     if not __import__("os").path.exists(S.WEIGHTS_L7):
         pytest.skip("no trained weights")
     p, f = meshgen.jittered_icosphere(7, seed=0)
-    prm = dict(wp(p, f, kappa_b=20.0, vfrac=0.65), cont_lambda=0.0)
+    prm = wp(p, f, kappa_b=20.0, vfrac=0.65)
     x0, _ = relaxed_state(p, f, prm)
     mesh = C.Mesh(x0, f)
     en = C.Energy(mesh, C.params(**prm))
     x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
-    DeviceChain(mesh, en, x, dt=5e-6, n_leapfrog=20, flip_ratio=0.0, seed=3).run(5)
+    DeviceChain(mesh, en, x, dt=2e-6, n_leapfrog=20, flip_ratio=0.2, seed=3).run(5)
     L = C.lib()
     C.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, _p(x), None))
     g_exact = torch.empty_like(x)

@@ -45,7 +45,6 @@
 #include "tm_internal.h"
 #include "tm_math.cuh"
 #include "tm_topo.cuh"
-#include "tm_dw.cuh"
 
 using namespace tmg;
 
@@ -451,7 +450,7 @@ __device__ bool repulsion_near8(int v, d3 xv, const double* P, const EP& ep, con
 __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, const long long* win,
                                               const unsigned char* winner, const int* limit, const double* P,
                                               EP ep, NLView nl, double* part, unsigned char* okf, double* dpn,
-                                              float* dpf, PosDW X, EPD epd, const float4* __restrict__ sctf) {
+                                              float* dpf, const double2* __restrict__ sct) {
   __shared__ int sr[8][TM_MAXVAL + 1];
   __shared__ unsigned char sf[8][TM_MAXVAL + 1];
   __shared__ int sn[8];
@@ -543,49 +542,39 @@ __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, 
   const int n = sn[sub];
   const d3 xv = ld3(P, v);
   // per ring position m (face (v, r_m, r_m-1), edge (v, r_m)): half edge
-  // length x angle, face area, face volume, bond, in double-words on the
-  // FP32 pipe (positions relative to x_v: the face normal N0 = (x_j - x_v) x
-  // (x_k - x_v), the volume term x_v . N0 / 6 = (x_j x x_k) . x_v / 6).
-  // With n <= 8 every lane holds one position and the normal of the next
-  // face comes from the next lane (the same cross product).
-  const df3 xw = X.at(v);
-  df sc = df_make(0.0f), sa = sc, sv = sc, stt = sc;
-  auto terms = [&](const df3& ev, const df& el, const df& il, const df& n0s, const df& r0, const df3& N0,
-                   bool have1, const df3& N1, const df& n1s, const df& r1) {
-    df th = df_make(0.0f);
-    if (have1 && n0s.hi != 0.0f && n1s.hi != 0.0f) {
+  // length x angle, face area, face volume, bond.  With n <= 8 every lane
+  // holds one position and the normal of the next face comes from the next
+  // lane (the same cross product: (x_r(m+1) - x_v) x (x_r(m) - x_v)).
+  double sc = 0.0, sa = 0.0, sv = 0.0, stt = 0.0;
+  auto terms = [&](d3 xj, d3 xk, d3 ev, double el, double il, double n0s, double r0, const d3& N0, bool have1,
+                   const d3& N1, double n1s, double r1) {
+    double th = 0.0;
+    if (have1 && n0s != 0.0 && n1s != 0.0) {
       // dihedral angle from cosine and signed sine (N0 x N1 lies along the
       // edge; its sign is the reference's test (N0 x N1) . e >= 0)
-      const df inv = mul_s(r0, r1);
-      const df sd = mul_s(dot3(cross3(N0, N1), ev), mul_s(inv, il));
-      th = angle_dw(sd, mul_s(dot3(N0, N1), inv), sctf);
+      double inv = r0 * r1;
+      double sd = dot(cross(N0, N1), ev) * (inv * il);
+      double a = angle_sc(fabs(sd), dot(N0, N1) * inv, sct);
+      th = sd >= 0.0 ? a : -a;
     }
-    const df fa = half(mul_s(n0s, r0));
-    df tt = df_make(0.0f);
+    double fa = 0.5 * (n0s * r0);
+    double tt = 0.0;
     if (ep.btype == 0) {
-      if (ep.r >= 1) {
-        if (df_less(epd.lc0, el))
-          tt = mul_s(epd.br1, ipow_dw(sub_s(el, epd.lc0), ep.r));
-        else if (df_less(el, epd.lc1))
-          tt = mul_s(df_exp_nonpos(mul_s(el, rcp_dw(sub_s(el, epd.lc1)))), ipow_dw(il, ep.r));
-      } else {  // non-positive exponents: FP64
-        const double eld = df_to(el), ild = df_to(il);
-        double t64 = 0.0;
-        if (eld > ep.lc0) t64 = ep.br1 * ipow(eld - ep.lc0, ep.r);
-        else if (eld < ep.lc1) t64 = exp(eld * (1.0 / (eld - ep.lc1))) * ipow(ild, ep.r);
-        tt = df_from(t64);
-      }
+      int r = ep.r;
+      // threshold tests on the length's bits (l >= 0 orders like its bits)
+      if (__double_as_longlong(el) > __double_as_longlong(ep.lc0))
+        tt = ep.br1 * ipow(el - ep.lc0, r);
+      else if (__double_as_longlong(el) < __double_as_longlong(ep.lc1))
+        tt = exp(el * (1.0 / (el - ep.lc1))) * ipow(il, r);
     } else {
-      const df qa = sub_s(mul_s(fa, epd.inv_a0), df_make(1.0f));
-      tt = mul_s(qa, qa);
+      double qa = fa / ep.a0 - 1.0;
+      tt = qa * qa;
     }
-    sc = add_s(sc, half(mul_s(el, th)));
-    sa = add_s(sa, fa);
-    sv = add_s(sv, mul_s(dot3(xw, N0), sixth()));
-    stt = add_s(stt, tt);
+    sc += 0.5 * el * th;
+    sa += fa;
+    sv += dot(cross(xj, xk), xv) * (1.0 / 6.0);
+    stt += tt;
   };
-  const df zero = df_make(0.0f);
-  const df3 zero3 = {zero, zero, zero};
   if (n <= 8) {
     // lanes past the ring and positions without a face compute nothing; the
     // next face's normal is used only where that face exists, and then its
@@ -593,67 +582,68 @@ __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, 
     const int m = w8 < n ? w8 : 0;
     const int mn = m + 1 == n ? 0 : m + 1;
     const bool act = w8 < n && sf[sub][m];
-    df3 ev = zero3, N0 = zero3;
-    df il = zero, el = zero, n0s = zero, r0 = zero;
+    d3 xj = mk(0, 0, 0), xk = xj, ev = xj, N0 = xj;
+    double il = 0.0, el = 0.0, n0s = 0.0, r0 = 0.0;
     if (act) {
-      const df3 xj = X.at(sr[sub][m]), xk = X.at(sr[sub][m == 0 ? n - 1 : m - 1]);
-      ev = sub3(xj, xw);
-      const df l2 = dot3(ev, ev);
-      il = rsqrt_dw(l2);
-      el = mul_s(l2, il);
-      N0 = cross3(ev, sub3(xk, xw));
-      n0s = dot3(N0, N0);
-      r0 = rsqrt_dw(n0s);
+      xj = ld3(P, sr[sub][m]);
+      xk = ld3(P, sr[sub][m == 0 ? n - 1 : m - 1]);
+      ev = xj - xv;
+      double l2 = dot(ev, ev);
+      il = rsqrt(l2);
+      el = l2 * il;
+      N0 = cross(ev, xk - xv);
+      n0s = dot(N0, N0);
+      r0 = rsqrt(n0s);
     }
     const int src = gbase + mn;
-    auto shf = [&](const df& x) {
-      return df{__shfl_sync(gmask, x.hi, src), __shfl_sync(gmask, x.lo, src)};
-    };
-    const df3 N1 = {shf(N0.x), shf(N0.y), shf(N0.z)};
-    const df n1s = shf(n0s), r1 = shf(r0);
-    if (act) terms(ev, el, il, n0s, r0, N0, sf[sub][mn] != 0, N1, n1s, r1);
+    d3 N1;
+    N1.x = __shfl_sync(gmask, N0.x, src);
+    N1.y = __shfl_sync(gmask, N0.y, src);
+    N1.z = __shfl_sync(gmask, N0.z, src);
+    const double n1s = __shfl_sync(gmask, n0s, src);
+    const double r1 = __shfl_sync(gmask, r0, src);
+    if (act) terms(xj, xk, ev, el, il, n0s, r0, N0, sf[sub][mn] != 0, N1, n1s, r1);
   } else {
     for (int m = w8; m < n; m += 8) {
       if (!sf[sub][m]) continue;
-      const int mn = m + 1 == n ? 0 : m + 1;
-      const df3 xj = X.at(sr[sub][m]), xk = X.at(sr[sub][m == 0 ? n - 1 : m - 1]);
-      const df3 ev = sub3(xj, xw);
-      const df l2 = dot3(ev, ev);
-      const df il = rsqrt_dw(l2), el = mul_s(l2, il);
-      const df3 N0 = cross3(ev, sub3(xk, xw));
-      const df n0s = dot3(N0, N0), r0 = rsqrt_dw(n0s);
-      df3 N1 = zero3;
-      df n1s = zero, r1 = zero;
+      int j = sr[sub][m], k = sr[sub][m == 0 ? n - 1 : m - 1];
+      int mn = m + 1 == n ? 0 : m + 1;
+      d3 xj = ld3(P, j), xk = ld3(P, k);
+      d3 ev = xj - xv;
+      double l2 = dot(ev, ev);
+      double il = rsqrt(l2);
+      double el = l2 * il;
+      d3 N0 = cross(ev, xk - xv);
+      double n0s = dot(N0, N0);
+      double r0 = rsqrt(n0s);
+      d3 N1 = mk(0, 0, 0);
+      double n1s = 0.0, r1 = 0.0;
       const bool have1 = sf[sub][mn] != 0;
       if (have1) {
-        N1 = cross3(sub3(X.at(sr[sub][mn]), xw), ev);
-        n1s = dot3(N1, N1);
-        r1 = rsqrt_dw(n1s);
+        N1 = cross(ld3(P, sr[sub][mn]) - xv, ev);
+        n1s = dot(N1, N1);
+        r1 = rsqrt(n1s);
       }
-      terms(ev, el, il, n0s, r0, N0, have1, N1, n1s, r1);
+      terms(xj, xk, ev, el, il, n0s, r0, N0, have1, N1, n1s, r1);
     }
   }
   // sums over the ring: a butterfly over the 8 lanes (every lane ends with
-  // the same sums: each double-word addition is commutative)
+  // the same sums)
 #pragma unroll
   for (int o = 4; o > 0; o >>= 1) {
-    auto bfly = [&](df& x) {
-      const df y = {__shfl_xor_sync(gmask, x.hi, o), __shfl_xor_sync(gmask, x.lo, o)};
-      x = add_s(x, y);
-    };
-    bfly(sc);
-    bfly(sa);
-    bfly(sv);
-    bfly(stt);
+    sc += __shfl_xor_sync(gmask, sc, o);
+    sa += __shfl_xor_sync(gmask, sa, o);
+    sv += __shfl_xor_sync(gmask, sv, o);
+    stt += __shfl_xor_sync(gmask, stt, o);
   }
   double* o = part + 8 * 8 * (size_t)s + 8 * sub;
   if (w8 == 0) {
-    const df A = mul_s(sa, third()), C = half(sc);
-    o[0] = df_to(A);
-    o[1] = df_to(mul_s(sv, third()));
-    o[2] = df_to(C);
-    o[3] = df_to(ldexp2(mul_s(mul_s(C, C), rcp_dw(A)), 2.0f));
-    o[4] = df_to(mul_s(stt, epd.inv_tdiv));
+    const double A = sa * (1.0 / 3.0), C = 0.5 * sc;
+    o[0] = A;
+    o[1] = sv * (1.0 / 3.0);
+    o[2] = C;
+    o[3] = 2 * C * C / A;
+    o[4] = stt * ep.itdiv;
   }
   // repulsion: the near row shared by the variant's 8 lanes, else one lane
   // walks the cell list
@@ -969,12 +959,8 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     e->stencil = stencil;
   }
   EP ep = make_ep(e);
-  const EPD epd = make_epd(ep);
-  // the positions as double-words for the property changes (k_delta), and
-  // the float copy read by the repulsion prefilter
-  const PosDW X{split_positions_dw(e, m->nv, P, s), std::max(m->nv, 1)};
   NLView nlv = e->nl.view;
-  nlv.pos32 = e->pos32.get();
+  nlv.pos32 = e->pos32.get();  // written by the evaluation above
   TopoW t = m->topo_w();
   // workspace of the energy handle: no allocation per sweep
   DevBuf<int>& owner = e->fw_owner;
@@ -1050,7 +1036,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       TM_LAUNCH();
       claim_win(coop);
       k_delta<<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), P, ep, nlv, part.get(), okf.get(),
-                               dpn.get(), dpf.get(), X, epd, e->sctf.get());
+                               dpn.get(), dpf.get(), e->sct.get());
       TM_LAUNCH();
       k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(), accl.get(),
                                pend.get());
@@ -1067,7 +1053,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       key.insert(key.end(), b, b + n);
     };
     const void* ptrs[] = {P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(), part.get(),
-                          okf.get(), dpn.get(), dpf.get(), accl.get(), e->sctf.get(), X.p, m->d_to.get(),
+                          okf.get(), dpn.get(), dpf.get(), accl.get(), e->sct.get(), m->d_to.get(),
                           m->d_next.get(), m->d_face.get(), m->d_vout.get(), m->d_fhe.get(), m->d_slot.get(),
                           m->d_nbr.get(), m->d_val.get(), m->d_fv.get(), m->d_edge.get()};
     add(ptrs, sizeof ptrs);
@@ -1077,7 +1063,6 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
     add(&nlv, sizeof nlv);
     add(&fe, sizeof fe);
     add(&fg, sizeof fg);
-    add(&epd, sizeof epd);
     if (!e->flip_graph.exec || e->flip_graph.key != key) {
       if (e->flip_graph.exec) cudaGraphExecDestroy(e->flip_graph.exec);
       e->flip_graph.exec = nullptr;
