@@ -319,71 +319,64 @@ def batch_replicas():
     return capi.Batch([(p, f) for p, f, _ in reps], [capi.params(**prm) for _, _, prm in reps])
 
 
-def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_steps=20):
+def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_steps=500, n_seq=20, dt=1e-6):
     """Replica batch of the 64-membrane configuration: 16 replicas each of
     642, 2,562, 10,242 and 40,962 vertices, reduced volume ~ U[0.6, 0.95] and
-    kappa_b ~ U[10, 50] (seeded), sampled together by device-side HMC (one
-    launch per stage for all replicas, each HMC step one CUDA graph replay),
-    against the same replicas evaluated one mesh at a time (FP32 stencil,
-    like the batch)."""
+    kappa_b ~ U[10, 50] (seeded), FP32 stencils with FP64 sums.  n_steps HMC
+    steps of n_leapfrog velocity-Verlet steps for all 64 replicas together
+    (each step one CUDA graph replay: the size classes' element kernels side
+    by side, neighbour lists rebuilt after every step), against the same 64
+    replicas as 64 single-mesh device HMC chains run one after another
+    (n_seq steps each, same moves, rebuild after every step).  The measure
+    is aggregate vertex updates per second: n_leapfrog x vertices per HMC
+    step.  The time step is 1e-6: the jittered members reject the
+    configuration's 1e-4 (as the CPU-sized membrane does)."""
     import torch
 
     from trimem_gb300 import capi
+    from trimem_gb300.mc.device import DeviceChain
 
-    L = capi.lib()
     reps = batch_members(n_per_level, levels)
     n_rep = len(reps)
     nvert = sum(len(p) for p, _, _ in reps)
     b = capi.Batch([(p, f) for p, f, _ in reps], [capi.params(**prm) for _, _, prm in reps])
-    # evaluations of all replicas at their construction positions (the
-    # sequential loop below evaluates the same states)
-    for _ in range(3):
-        b.energy(with_grad=False)
-    n_batch = 20
-    e0 = time.perf_counter()
-    for _ in range(n_batch):
-        b.energy(with_grad=False)
-    e1 = time.perf_counter()
-    # then device-side HMC of all replicas, one graph replay per step
-    b.hmc(3, n_leapfrog, 1e-6, seed=1)  # warm-up and graph capture
+    tuning = b.tuning()
+    b.hmc(3, n_leapfrog, dt, seed=1)  # warm-up and graph capture
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    acc = b.hmc(n_steps, n_leapfrog, 1e-6, seed=1)
-    t1 = time.perf_counter()
-    singles = []
+    acc = b.hmc(n_steps, n_leapfrog, dt, seed=1)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    # the same replicas one at a time: single-mesh device chains (FP32
+    # stencils like the batch), each timed over n_seq steps after a warm-up
+    t_seq, acc_seq = 0.0, 0
     for p, f, prm in reps:
         m = capi.Mesh(p, f)
         e = capi.Energy(m, capi.params(**prm))
         e.set_stencil_precision(1)
         x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
-        g = torch.empty_like(x)
-        capi.check(L.tm_energy_update_repulsion_device(e.h, m.h, ctypes_ptr(x), ctypes_ptr_s(stream)))
-        singles.append((m, e, x, g))
-
-    def sweep():
-        for m, e, x, g in singles:
-            capi.check(L.tm_energy_eval_device(e.h, m.h, ctypes_ptr(x), ctypes_ptr(g), None, ctypes_ptr_s(stream)))
-
-    for _ in range(3):
-        sweep()
-    torch.cuda.synchronize()
-    n_sweeps = 10
-    s0 = time.perf_counter()
-    for _ in range(n_sweeps):
-        sweep()
-    torch.cuda.synchronize()
-    s1 = time.perf_counter()
-    batch_rate = n_batch * n_rep / (e1 - e0)
-    seq_rate = n_sweeps * n_rep / (s1 - s0)
+        ch = DeviceChain(m, e, x, dt=dt, n_leapfrog=n_leapfrog, flip_ratio=0.0, refresh=1, seed=3, stream=stream)
+        ch.run(2)
+        torch.cuda.synchronize()
+        a0 = ch.accepted
+        s0 = time.perf_counter()
+        ch.run(n_seq)
+        torch.cuda.synchronize()
+        t_seq += time.perf_counter() - s0
+        acc_seq += ch.accepted - a0
+    upd_batch = n_steps * n_leapfrog * nvert / t_batch
+    upd_seq = n_seq * n_leapfrog * nvert / t_seq
     return {"replicas": n_rep, "vertices": nvert, "sizes": "642/2562/10242/40962 vertices, 16 replicas each",
-            "hmc": f"{n_steps} steps x {n_leapfrog} leapfrog, dt 1e-6, graph replay",
-            "hmc_steps_per_s": round(n_steps / (t1 - t0), 2),
-            "batch_replica_evals_per_s": round(batch_rate, 1),
-            "batch_vertex_evals_per_s": round(batch_rate * nvert / n_rep, 1),
-            "sequential_replica_evals_per_s": round(seq_rate, 1),
-            "speedup": round(batch_rate / seq_rate, 2),
-            "acceptance": round(float(acc.mean()) / n_steps, 3),
-            "timing": "wall clock: 20 synchronising batch evaluations (energy and gradient of all 64) against "
-                      "10 sweeps of single-mesh evaluations with one synchronisation; HMC steps separately"}
+            "size_classes": [{"vertices": [c[0], c[1]], "block_split_face_edge_grad": list(c[2:])} for c in tuning],
+            "hmc": f"{n_steps} steps x {n_leapfrog} leapfrog, dt {dt:g}, graph replay, rebuild every step",
+            "hmc_steps_per_s": round(n_steps / t_batch, 2),
+            "vertex_updates_per_s": round(upd_batch, 1),
+            "acceptance": round(float(acc.sum()) / (n_steps * n_rep), 3),
+            "sequential": {"steps_per_replica": n_seq, "vertex_updates_per_s": round(upd_seq, 1),
+                           "seconds": round(t_seq, 3), "acceptance": round(acc_seq / (n_seq * n_rep), 3)},
+            "speedup": round(upd_batch / upd_seq, 2),
+            "timing": "wall clock around synchronised HMC runs: the batch's n_steps against the sum over the 64 "
+                      "single-mesh chains of n_seq steps each (rates compared)"}
 
 
 def chain_start():

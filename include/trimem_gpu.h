@@ -290,15 +290,24 @@ int tm_surrogate_train_status(tm_strain* t);
 
 /* ---- batches of replicas (no counterpart in the reference: the reference
  * runs one membrane per process) -------------------------------------------
- * n_rep independent meshes with their own parameters evaluated and sampled
- * together: FP32 stencils, FP64 global sums, one launch per stage for all
- * replicas.  Positions live on the device in a padded layout: replica r
- * occupies vertices [offsets[r], offsets[r] + n_points[r]) of
- * [0, n_total) (see tm_batch_layout); padding vertices are inert. */
+ * n_rep independent meshes with their own parameters (exclusion levels
+ * included) evaluated and sampled together: FP32 stencils, FP64 global
+ * sums.  Replicas are grouped into size classes (runs of consecutive
+ * replicas whose vertex counts share a power of two); the element kernels
+ * run per class with block sizes the autotuner picks for that class at
+ * creation, side by side on the classes' streams, and the vertex stage and
+ * repulsion run once for all replicas.  Positions live on the device in a
+ * padded layout: replica r occupies vertices [offsets[r], offsets[r] +
+ * n_points[r]) of [0, n_total) (see tm_batch_layout); padding vertices are
+ * inert. */
 typedef struct tm_batch tm_batch;
 int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_points, const int32_t* const* faces,
                     const int64_t* n_faces, const tm_params* params, tm_batch** out);
 int tm_batch_destroy(tm_batch* b);
+/* the size classes: their number, and per class (up to 8) six ints: first
+ * and end vertex of its range, tuned block sizes of the split, face, edge
+ * and gradient kernels */
+int tm_batch_tuning(tm_batch* b, int32_t* n_classes, int32_t* info);
 int tm_batch_layout(tm_batch* b, int64_t* n_total, int64_t* offsets);
 /* direction 0: device -> host_x, 1: host_x -> device; host_x is n_total x 3 */
 int tm_batch_positions(tm_batch* b, double* host_x, int direction);

@@ -1,6 +1,7 @@
-"""Batches of replicas: one launch per stage for all replicas must give each
-replica the result of its own single-mesh evaluation (FP32 stencils, FP64
-sums), and the batched HMC must be deterministic with and without graphs."""
+"""Batches of replicas: the size-class launches must give each replica the
+result of its own single-mesh evaluation (FP32 stencils, FP64 sums, the
+replica's own exclusion level), and the batched HMC must be deterministic
+with and without graphs."""
 import numpy as np
 import pytest
 
@@ -12,10 +13,13 @@ pytestmark = pytest.mark.gpu
 
 
 def _replicas():
+    """Four replicas of three sizes (three size classes), each with its own
+    bending rigidity, volume target and exclusion level."""
     out = []
-    for k, (level, seed, kb, vf) in enumerate([(2, 1, 10.0, 0.9), (3, 2, 30.0, 0.7), (3, 3, 50.0, 0.95), (4, 4, 20.0, 0.6)]):
+    for level, seed, kb, vf, excl in [(2, 1, 10.0, 0.9, 1), (3, 2, 30.0, 0.7, 2), (3, 3, 50.0, 0.95, 0),
+                                      (4, 4, 20.0, 0.6, 1)]:
         p, f = meshgen.jittered_icosphere(level, seed=seed)
-        prm = workload_params(p, f, kappa_b=kb, vfrac=vf, excl=1, rep_scale=1.2)
+        prm = workload_params(p, f, kappa_b=kb, vfrac=vf, excl=excl, rep_scale=1.2)
         out.append((p, f, prm))
     return out
 
@@ -30,6 +34,11 @@ def test_batch_matches_single_meshes(C):
     reps = _replicas()
     b = C.Batch([(p, f) for p, f, _ in reps], [C.params(**prm) for _, _, prm in reps])
     assert b.n_total % 256 == 0 and list(b.offsets[:-1] % 256) == [0] * len(reps)
+    # size classes: 162 / 642 / 2,562 vertices, each with its tuned block sizes
+    cls = b.tuning()
+    assert [c[:2] for c in cls] == [(b.offsets[0], b.offsets[1]), (b.offsets[1], b.offsets[3]),
+                                     (b.offsets[3], b.offsets[4])]
+    assert all(bs in (64, 128, 256, 512) for c in cls for bs in c[2:])
     eb, gb = b.energy(with_grad=True)
     for r, (p, f, prm) in enumerate(reps):
         m = C.Mesh(p, f)

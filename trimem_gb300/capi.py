@@ -130,6 +130,7 @@ _SIGS = {
     "tm_surrogate_train_step": (_i32, [_p, _p, _p, _p, _p, _p, _p, _i64, _i32, _f32, _f32, _f32, _f32, _f32, _p,
                                        _p]),
     "tm_surrogate_train_status": (_i32, [_p]),
+    "tm_batch_tuning": (_i32, [_p, _p, _p]),
 }
 
 _lib = None
@@ -408,6 +409,14 @@ class Batch:
 
     def update_repulsion(self):
         check(lib().tm_batch_update_repulsion(self.h))
+
+    def tuning(self):
+        """Size classes: (first vertex, end vertex, block sizes of the split,
+        face, edge and gradient kernels) per class."""
+        n = ctypes.c_int32()
+        info = (ctypes.c_int32 * (6 * 8))()
+        check(lib().tm_batch_tuning(self.h, ctypes.byref(n), info))
+        return [tuple(int(v) for v in info[6 * c:6 * c + 6]) for c in range(n.value)]
 
     def hmc(self, n_steps, n_leapfrog, dt, mass=1.0, temperature=1.0, seed=0, use_graph=True, refresh=None):
         """n_steps HMC steps of every replica; accepted steps per replica.

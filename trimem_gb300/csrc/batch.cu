@@ -2,8 +2,7 @@
 //
 // The replicas are one disjoint-union mesh: replica r owns the vertex range
 // [voff[r], voff[r] + nv_r), padded with isolated vertices to a multiple of
-// 256 so that no 256-vertex block straddles two replicas.  Every stage of an
-// evaluation is then one launch for all replicas; per-replica parameters,
+// 256 so that no 256-vertex block straddles two replicas.  Per-replica parameters,
 // global sums (a ticket per replica picks the block that finishes the
 // replica's reduction) and neighbour-list cells (keys tagged with the replica)
 // are looked up through vrep (vertex -> replica, -1 for padding).  Stencils are
@@ -12,9 +11,17 @@
 // An HMC step (momenta, L velocity-Verlet steps, per-replica Metropolis on the
 // exact energies) runs entirely on the device; random numbers come from a
 // device-side step counter, so one step can be captured once into a CUDA graph
-// and replayed.  A small autotuner times the element kernels at a few block
-// sizes when the batch is created and keeps the fastest.
+// and replayed.
+//
+// Replicas fall into size classes (runs of consecutive replicas whose
+// vertex counts share a power of two).  The element kernels (position
+// split, faces, edges, gradient) run per class, side by side on the
+// classes' streams inside the captured step, each with the block size the
+// autotuner picked for that class when the batch was created; the
+// repulsion and the vertex stage (with the per-replica reductions) run once
+// for all replicas.  Each replica keeps its own exclusion level.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -48,7 +55,7 @@ struct tm_batch {
   std::vector<double> initial;  // 6 per replica
   std::unique_ptr<tm_mesh> mesh;
   std::unique_ptr<tm_energy> en;
-  DevBuf<int> vrep;
+  DevBuf<int> vrep, rexcl;  // vertex -> replica, replica -> exclusion level
   DevBuf<int2> rblocks;
   DevBuf<EP> eps;
   DevBuf<Globals> gs;
@@ -57,7 +64,11 @@ struct tm_batch {
   DevBuf<double> x, xs, p, g0, g1, part, sc;  // sc: 4 scalars per replica (E0, K0, E1, K1)
   DevBuf<int> flag, acc;
   DevBuf<unsigned long long> counter;
-  int blk[4] = {256, 256, 256, 256};
+  // size classes (runs of consecutive replicas of similar size) with their
+  // element ranges and tuned block sizes, and their side streams
+  std::vector<BatchClass> cls;
+  BatchStreams bs{};
+  bool have_side = false;
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -72,6 +83,14 @@ struct tm_batch {
   ~tm_batch() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
+    if (have_side) {
+      for (size_t c = 0; c < cls.size(); ++c) {
+        cudaStreamDestroy(bs.cs[c]);
+        cudaEventDestroy(bs.join[c]);
+      }
+      cudaEventDestroy(bs.fork[0]);
+      cudaEventDestroy(bs.fork[1]);
+    }
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -181,7 +200,7 @@ __global__ void k_tick(unsigned long long* counter) {
 
 static void batch_eval(tm_batch* b, const double* x, double* g, cudaStream_t s) {
   energy_eval_batch32(b->en.get(), b->mesh.get(), x, g, b->eps.get(), b->vrep.get(), b->rblocks.get(), b->gs.get(),
-                      b->blk, s);
+                      b->cls.data(), (int)b->cls.size(), b->have_side ? &b->bs : nullptr, s);
 }
 
 static void batch_hmc_step(tm_batch* b, int L, double dt, double m, double T, unsigned long long seed,
@@ -234,35 +253,118 @@ static void rebuild_nlist(tm_batch* b, bool near_rows = true) {
   // near rows when every replica's cells are at least its repulsion cut-off
   bool near = near_rows;
   for (const tm_params& p : b->prm) near = near && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1;
-  nlist_make_batch(&b->en->nl, b->mesh.get(), b->R, b->vrep.get(), b->rblocks.get(), b->rlist.get(),
-                   b->prm[0].exclusion_level, b->x.get(), b->stream, b->eps.get(), near);
+  int excl = 0;
+  for (const tm_params& p : b->prm) excl = std::max(excl, (int)p.exclusion_level);
+  nlist_make_batch(&b->en->nl, b->mesh.get(), b->R, b->vrep.get(), b->rblocks.get(), b->rlist.get(), excl,
+                   b->rexcl.get(), b->x.get(), b->stream, b->eps.get(), near);
 }
 
-// block sizes of {split, face, edge, grad} by timing each candidate
+// Size classes: runs of consecutive replicas whose vertex counts have the
+// same power of two (the 642 / 2,562 / 10,242 / 40,962-vertex levels of the
+// benchmark batch are one class each), with their vertex, face and edge
+// ranges in the union mesh (a replica's faces and edges are consecutive:
+// the union is built replica by replica).  More than TM_MAX_CLASSES runs,
+// or ranges that are not consecutive, give one class for the whole batch.
+static int log2_floor(int n) {
+  int k = -1;
+  for (unsigned u = (unsigned)std::max(n, 1); u; u >>= 1) ++k;
+  return k;
+}
+static void make_classes(tm_batch* b) {
+  tm_mesh* m = b->mesh.get();
+  std::vector<int> rcls(b->R, 0);
+  std::vector<std::pair<int, int>> runs;  // replica ranges
+  for (int r = 0; r < b->R; ++r) {
+    if (r == 0 || log2_floor(b->nreal[r]) != log2_floor(b->nreal[r - 1]))
+      runs.push_back({r, r + 1});
+    else
+      runs.back().second = r + 1;
+    rcls[r] = (int)runs.size() - 1;
+  }
+  std::vector<int> vrep(std::max(m->nv, 1));
+  TM_CUDA(cudaMemcpy(vrep.data(), b->vrep.get(), sizeof(int) * m->nv, cudaMemcpyDeviceToHost));
+  std::vector<int> fv(3 * (size_t)std::max(m->nf, 1));
+  std::vector<int4> ed(std::max(m->ne, 1));
+  if (m->nf) TM_CUDA(cudaMemcpy(fv.data(), m->d_fv.get(), sizeof(int) * 3 * m->nf, cudaMemcpyDeviceToHost));
+  if (m->ne) TM_CUDA(cudaMemcpy(ed.data(), m->d_edge.get(), sizeof(int4) * m->ne, cudaMemcpyDeviceToHost));
+  const int nc = (int)runs.size();
+  std::vector<BatchClass> cls(nc);
+  bool ok = nc <= TM_MAX_CLASSES;
+  for (int c = 0; c < nc && ok; ++c) {
+    cls[c].v0 = b->voff[runs[c].first];
+    cls[c].v1 = b->voff[runs[c].second];
+    cls[c].f0 = cls[c].e0 = INT_MAX;
+    cls[c].f1 = cls[c].e1 = -1;
+  }
+  std::vector<int> fcount(nc, 0), ecount(nc, 0);
+  for (int f = 0; f < m->nf && ok; ++f) {
+    const int c = rcls[vrep[fv[3 * (size_t)f]]];
+    cls[c].f0 = std::min(cls[c].f0, f);
+    cls[c].f1 = std::max(cls[c].f1, f + 1);
+    ++fcount[c];
+  }
+  for (int e = 0; e < m->ne && ok; ++e) {
+    const int c = rcls[vrep[ed[e].x]];
+    cls[c].e0 = std::min(cls[c].e0, e);
+    cls[c].e1 = std::max(cls[c].e1, e + 1);
+    ++ecount[c];
+  }
+  for (int c = 0; c < nc && ok; ++c)
+    ok = cls[c].f1 - cls[c].f0 == fcount[c] && cls[c].e1 - cls[c].e0 == ecount[c];
+  if (!ok) cls.assign(1, BatchClass{0, m->nv, 0, m->nf, 0, m->ne, {256, 256, 256, 256}});
+  for (BatchClass& c : cls)
+    for (int k = 0; k < 4; ++k) c.blk[k] = 256;
+  b->cls = cls;
+  if (cls.size() > 1) {
+    for (size_t c = 0; c < cls.size(); ++c) {
+      TM_CUDA(cudaStreamCreateWithFlags(&b->bs.cs[c], cudaStreamNonBlocking));
+      TM_CUDA(cudaEventCreateWithFlags(&b->bs.join[c], cudaEventDisableTiming));
+    }
+    TM_CUDA(cudaEventCreateWithFlags(&b->bs.fork[0], cudaEventDisableTiming));
+    TM_CUDA(cudaEventCreateWithFlags(&b->bs.fork[1], cudaEventDisableTiming));
+    b->have_side = true;
+  }
+}
+
+// The autotuner: for every size class and element kernel (split, face,
+// edge, gradient), the block size among 64 .. 512 (the gradient kernel is
+// built for at most 256) with the shortest median of five timed launches
+// of that class's kernel alone, after a full evaluation has filled its
+// inputs.
 static void autotune(tm_batch* b) {
   const int cand[4] = {64, 128, 256, 512};
   cudaEvent_t e0, e1;
   TM_CUDA(cudaEventCreate(&e0));
   TM_CUDA(cudaEventCreate(&e1));
-  for (int k = 0; k < 4; ++k) {
-    float best = 1e30f;
-    int bestb = 256;
-    for (int c : cand) {
-      if (k == 3 && c > 256) continue;  // the gradient kernel is built for at most 256 threads
-      b->blk[k] = c;
-      batch_eval(b, b->x.get(), b->g0.get(), b->stream);  // warm
-      TM_CUDA(cudaEventRecord(e0, b->stream));
-      for (int rep = 0; rep < 3; ++rep) batch_eval(b, b->x.get(), b->g0.get(), b->stream);
-      TM_CUDA(cudaEventRecord(e1, b->stream));
-      TM_CUDA(cudaEventSynchronize(e1));
-      float ms = 0;
-      TM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms < best) {
-        best = ms;
-        bestb = c;
+  cudaStream_t s = b->stream;
+  batch_eval(b, b->x.get(), b->g0.get(), s);
+  for (BatchClass& c : b->cls) {
+    for (int k = 0; k < 4; ++k) {
+      float best = 1e30f;
+      int bestb = 256;
+      for (int bsz : cand) {
+        if (k == 3 && bsz > 256) continue;
+        batch32_class_kernel(k, c, bsz, b->en.get(), b->mesh.get(), b->x.get(), b->g0.get(), b->eps.get(),
+                             b->vrep.get(), b->gs.get(), s);  // warm
+        std::vector<float> t;
+        for (int rep = 0; rep < 5; ++rep) {
+          TM_CUDA(cudaEventRecord(e0, s));
+          batch32_class_kernel(k, c, bsz, b->en.get(), b->mesh.get(), b->x.get(), b->g0.get(), b->eps.get(),
+                               b->vrep.get(), b->gs.get(), s);
+          TM_CUDA(cudaEventRecord(e1, s));
+          TM_CUDA(cudaEventSynchronize(e1));
+          float ms = 0;
+          TM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          t.push_back(ms);
+        }
+        std::sort(t.begin(), t.end());
+        if (t[2] < best) {
+          best = t[2];
+          bestb = bsz;
+        }
       }
+      c.blk[k] = bestb;
     }
-    b->blk[k] = bestb;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -280,8 +382,7 @@ int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_poi
   for (int r = 0; r < n_rep; ++r) {
     if (params[r].n_search != 0) fail(TM_ERR_ARG, "batches use the cell list");
     if (params[r].bond_type != 0 && params[r].bond_type != 1) fail(TM_ERR_ARG, "Unknown bond potential");
-    if (params[r].exclusion_level != params[0].exclusion_level)
-      fail(TM_ERR_ARG, "all replicas of a batch share one exclusion level");
+    if (params[r].exclusion_level < 0 || params[r].exclusion_level > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
     b->prm.push_back(params[r]);
   }
   // union layout: replica ranges padded to multiples of 256 vertices
@@ -330,11 +431,17 @@ int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_poi
   b->acc.ensure(n_rep);
   b->counter.ensure(1);
   std::vector<double> rl(n_rep);
-  for (int r = 0; r < n_rep; ++r) rl[r] = params[r].rlist;
+  std::vector<int> rx(n_rep);
+  for (int r = 0; r < n_rep; ++r) {
+    rl[r] = params[r].rlist;
+    rx[r] = params[r].exclusion_level;
+  }
+  b->rexcl.ensure(n_rep);
   cudaStream_t s = b->stream;
   TM_CUDA(cudaMemcpyAsync(b->vrep.get(), vrep.data(), sizeof(int) * nv, cudaMemcpyHostToDevice, s));
   TM_CUDA(cudaMemcpyAsync(b->rblocks.get(), rb.data(), sizeof(int2) * n_rep, cudaMemcpyHostToDevice, s));
   TM_CUDA(cudaMemcpyAsync(b->rlist.get(), rl.data(), sizeof(double) * n_rep, cudaMemcpyHostToDevice, s));
+  TM_CUDA(cudaMemcpyAsync(b->rexcl.get(), rx.data(), sizeof(int) * n_rep, cudaMemcpyHostToDevice, s));
   TM_CUDA(cudaMemcpyAsync(b->x.get(), P.data(), sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, s));
   TM_CUDA(cudaMemsetAsync(b->gs.get(), 0, sizeof(Globals) * n_rep, s));
   TM_CUDA(cudaMemsetAsync(b->acc.get(), 0, sizeof(int) * n_rep, s));
@@ -356,8 +463,22 @@ int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_poi
   }
   upload_eps(b.get());
   rebuild_nlist(b.get());
+  make_classes(b.get());
   autotune(b.get());
   *out = b.release();
+  TM_API_END
+}
+
+int tm_batch_tuning(tm_batch* b, int32_t* n_classes, int32_t* info) {
+  TM_API_BEGIN
+  if (!b || !n_classes) fail(TM_ERR_ARG, "NULL argument");
+  *n_classes = (int32_t)b->cls.size();
+  if (info)
+    for (size_t c = 0; c < b->cls.size(); ++c) {
+      const BatchClass& k = b->cls[c];
+      const int32_t row[6] = {k.v0, k.v1, k.blk[0], k.blk[1], k.blk[2], k.blk[3]};
+      std::memcpy(info + 6 * c, row, sizeof row);
+    }
   TM_API_END
 }
 

@@ -25,18 +25,20 @@ namespace {
 
 using namespace fp32;
 
-__global__ void k_split(int nv, const double* __restrict__ P, float* __restrict__ hi, float* __restrict__ lo) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 3 * nv) return;
+// elements [i0, i1) of the 3 n coordinates
+__global__ void k_split(int i0, int i1, const double* __restrict__ P, float* __restrict__ hi, float* __restrict__ lo) {
+  int i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= i1) return;
   double x = P[i];
   float h = (float)x;
   hi[i] = h;
   lo[i] = (float)(x - (double)h);
 }
 
-__global__ void k_face32(Topo t, Split S, FaceF* __restrict__ fd) {
-  int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= t.nf) return;
+// faces [f0, f1)
+__global__ void k_face32(int f0, int f1, Topo t, Split S, FaceF* __restrict__ fd) {
+  int f = f0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= f1) return;
   int a = t.fv[3 * f], b = t.fv[3 * f + 1], c = t.fv[3 * f + 2];
   f3 eab = S.diff(b, a), eac = S.diff(c, a), ebc = S.diff(c, b);
   f3 N = fcross(eab, eac);
@@ -247,10 +249,11 @@ __global__ void __launch_bounds__(256) k_grad32(Topo t, Split S, const FaceF* __
 // Same arithmetic as the single-mesh FP32 kernels; the parameters and the
 // global sums are per replica (vrep: vertex -> replica, -1 for padding).
 
-__global__ void k_edge32b(Topo t, Split S, const FaceF* __restrict__ fd, EdgeF* __restrict__ ed,
+// edges [e0, e1)
+__global__ void k_edge32b(int e0, int e1, Topo t, Split S, const FaceF* __restrict__ fd, EdgeF* __restrict__ ed,
                           float* __restrict__ ebond, const EP* __restrict__ eps, const int* __restrict__ vrep) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= t.ne) return;
+  int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
   int4 E = t.edge[e];
   const EP& ep = eps[vrep[E.x]];
   f3 ev = S.diff(E.y, E.x);
@@ -363,13 +366,14 @@ __global__ void __launch_bounds__(VB) k_vertex32b(Topo t, const FaceF* __restric
   }
 }
 
-__global__ void __launch_bounds__(256) k_grad32b(Topo t, Split S, const FaceF* __restrict__ fd,
+// vertices [v0, v1)
+__global__ void __launch_bounds__(256) k_grad32b(int v0, int v1, Topo t, Split S, const FaceF* __restrict__ fd,
                                                 const EdgeF* __restrict__ ed, const float* __restrict__ rho,
                                                 const double* __restrict__ repg, const Globals* __restrict__ gs,
                                                 const EP* __restrict__ eps, const int* __restrict__ vrep,
                                                 double* __restrict__ grad) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= t.nv) return;
+  int i = v0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v1) return;
   int rep = vrep[i];
   if (rep < 0) {
     grad[3 * i] = grad[3 * i + 1] = grad[3 * i + 2] = 0.0;
@@ -468,11 +472,11 @@ void energy_eval32(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, bo
   (void)nf;
   (void)ne;
   if (ev) TM_CUDA(cudaEventRecord(ev[0], s));
-  if (m->nv) k_split<<<nblk(3L * m->nv, 256), 256, 0, s>>>(m->nv, P, e->pos32.get(), lo);
+  if (m->nv) k_split<<<nblk(3L * m->nv, 256), 256, 0, s>>>(0, 3 * m->nv, P, e->pos32.get(), lo);
   TM_LAUNCH();
   const bool conc = ev == nullptr;  // repulsion overlaps the face and edge kernels
   if (conc) fork_repulsion(e, m, P, want_grad, s, true);
-  if (t.nf) k_face32<<<nblk(t.nf, 256), 256, 0, s>>>(t, S, fd);
+  if (t.nf) k_face32<<<nblk(t.nf, 256), 256, 0, s>>>(0, t.nf, t, S, fd);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
   if (t.ne) k_edge32<<<nblk(t.ne, 256), 256, 0, s>>>(t, S, fd, ed, eb, ep);
@@ -513,9 +517,9 @@ void energy_eval32_local(tm_energy* e, tm_mesh* m, const double* P, double* d_gr
   float* rho = reinterpret_cast<float*>(e->rho.get());
   TM_CUDA(cudaMemsetAsync(e->reppot.get(), 0, sizeof(double) * nv, s));
   TM_CUDA(cudaMemsetAsync(e->repg.get(), 0, sizeof(double) * 3 * nv, s));
-  if (m->nv) k_split<<<nblk(3L * m->nv, 256), 256, 0, s>>>(m->nv, P, e->pos32.get(), e->poslo.get());
+  if (m->nv) k_split<<<nblk(3L * m->nv, 256), 256, 0, s>>>(0, 3 * m->nv, P, e->pos32.get(), e->poslo.get());
   TM_LAUNCH();
-  if (t.nf) k_face32<<<nblk(t.nf, 256), 256, 0, s>>>(t, S, fd);
+  if (t.nf) k_face32<<<nblk(t.nf, 256), 256, 0, s>>>(0, t.nf, t, S, fd);
   TM_LAUNCH();
   if (t.ne) k_edge32<<<nblk(t.ne, 256), 256, 0, s>>>(t, S, fd, ed, eb, ep);
   TM_LAUNCH();
@@ -526,32 +530,73 @@ void energy_eval32_local(tm_energy* e, tm_mesh* m, const double* P, double* d_gr
   TM_LAUNCH();
 }
 
-void energy_eval_batch32(tm_energy* e, tm_mesh* m, const double* P, double* d_grad, const EP* eps,
-                         const int* vrep, const int2* rblocks, Globals* gs, const int* blk, cudaStream_t s) {
-  e->ensure(m->nv, m->ne, m->nf);
-  size_t nv = std::max(m->nv, 1);
+// One element kernel of one size class of a batch: which 0 split, 1 face,
+// 2 edge, 3 gradient, with block size blk, on stream s.
+void batch32_class_kernel(int which, const BatchClass& c, int blk, tm_energy* e, tm_mesh* m, const double* P,
+                          double* d_grad, const EP* eps, const int* vrep, const Globals* gs, cudaStream_t s) {
   Topo t = m->topo();
-  e->pos32.ensure(3 * nv);
-  e->poslo.ensure(3 * nv);
   Split S{e->pos32.get(), e->poslo.get()};
   FaceF* fd = reinterpret_cast<FaceF*>(e->face.get());
   EdgeF* ed = reinterpret_cast<EdgeF*>(e->edge.get());
   float* eb = reinterpret_cast<float*>(e->ebond.get());
   float* rho = reinterpret_cast<float*>(e->rho.get());
-  // blk: tuned block sizes of the element kernels {split, face, edge, grad}
-  if (m->nv) k_split<<<nblk(3L * m->nv, blk[0]), blk[0], 0, s>>>(m->nv, P, e->pos32.get(), e->poslo.get());
+  if (which == 0 && c.v1 > c.v0)
+    k_split<<<nblk(3L * (c.v1 - c.v0), blk), blk, 0, s>>>(3 * c.v0, 3 * c.v1, P, e->pos32.get(), e->poslo.get());
+  if (which == 1 && c.f1 > c.f0) k_face32<<<nblk(c.f1 - c.f0, blk), blk, 0, s>>>(c.f0, c.f1, t, S, fd);
+  if (which == 2 && c.e1 > c.e0)
+    k_edge32b<<<nblk(c.e1 - c.e0, blk), blk, 0, s>>>(c.e0, c.e1, t, S, fd, ed, eb, eps, vrep);
+  if (which == 3 && c.v1 > c.v0)
+    k_grad32b<<<nblk(c.v1 - c.v0, blk), blk, 0, s>>>(c.v0, c.v1, t, S, fd, ed, rho, e->repg.get(), gs, eps, vrep,
+                                                      d_grad);
   TM_LAUNCH();
-  if (t.nf) k_face32<<<nblk(t.nf, blk[1]), blk[1], 0, s>>>(t, S, fd);
-  TM_LAUNCH();
-  if (t.ne) k_edge32b<<<nblk(t.ne, blk[2]), blk[2], 0, s>>>(t, S, fd, ed, eb, eps, vrep);
-  TM_LAUNCH();
+}
+
+// The batch's evaluation: per size class (consecutive replicas of similar
+// size, each with its own tuned block sizes) the split, face and edge
+// kernels, then the repulsion and the vertex stage for all replicas, then
+// the gradient per class.  With side streams the classes' kernels run
+// side by side (fork and join events), so the small replicas' launches fill
+// the SMs the large ones leave idle.
+void energy_eval_batch32(tm_energy* e, tm_mesh* m, const double* P, double* d_grad, const EP* eps,
+                         const int* vrep, const int2* rblocks, Globals* gs, const BatchClass* cls, int ncls,
+                         const BatchStreams* bs, cudaStream_t s) {
+  e->ensure(m->nv, m->ne, m->nf);
+  size_t nv = std::max(m->nv, 1);
+  Topo t = m->topo();
+  e->pos32.ensure(3 * nv);
+  e->poslo.ensure(3 * nv);
+  FaceF* fd = reinterpret_cast<FaceF*>(e->face.get());
+  EdgeF* ed = reinterpret_cast<EdgeF*>(e->edge.get());
+  float* eb = reinterpret_cast<float*>(e->ebond.get());
+  float* rho = reinterpret_cast<float*>(e->rho.get());
+  const bool side = bs && ncls > 1;
+  auto stream_of = [&](int c) { return side ? bs->cs[c] : s; };
+  auto fork = [&](int k) {
+    if (!side) return;
+    TM_CUDA(cudaEventRecord(bs->fork[k], s));
+    for (int c = 0; c < ncls; ++c) TM_CUDA(cudaStreamWaitEvent(bs->cs[c], bs->fork[k], 0));
+  };
+  auto join = [&]() {
+    if (!side) return;
+    for (int c = 0; c < ncls; ++c) {
+      TM_CUDA(cudaEventRecord(bs->join[c], bs->cs[c]));
+      TM_CUDA(cudaStreamWaitEvent(s, bs->join[c], 0));
+    }
+  };
+  fork(0);
+  for (int c = 0; c < ncls; ++c)
+    for (int k = 0; k < 3; ++k)
+      batch32_class_kernel(k, cls[c], cls[c].blk[k], e, m, P, d_grad, eps, vrep, gs, stream_of(c));
+  join();
   repulsion_eval(e, m, P, e->pos32.get(), true, e->reppot.get(), e->repg.get(), e->slow.get(),
                  e->slow.get() + std::max(m->nv, 1), s, eps);
   int nb = std::max(1, nblk(t.nv, VB));
   k_vertex32b<<<nb, VB, 0, s>>>(t, fd, ed, eb, e->reppot.get(), eps, vrep, rblocks, rho, e->partials.get(), gs);
   TM_LAUNCH();
-  if (t.nv) k_grad32b<<<nblk(t.nv, blk[3]), blk[3], 0, s>>>(t, S, fd, ed, rho, e->repg.get(), gs, eps, vrep, d_grad);
-  TM_LAUNCH();
+  fork(1);
+  for (int c = 0; c < ncls; ++c)
+    batch32_class_kernel(3, cls[c], cls[c].blk[3], e, m, P, d_grad, eps, vrep, gs, stream_of(c));
+  join();
 }
 
 }  // namespace tmg

@@ -497,6 +497,7 @@ __global__ void __launch_bounds__(NB) k_near(int nv, const double* P, NLView nl,
   // exclusion flags (nl_excluded): an entry is excluded when it is in the
   // ring of a or, at level 2, in the ring of a ring vertex of a; the rings
   // are walked once and their vertices looked up in the row
+  if (nl.rexcl) excl = nl.rexcl[rep];  // batch: the replica's level
   if (excl > 0 && n > 0) {
     const int d = t.val[a];
     for (int m = 0; m < d; ++m) {
@@ -783,8 +784,8 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
 }
 
 void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
-                      const double* d_rlist, int excl, const double* P, cudaStream_t s, const EP* d_eps,
-                      bool near) {
+                      const double* d_rlist, int excl, const int* d_rexcl, const double* P, cudaStream_t s,
+                      const EP* d_eps, bool near) {
   if (excl < 0 || excl > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
   int nv = m->nv;
   nl->nv = nv;
@@ -794,6 +795,7 @@ void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const 
   V = NLView{};
   V.kind = 0;
   V.excl = excl;
+  V.rexcl = d_rexcl;
   V.vrep = d_vrep;
   int nb = std::max(1, nblk(nv, BB));
   nl->bbox.ensure(6 * (size_t)nb);

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(256) k_rep_fast(Topo t, const double* __restri
   d3 p = ld3(P, v);
   PairTest pt = make_pair_test(nl, v, ep.rlc1, ep.rT);
   RepAcc acc{ep.rlc1, ep.rr, 0.0, mk(0, 0, 0), GRAD};
-  TableExcl x{t, nl.excl};
+  TableExcl x{t, nl.excl, &nl};
   if (nl.kind == 0) {
     int co[3];
     bool fast = in_build_cell(nl, v, p, co);
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256) k_rep_slow(Topo t, const double* __restri
   int lane = threadIdx.x & 31;
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int nwarps = (gridDim.x * blockDim.x) >> 5;
-  TableExcl x{t, nl.excl};
+  TableExcl x{t, nl.excl, &nl};
   for (int i = warp; i < n; i += nwarps) {
     int v = slow[i];
     const NLGeom& G = geom_of(nl, v);

@@ -91,7 +91,8 @@ __device__ __forceinline__ bool excluded(const Topo& t, int excl, int v, int j) 
 struct TableExcl {  // exclusion on the current topology tables
   const Topo& t;
   int excl;
-  __device__ bool operator()(int v, int j) const { return excluded(t, excl, v, j); }
+  const NLView* nl = nullptr;  // per-replica levels of a batch, when given
+  __device__ bool operator()(int v, int j) const { return excluded(t, nl ? excl_of(*nl, v) : excl, v, j); }
 };
 
 // Cell coordinate int((p - bmin) / rl) with C truncation
@@ -285,7 +286,7 @@ __device__ __forceinline__ void for_each_neighbour_x(const NLView& nl, const dou
 template <class F>
 __device__ __forceinline__ void for_each_neighbour(const NLView& nl, const Topo& t, const double* P, int v, d3 p,
                                                    double dmax, double T, F&& fn) {
-  TableExcl x{t, nl.excl};
+  TableExcl x{t, nl.excl, &nl};
   for_each_neighbour_x(nl, P, v, p, dmax, T, x, fn);
 }
 

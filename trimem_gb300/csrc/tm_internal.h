@@ -98,7 +98,9 @@ constexpr int TM_SCT_N = 404;
 
 struct NLView {
   int kind;  // 0 cell list, 1 Verlet list
-  int excl;
+  int excl;  // exclusion level; for a batch the largest of its replicas' levels
+  // batch of replicas: each replica's exclusion level (by vrep), else NULL
+  const int* rexcl;
   // cell geometry; for a batch of replicas one entry per replica selected by
   // vrep (vertex -> replica), and hash keys carry the replica in bits 44+
   const NLGeom* geom;
@@ -131,6 +133,8 @@ struct NLView {
 __device__ __forceinline__ int rep_of(const NLView& nl, int v) { return nl.vrep ? nl.vrep[v] : 0; }
 __device__ __forceinline__ const NLGeom& geom_of(const NLView& nl, int v) { return nl.geom[rep_of(nl, v)]; }
 __device__ __forceinline__ long long cell_key(long long cid, int rep) { return cid + ((long long)rep << 44); }
+// exclusion level that applies to vertex v
+__device__ __forceinline__ int excl_of(const NLView& nl, int v) { return nl.rexcl ? nl.rexcl[rep_of(nl, v)] : nl.excl; }
 #endif
 
 struct TopoW;
@@ -265,9 +269,25 @@ void surrogate_grad(tm_surrogate* sg, tm_energy* e, tm_mesh* m, const double* d_
                     cudaStream_t s);
 // local terms only (bending and repulsion weights zero), FP32 stencils
 void energy_eval32_local(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, cudaStream_t s);
-// batch of replicas, FP32 stencils and FP64 sums per replica
+// batch of replicas, FP32 stencils and FP64 sums per replica.  A size class
+// is a run of consecutive replicas of similar size: its vertex, face and
+// edge ranges in the union mesh and the block sizes tuned for it
+// {split, face, edge, gradient}.
+struct BatchClass {
+  int v0, v1, f0, f1, e0, e1;
+  int blk[4];
+};
+constexpr int TM_MAX_CLASSES = 8;
+// side streams of the classes and the fork / join events between them
+struct BatchStreams {
+  cudaStream_t cs[TM_MAX_CLASSES];
+  cudaEvent_t fork[2], join[TM_MAX_CLASSES];
+};
 void energy_eval_batch32(tm_energy* e, tm_mesh* m, const double* d_points, double* d_grad, const EP* eps,
-                         const int* vrep, const int2* rblocks, Globals* gs, const int* blk, cudaStream_t s);
+                         const int* vrep, const int2* rblocks, Globals* gs, const BatchClass* cls, int ncls,
+                         const BatchStreams* bs, cudaStream_t s);
+void batch32_class_kernel(int which, const BatchClass& c, int blk, tm_energy* e, tm_mesh* m, const double* P,
+                          double* d_grad, const EP* eps, const int* vrep, const Globals* gs, cudaStream_t s);
 // double-float stencil variant (stencil mode 2)
 void energy_eval_df(tm_energy* e, tm_mesh* m, const double* d_points, bool want_grad, double* d_grad,
                     cudaStream_t s, cudaEvent_t* ev);
@@ -281,9 +301,10 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* d_po
 int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* d_points, double rdist, cudaStream_t s);
 // cell list over a batch of replicas (disjoint-union mesh with replica-aligned
 // 256-vertex blocks): per-replica boxes and cut-offs, replica-tagged cells
+// excl: the largest level of the replicas, d_rexcl: each replica's level
 void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
-                      const double* d_rlist, int excl, const double* d_points, cudaStream_t s, const EP* d_eps,
-                      bool near);
+                      const double* d_rlist, int excl, const int* d_rexcl, const double* d_points, cudaStream_t s,
+                      const EP* d_eps, bool near);
 int64_t nlist_point_distances(tm_nlist* nl, tm_mesh* m, const double* d_points, int pid, double rdist,
                               cudaStream_t s);
 // smallest double T with sqrt(T) >= d (IEEE round-to-nearest sqrt), so that
