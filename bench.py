@@ -1,4 +1,4 @@
-"""Benchmark: FP64 energy+gradient evaluations per second on one GB300.
+"""Benchmark: FP64-accurate energy+gradient evaluations per second on one GB300.
 
 Workload (metric "grad evals/s" on one GB300 at 163k vertices): a level-7
 icosphere (163,842 vertices, 327,680 faces), vertices jittered by 13% of the
@@ -13,28 +13,36 @@ sign alternating from step to step so the positions do not drift).
 
 value:  device-resident evaluations (positions, gradient and energy in HBM),
         every evaluation and rebuild timed with CUDA events on the launching
-        stream, L2 flushed (256 MB write) before each timed piece.
-e2e:    the same evaluations through the public API (trimem_gb300.core:
-        write the positions into TriMesh.points(), EnergyManager
-        .energy_gradient), i.e. host positions uploaded and the gradient read
-        back every evaluation.
+        stream, L2 flushed (256 MB write) before each timed piece; the
+        stencils in double-word arithmetic on the FP32 pipe (the library's
+        default; FP64 results within 1e-10 of the FP64 oracle, tested at this
+        mesh), FP64 global sums and penalties.
+e2e:    the same evaluations through the public API as the reference's
+        drivers call it (trimem_gb300.core: write the positions into
+        TriMesh.points(), EnergyManager.energy and .gradient), i.e. host
+        positions uploaded and the gradient read back every evaluation; the
+        fused energy_gradient call beside it.
 cpu_baseline / --impl reference: the reference algorithm restated on the
         host cores (the reference itself cannot be built: its OpenMesh
         submodule is empty), all threads, energy() + gradient() per
-        evaluation like the reference's Python drivers; chain_step: chain
-        steps of the same restatement from the chains' warmed state.
+        evaluation like the reference's Python drivers (built -O3 -fopenmp
+        with FP contraction; the parity build's rate beside it); chain_step:
+        chain steps of the same restatement from the chains' start state.
 
 Secondary objects on the same line (measured after the timed region):
-roofline        per-kernel times of one cold evaluation (CUDA events inside
-                the library), algorithmic bytes, DRAM traffic and FP64 pipe
+roofline        the whole evaluation against HBM (132 algorithmic bytes
+                per vertex), per-stage times of one cold evaluation (CUDA
+                events inside the library), DRAM traffic and issue-slot
                 activity from the committed ncu summary
 fp32_stencil, df64_stencil   the other stencil precisions: time and error
 surrogate_force the learned force: time, and its tensor-core FLOP rate
 level6          the 40,962-vertex evaluation loop, GPU and CPU
 batch_replicas  64 membranes of 642-40,962 vertices in one batch
-hmc_chain       device chains (HMC move + flip sweep) from a shared warm-up:
-                per-move times, acceptance, ESS/s of the bending energy and
-                the reduced volume, quarter means of the bending trace
+hmc_chain       device chains (HMC move + flip sweep) from a shared
+                equilibrated start (L-BFGS + flip rounds to the 0.65 volume
+                target, long-trajectory heating): per-move times,
+                acceptance, ESS/s of the bending energy and the reduced
+                volume, quarter means and a drift test of the bending trace
 """
 import argparse
 import json
@@ -72,11 +80,12 @@ def config():
             "parallelism": "replicas"}
 
 
-# the committed ncu summary of the headline evaluation's stages: DRAM bytes
-# per stage and the activity of the pipe that bounds the stencils
-TRAFFIC_PROFILE = "profiles/eval_kernels_L7_fp64_sections.md"
-PIPE_NAME = "fp64"
-PIPE_METRIC = "sm__pipe_fp64_cycles_active"
+# the committed ncu summary of the headline (double-word) evaluation's
+# stages: DRAM bytes per stage and the issue-slot activity of each stage's
+# main kernel
+TRAFFIC_PROFILE = "profiles/eval_kernels_L7_df64_sections.md"
+PIPE_NAME = "issue"
+PIPE_METRIC = "smsp__issue_active"
 
 
 def read_traffic():
@@ -379,17 +388,17 @@ def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_step
                       "single-mesh chains of n_seq steps each (rates compared)"}
 
 
-def chain_start():
-    """The chains' workload: the 163,842-vertex membrane with the
-    very-large-mesh energy (reduced-volume target 0.65), relaxed by the
-    device L-BFGS towards that target before sampling (the jittered input is
-    far from equilibrium: its short edges give forces no time step
-    survives).  The learned surrogate's training volumes include this one."""
-    from trimem_gb300.mc.device import relaxed_state
+def chain_state(stream):
+    """The chains' workload and start: the 163,842-vertex membrane with the
+    very-large-mesh energy (reduced-volume target 0.65 of the input sphere's
+    volume at its area), brought to that target by rounds of device L-BFGS
+    and flip sweeps, then heated at T 1 by long-trajectory HMC moves
+    (equilibrated_state), so that the measured chains sample at
+    equilibrium instead of relaxing the sphere's collapse."""
+    from trimem_gb300.mc.device import equilibrated_state
 
     p, f, prm = workload()
-    x0, info = relaxed_state(p, f, prm)
-    return x0, f, prm, info
+    return equilibrated_state(p, f, prm, stream=stream)
 
 
 DT_CANDIDATES = (5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6, 5e-7, 2e-7)
@@ -412,33 +421,6 @@ def _chain_handles(state, stencil):
     en.set_stencil_precision(stencil)
     x = torch.tensor(state["x"], dtype=torch.float64, device="cuda").contiguous()
     return mesh, en, x
-
-
-def chain_warm(stream, start, n_warm=1000):
-    """The chains' common start: the relaxed membrane heated at T 1 by a
-    chain of n_warm steps (the same moves as the measured chains, default
-    stencils, time step tuned at the relaxed state), so that the measured
-    traces start closer to equilibrium instead of climbing from the energy
-    minimum."""
-    import torch
-
-    from trimem_gb300.mc.device import DeviceChain, tune_dt
-
-    x0, f, prm, info = start
-    state = {"x": x0, "faces": f, "prm": prm}
-    mesh, en, x = _chain_handles(state, 2)
-    initial = en.initial_props()
-    dt, _ = tune_dt(mesh, en, x, candidates=DT_CANDIDATES, stream=stream)
-    ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=5, stream=stream)
-    t0 = time.perf_counter()
-    trace = ch.run(n_warm)
-    torch.cuda.synchronize()
-    bend = prm["kappa_b"] * trace[:, 3]
-    q = np.array_split(bend, 4)
-    info = dict(info, warm_steps=n_warm, warm_dt=dt, warm_seconds=round(time.perf_counter() - t0, 3),
-                warm_bending_quarter_means=[round(float(b.mean()), 1) for b in q])
-    return {"x": ch.x.cpu().numpy(), "faces": mesh.fv_indices(), "topo": mesh.topology(), "initial": initial,
-            "prm": prm, "info": info}
 
 
 def drift_check(trace):
@@ -720,11 +702,13 @@ def main():
     # the unique bytes each stage's kernels read and write per launch (their
     # inputs and outputs, including this implementation's face and edge
     # records), for comparison with the per-stage DRAM traffic
+    # (double-word stencils: positions split into 32-byte hi/lo records and
+    # 12-byte floats first, then read as 32 bytes per vertex)
     stage_bytes = {
-        "k_face": 3 * 4 * F + 24 * V + 64 * F,
-        "k_edge": 16 * E + 24 * V + 64 * F + 40 * E,
+        "k_face": 24 * V + 32 * V + 12 * V + 3 * 4 * F + 32 * V + 64 * F + 16 * F,
+        "k_edge": 16 * E + 32 * V + 64 * F + 32 * E + 16 * E,
         "k_vertex": 4 * V + 16 * 2 * E + 16 * F + 16 * E + 8 * V + 16 * V,
-        "k_grad": 4 * V + 16 * 2 * E + 24 * V + 16 * V + 64 * F + 32 * E + 24 * V + 24 * V,
+        "k_grad": 4 * V + 16 * 2 * E + 32 * V + 16 * V + 64 * F + 32 * E + 24 * V + 24 * V,
     }
     peaks = read_peaks()
     hbm = peaks.get("hbm_gbs")
@@ -746,8 +730,8 @@ def main():
                 "stage_ms_cold": {n: round(float(k), 5) for n, k in zip(names, kms[:4])},
                 "eval_ms_cold": round(float(kms[4]), 5),
                 "stage_unique_bytes": stage_bytes,
-                # what bounds the stencils instead of HBM: instruction issue on
-                # the arithmetic pipe of the dominant stage
+                # what bounds the stencils instead of HBM: the issue slots of
+                # the dominant stage's kernel (latency and occupancy limited)
                 "issue_bound": {"pipe": PIPE_NAME, "kernel": dname,
                                 "pipe_active_frac": (round(pipe_active[dname] / 100.0, 3)
                                                      if dname in pipe_active else None),
@@ -898,7 +882,7 @@ def main():
     chain = {}
     warm = None
     try:
-        warm = chain_warm(stream, chain_start())
+        warm = chain_state(stream)
         chain["start"] = warm["info"]
         plain = chain_leg(stream, warm, 2)
         chain["plain_df64"] = plain
@@ -921,7 +905,7 @@ def main():
         cb["parity_build"] = cpu_baseline_parity_build()
         if warm is not None:
             try:
-                cc = cpu_chain_step(warm, dt=warm["info"]["warm_dt"])
+                cc = cpu_chain_step(warm, dt=warm["info"]["heat_dt"])
                 pl = chain.get("plain_df64", {})
                 if "ess_bending" in pl:
                     # same moves and the same algorithm: the GPU chain's ESS
@@ -931,12 +915,13 @@ def main():
             except Exception as exc:
                 cb["chain_step"] = {"error": f"{type(exc).__name__}: {exc}"}
 
-    # this library's kernels per step: 8 per FP64 evaluation (k_face, k_edge,
-    # k_bond_short, k_moved, k_rep_fast, k_rep_slow, k_vertex, k_grad) and 14
+    # this library's kernels per step: 9 per double-word evaluation (k_split_dw,
+    # k_face_dw, k_edge_dw, k_bond_short_dw, k_moved, k_rep_fast, k_rep_slow,
+    # k_vertex_dw, k_grad_dw) and 14
     # per cell-list rebuild (box 2, table 1, insert 1, counts 1, scan 3,
     # starts 1, scatter 1, sort 1, near-row check / build / done 3); the
     # displacement and L2-flush kernels are torch's
-    launches_per_step = 8 * EVALS_PER_STEP + 14
+    launches_per_step = 9 * EVALS_PER_STEP + 14
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

@@ -123,30 +123,44 @@ def test_surrogate_hmc_step_uses_the_exact_hamiltonian(C):
     assert np.isfinite(out4[1]) and np.isfinite(out4[2])
 
 
-def test_trained_network_lowers_the_force_error(C):
-    """What the trained network gains over the leapfrog without it: on a
-    state of the 163,842-vertex benchmark membrane at reduced-volume target
-    0.65 (one of the training volumes; relaxed by the device L-BFGS, then a
-    few chain steps at T 1), the surrogate gradient g_local - F_nn is far
-    closer to the exact gradient than g_local alone (the same integrator
-    with no learned force)."""
-    import torch
-
+@pytest.fixture(scope="module")
+def eq065(C):
+    """The learned-surrogate chains' state: the 163,842-vertex benchmark
+    membrane brought to the reduced-volume target 0.65 (one of the training
+    volumes) and heated at T 1 (equilibrated_state, ~35 s)."""
     from trimem_gb300 import surrogate as S
-    from trimem_gb300.mc.device import DeviceChain, relaxed_state
+    from trimem_gb300.mc.device import equilibrated_state
     from trimem_gb300.workloads import workload_params as wp
 
     if not __import__("os").path.exists(S.WEIGHTS_L7):
         pytest.skip("no trained weights")
     p, f = meshgen.jittered_icosphere(7, seed=0)
     prm = wp(p, f, kappa_b=20.0, vfrac=0.65)
-    x0, _ = relaxed_state(p, f, prm)
-    mesh = C.Mesh(x0, f)
-    en = C.Energy(mesh, C.params(**prm))
-    x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
-    DeviceChain(mesh, en, x, dt=2e-6, n_leapfrog=20, flip_ratio=0.2, seed=3).run(5)
+    return equilibrated_state(p, f, prm, seed=4242)
+
+
+def _handles(C, st):
+    import torch
+
+    mesh = C.Mesh(st["x"], st["faces"])
+    mesh.set_topology(st["topo"])
+    en = C.Energy(mesh, C.params(**st["prm"]))
+    en.set_initial_props(st["initial"])
+    x = torch.tensor(st["x"], dtype=torch.float64, device="cuda").contiguous()
+    C.check(C.lib().tm_energy_update_repulsion_device(en.h, mesh.h, _p(x), None))
+    return mesh, en, x
+
+
+def test_trained_network_lowers_the_force_error(C, eq065):
+    """On the equilibrated state, the surrogate gradient g_local - F_nn is far
+    closer to the exact gradient than g_local alone (the leapfrog force with
+    no learned part)."""
+    import torch
+
+    from trimem_gb300 import surrogate as S
+
+    mesh, en, x = _handles(C, eq065)
     L = C.lib()
-    C.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, _p(x), None))
     g_exact = torch.empty_like(x)
     C.check(L.tm_energy_eval_device(en.h, mesh.h, _p(x), _p(g_exact), None, None))
     sg = C.Surrogate(mesh, np.load(S.WEIGHTS_L7))
@@ -160,3 +174,41 @@ def test_trained_network_lowers_the_force_error(C):
     print(f"relative gradient error: surrogate {err_net:.3e}, without the network {err_none:.3e}")
     assert err_none > 0.005, err_none  # bending and repulsion: a sizeable part of the force here
     assert err_net < 0.25 * err_none, (err_net, err_none)
+
+
+def test_trained_network_conserves_the_hamiltonian(C, eq065):
+    """What the learned force gains inside the sampler: from the equilibrated
+    state, surrogate-driven HMC moves (20 velocity-Verlet steps at dt 1e-6,
+    the exact FP64 Hamiltonian at both ends) with the trained network end
+    with far smaller Hamiltonian errors |H1 - H0|, and so far higher
+    acceptance, than the same moves with the network's output set to zero
+    (the leapfrog on g_local alone).  The exact-force moves are printed
+    beside them: plain HMC remains the better sampler on this energy."""
+    from trimem_gb300 import surrogate as S
+
+    mesh, en, x = _handles(C, eq065)
+    L = C.lib()
+    blob = np.load(S.WEIGHTS_L7)
+    zero = blob.copy()
+    zero[-(2 * S.H + 2):] = 0.0  # w_o, b_o, w_n, b_n: F = 0
+    out = {}
+    for name, w in (("trained", blob), ("zero", zero), ("exact", None)):
+        sg = C.Surrogate(mesh, w) if w is not None else None
+        dh = []
+        for k in range(8):
+            xc = x.clone()
+            o4 = (ctypes.c_double * 4)()
+            pr = (ctypes.c_double * 6)()
+            if sg is None:
+                C.check(L.tm_hmc_step_device(en.h, mesh.h, _p(xc), 1.0, 1e-6, 20, 1.0, 77, k, 0.5, o4, pr, None))
+            else:
+                C.check(L.tm_surrogate_hmc_step_device(sg.h, en.h, mesh.h, _p(xc), 1.0, 1e-6, 20, 1.0, 77, k, 0.5,
+                                                       o4, pr, None))
+            dh.append(o4[2] - o4[1])
+        out[name] = np.array(dh)
+    med = {k: float(np.median(np.abs(v))) for k, v in out.items()}
+    acc = {k: float(np.mean(np.minimum(1.0, np.exp(-v)))) for k, v in out.items()}
+    print(f"median |H1 - H0|: {med}; mean acceptance probability: {acc}")
+    assert np.isfinite(out["trained"]).all()
+    assert med["trained"] < 0.25 * med["zero"], med
+    assert acc["trained"] > acc["zero"] + 0.2, acc

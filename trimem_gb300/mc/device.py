@@ -123,3 +123,70 @@ def tune_dt(mesh, energy, x, candidates=(5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6), n_
         if seen[dt] >= target:
             return dt, seen
     return candidates[-1], seen
+
+
+def equilibrated_state(p, f, prm, rounds=8, maxiter=3000, sweeps=3, heat_steps=100, heat_leapfrog=200,
+                       dt_candidates=(5e-6, 2e-6, 1e-6, 5e-7), seed=1000, stream=None):
+    """A start for chains that sample at equilibrium, from the input mesh
+    (p, f) whose energy targets (area, volume: fractions of the input's) may
+    lie far from its shape, such as a sphere with a reduced-volume target of
+    0.65:
+
+    1. `rounds` rounds of the device L-BFGS (maxiter iterations each, the
+       neighbour list refreshed at every evaluation), each followed by
+       `sweeps` flip sweeps of ratio 0.2 at T 1, which let the triangulation
+       follow the large shape change (a sphere shrinking towards the volume
+       target at constant area buckles into a budded or stomatocyte-like
+       shape; without flips L-BFGS stalls in the symmetric shrunken sphere);
+    2. `heat_steps` HMC moves of `heat_leapfrog` velocity-Verlet steps (at the
+       largest of dt_candidates with pilot acceptance >= 0.5), each with one
+       flip sweep: trajectories ten times longer than the sampling chains'
+       20 steps carry the slow long-wavelength bending modes to their
+       thermal amplitudes in a few hundred moves instead of the hundreds of
+       thousands that short trajectories need (their motion is diffusive
+       below the trajectory's frequency).
+
+    The energy's reference properties stay those of the input mesh.  Returns
+    a dict: x (positions), faces and topo (the flipped triangulation with
+    its edge numbering), initial (reference properties), prm, info."""
+    import torch
+
+    from .. import capi
+    from .minim import minimize_device
+
+    mesh = capi.Mesh(p, f)
+    en = capi.Energy(mesh, capi.params(**prm))
+    initial = en.initial_props()
+    x = torch.tensor(p, dtype=torch.float64, device="cuda").contiguous()
+    lib = capi.lib()
+    sp = ctypes.c_void_p(stream or 0)
+    e0 = en.energy(mesh)
+    t0 = time.perf_counter()
+    relax = []
+    for r in range(rounds):
+        it, e = minimize_device(en, mesh, x, maxiter=maxiter, stream=stream)
+        nacc = 0
+        for k in range(sweeps):
+            n = ctypes.c_int32()
+            capi.check(lib.tm_flip_device(mesh.h, en.h, ctypes.c_void_p(x.data_ptr()), 0.2,
+                                          seed + sweeps * r + k, 1, 4096, ctypes.byref(n), sp))
+            nacc += n.value
+        capi.check(lib.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), sp))
+        relax.append({"iterations": it, "energy": e, "flips": nacc})
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    dt, pilot = tune_dt(mesh, en, x, candidates=dt_candidates, stream=stream)
+    ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=heat_leapfrog, flip_ratio=0.2, seed=seed + 7, stream=stream)
+    trace = ch.run(heat_steps)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    rv = 6.0 * np.sqrt(np.pi) * trace[:, 1] / trace[:, 0] ** 1.5
+    bend = prm["kappa_b"] * trace[:, 3]
+    info = {"energy_start": e0, "relax_rounds": rounds, "relax_iterations": maxiter, "relax_sweeps": sweeps,
+            "relax_energy": [round(r_["energy"], 1) for r_ in relax], "relax_seconds": round(t1 - t0, 2),
+            "heat_steps": heat_steps, "heat_leapfrog": heat_leapfrog, "heat_dt": dt, "heat_pilot": pilot,
+            "heat_acceptance": round(ch.accepted / max(heat_steps, 1), 3), "heat_seconds": round(t2 - t1, 2),
+            "heat_bending_quarter_means": [round(float(b.mean()), 1) for b in np.array_split(bend, 4)],
+            "heat_reduced_volume_quarter_means": [round(float(b.mean()), 4) for b in np.array_split(rv, 4)]}
+    return {"x": x.cpu().numpy(), "faces": mesh.fv_indices(), "topo": mesh.topology(), "initial": initial,
+            "prm": prm, "info": info}

@@ -240,14 +240,15 @@ VOLUMES = (0.65, 0.75, 0.85)
 def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, max_valence=16, log=print):
     """Training states: for each reduced volume, the 163,842-vertex membrane
     (level-7 icosphere, kb 20, the other parameters of the benchmark)
-    relaxed towards that volume by the device L-BFGS, then a plain device
-    HMC chain (20 velocity-Verlet steps at the tuned time step + a flip sweep
-    of ratio 0.2 per step) whose every `every`-th state gives one snapshot:
-    the network inputs and the target g_local - g_exact.  Everything stays
-    in device memory.  Returns (snapshots, (lbar, abar), per-volume info)."""
+    brought to that volume target and heated by equilibrated_state (the
+    start of the benchmark's chains), then a plain device HMC chain (20
+    velocity-Verlet steps at the heating's time step + a flip sweep of ratio
+    0.2 per step) whose every `every`-th state gives one snapshot: the
+    network inputs and the target g_local - g_exact.  Everything stays in
+    device memory.  Returns (snapshots, (lbar, abar), per-volume info)."""
     torch = _torch()
     from . import capi, meshgen
-    from .mc.device import DeviceChain, relaxed_state, tune_dt
+    from .mc.device import DeviceChain, equilibrated_state
     from .workloads import workload_params
 
     p, f = meshgen.jittered_icosphere(level, seed=0)
@@ -258,19 +259,19 @@ def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, m
     for vi, v in enumerate(volumes):
         prm = workload_params(p, f, kappa_b=20.0, vfrac=v)
         t0 = time.perf_counter()
-        x0, rinfo = relaxed_state(p, f, prm)
-        mesh = capi.Mesh(x0, f)
+        st = equilibrated_state(p, f, prm, seed=1000 + 100 * vi)
+        mesh = capi.Mesh(st["x"], st["faces"])
+        mesh.set_topology(st["topo"])
         en = capi.Energy(mesh, capi.params(**prm))
+        en.set_initial_props(st["initial"])
         if scales is None:
-            scales = mesh_scales(x0, f)
+            scales = mesh_scales(st["x"], st["faces"])
             net = make_net()
             with torch.no_grad():
                 net.scales.copy_(torch.tensor([scales[0], scales[1], 1.0]))
-            sg = capi.Surrogate(mesh, to_blob(net))
-        else:
-            sg = capi.Surrogate(mesh, to_blob(net))
-        x = torch.tensor(x0, dtype=torch.float64, device="cuda").contiguous()
-        dt, pilot = tune_dt(mesh, en, x)
+        sg = capi.Surrogate(mesh, to_blob(net))
+        x = torch.tensor(st["x"], dtype=torch.float64, device="cuda").contiguous()
+        dt = st["info"]["heat_dt"]
         ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=seed + vi)
         ch.run(burn)
         if g is None:
@@ -284,7 +285,7 @@ def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, m
             inp.target = (inp.gloc - g).float().contiguous()
             del inp.gloc
             data.append(inp)
-        info.append({"volume_frac": v, "relax": rinfo, "dt": dt, "pilot": pilot, "steps": ch.step_index,
+        info.append({"volume_frac": v, "start": st["info"], "dt": dt, "steps": ch.step_index,
                      "acceptance": round(ch.accepted / max(ch.step_index, 1), 3),
                      "seconds": round(time.perf_counter() - t0, 2)})
         if log:
