@@ -905,7 +905,7 @@ def main():
         cb["parity_build"] = cpu_baseline_parity_build()
         if warm is not None:
             try:
-                cc = cpu_chain_step(warm, dt=warm["info"]["heat_dt"])
+                cc = cpu_chain_step(warm, dt=warm["info"]["warm_dt"])
                 pl = chain.get("plain_df64", {})
                 if "ess_bending" in pl:
                     # same moves and the same algorithm: the GPU chain's ESS

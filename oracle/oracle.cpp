@@ -833,6 +833,23 @@ static void flip_patch(const Mesh& m, int e, std::vector<int>& out) {
   out.erase(std::unique(out.begin(), out.end()), out.end());
 }
 
+// The windowed sweep's patch of a proposal (the device's k_claim_win): the
+// claim is the quad's four vertices and their ring neighbours, the test the
+// quad's four vertices (va0, va1, vb0, vb1 as the device's quad_of).
+static void flip_vertex_patch(const Mesh& m, int e, std::vector<int>& claim, int quad[4]) {
+  quad[0] = m.to[2 * e];
+  quad[1] = m.to[m.next(2 * e)];
+  quad[2] = m.to[2 * e + 1];
+  quad[3] = m.to[m.next(2 * e + 1)];
+  claim.clear();
+  for (int k = 0; k < 4; ++k) {
+    claim.push_back(quad[k]);
+    m.voh(quad[k], [&](int g) { claim.push_back(m.to[g]); });
+  }
+  std::sort(claim.begin(), claim.end());
+  claim.erase(std::unique(claim.begin(), claim.end()), claim.end());
+}
+
 static int flip_serial(Mesh& m, const Energy& E, double ratio, uint64_t seed) {
   // the reference constructs but does not throw an error for ratio > 1
   int ne = m.ne();
@@ -1086,25 +1103,27 @@ static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, 
     return tot;
   };
   double e0 = flip_energy(props);
-  std::vector<int> owner(ne, std::numeric_limits<int>::max());
+  // per vertex: the lowest slot of the window whose patch claims it
+  std::vector<int> owner(m.nv(), std::numeric_limits<int>::max());
   std::vector<long> pending;
   long next_new = 0;
   int acc = 0;
-  std::vector<int> patch;
   std::vector<std::vector<int>> patches;
+  std::vector<std::array<int, 4>> quads;
   while (!pending.empty() || next_new < nflips) {
     std::vector<long> win(pending.begin(), pending.end());
     pending.clear();
     while ((int)win.size() < batch && next_new < nflips) win.push_back(next_new++);
     int W = (int)win.size();
     patches.assign(W, {});
+    quads.assign(W, {});
     for (int s = 0; s < W; ++s) {
-      flip_patch(m, flip_edge_of(seed, win[s], ne), patches[s]);
+      flip_vertex_patch(m, flip_edge_of(seed, win[s], ne), patches[s], quads[s].data());
       for (int x : patches[s]) owner[x] = std::min(owner[x], s);
     }
     std::vector<char> winner(W, 1);
     for (int s = 0; s < W; ++s)
-      for (int x : patches[s])
+      for (int x : quads[s])
         if (owner[x] != s) winner[s] = 0;
     for (int s = 0; s < W; ++s)
       for (int x : patches[s]) owner[x] = std::numeric_limits<int>::max();

@@ -94,9 +94,11 @@ void om_nlist_cell_info(void* nl, double* box6, double* rl3, int* shape3);
 /* flips (src/flips.cpp) */
 int om_flip_serial(void* m, void* e, double ratio, uint64_t seed);
 int om_flip_parallel(void* m, void* e, double ratio, uint64_t seed);
-/* CPU port of the device flip sweep: windows of proposals with disjoint
- * patches, sequential Metropolis in proposal order; mode 0 = window is the
- * longest conflict-free prefix (serial order), 1 = batch with deferral. */
+/* CPU port of the device flip sweep: windows of proposals whose quads lie
+ * at least two edges from the quads of lower slots of the window (vertex
+ * patches: the quad's vertices and their ring neighbours), sequential
+ * Metropolis in proposal order; mode 0 = window is the longest conflict-free
+ * prefix (serial order), 1 = batch with deferral. */
 int om_flip_windowed(void* m, void* e, double ratio, uint64_t seed, int mode, int batch);
 
 /* utilities (src/util.cpp) and the FD gradient (src/bindings.cpp:25-50) */

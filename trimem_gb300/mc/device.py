@@ -125,8 +125,8 @@ def tune_dt(mesh, energy, x, candidates=(5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6), n_
     return candidates[-1], seen
 
 
-def equilibrated_state(p, f, prm, rounds=8, maxiter=3000, sweeps=3, heat_steps=100, heat_leapfrog=200,
-                       dt_candidates=(5e-6, 2e-6, 1e-6, 5e-7), seed=1000, stream=None):
+def equilibrated_state(p, f, prm, rounds=8, maxiter=3000, sweeps=3, warm_steps=100, heat_steps=200,
+                       heat_leapfrog=200, dt_candidates=(5e-6, 2e-6, 1e-6, 5e-7, 2e-7), seed=1000, stream=None):
     """A start for chains that sample at equilibrium, from the input mesh
     (p, f) whose energy targets (area, volume: fractions of the input's) may
     lie far from its shape, such as a sphere with a reduced-volume target of
@@ -138,13 +138,18 @@ def equilibrated_state(p, f, prm, rounds=8, maxiter=3000, sweeps=3, heat_steps=1
        follow the large shape change (a sphere shrinking towards the volume
        target at constant area buckles into a budded or stomatocyte-like
        shape; without flips L-BFGS stalls in the symmetric shrunken sphere);
-    2. `heat_steps` HMC moves of `heat_leapfrog` velocity-Verlet steps (at the
-       largest of dt_candidates with pilot acceptance >= 0.5), each with one
-       flip sweep: trajectories ten times longer than the sampling chains'
-       20 steps carry the slow long-wavelength bending modes to their
-       thermal amplitudes in a few hundred moves instead of the hundreds of
-       thousands that short trajectories need (their motion is diffusive
-       below the trajectory's frequency).
+    2. `warm_steps` HMC moves of 20 velocity-Verlet steps, each with one flip
+       sweep, which bring the fast modes to temperature 1 (long
+       trajectories from the energy minimum are mostly rejected);
+    3. `heat_steps` HMC moves of `heat_leapfrog` velocity-Verlet steps, each
+       with one flip sweep: trajectories ten times longer than the sampling
+       chains' 20 steps carry the slow long-wavelength bending modes to
+       their thermal amplitudes in a few hundred moves instead of the
+       hundreds of thousands that short trajectories need (their motion is
+       diffusive below the trajectory's frequency).
+
+    Each phase runs at the largest of dt_candidates whose pilot acceptance
+    (at that phase's trajectory length) reaches 0.5.
 
     The energy's reference properties stay those of the input mesh.  Returns
     a dict: x (positions), faces and topo (the flipped triangulation with
@@ -175,7 +180,10 @@ def equilibrated_state(p, f, prm, rounds=8, maxiter=3000, sweeps=3, heat_steps=1
         relax.append({"iterations": it, "energy": e, "flips": nacc})
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    dt, pilot = tune_dt(mesh, en, x, candidates=dt_candidates, stream=stream)
+    dtw, _ = tune_dt(mesh, en, x, candidates=dt_candidates, stream=stream)
+    cw = DeviceChain(mesh, en, x, dt=dtw, n_leapfrog=20, flip_ratio=0.2, seed=seed + 5, stream=stream)
+    cw.run(warm_steps)
+    dt, pilot = tune_dt(mesh, en, x, candidates=dt_candidates, n_leapfrog=heat_leapfrog, stream=stream)
     ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=heat_leapfrog, flip_ratio=0.2, seed=seed + 7, stream=stream)
     trace = ch.run(heat_steps)
     torch.cuda.synchronize()
@@ -184,6 +192,8 @@ def equilibrated_state(p, f, prm, rounds=8, maxiter=3000, sweeps=3, heat_steps=1
     bend = prm["kappa_b"] * trace[:, 3]
     info = {"energy_start": e0, "relax_rounds": rounds, "relax_iterations": maxiter, "relax_sweeps": sweeps,
             "relax_energy": [round(r_["energy"], 1) for r_ in relax], "relax_seconds": round(t1 - t0, 2),
+            "warm_steps": warm_steps, "warm_dt": dtw,
+            "warm_acceptance": round(cw.accepted / max(warm_steps, 1), 3),
             "heat_steps": heat_steps, "heat_leapfrog": heat_leapfrog, "heat_dt": dt, "heat_pilot": pilot,
             "heat_acceptance": round(ch.accepted / max(heat_steps, 1), 3), "heat_seconds": round(t2 - t1, 2),
             "heat_bending_quarter_means": [round(float(b.mean()), 1) for b in np.array_split(bend, 4)],

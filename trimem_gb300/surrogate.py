@@ -242,7 +242,7 @@ def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, m
     (level-7 icosphere, kb 20, the other parameters of the benchmark)
     brought to that volume target and heated by equilibrated_state (the
     start of the benchmark's chains), then a plain device HMC chain (20
-    velocity-Verlet steps at the heating's time step + a flip sweep of ratio
+    velocity-Verlet steps at the warm-up's time step + a flip sweep of ratio
     0.2 per step) whose every `every`-th state gives one snapshot: the
     network inputs and the target g_local - g_exact.  Everything stays in
     device memory.  Returns (snapshots, (lbar, abar), per-volume info)."""
@@ -271,7 +271,7 @@ def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, m
                 net.scales.copy_(torch.tensor([scales[0], scales[1], 1.0]))
         sg = capi.Surrogate(mesh, to_blob(net))
         x = torch.tensor(st["x"], dtype=torch.float64, device="cuda").contiguous()
-        dt = st["info"]["heat_dt"]
+        dt = st["info"]["warm_dt"]
         ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=seed + vi)
         ch.run(burn)
         if g is None:
