@@ -24,25 +24,22 @@
 //             edges of the faces around the quad's vertices
 //             (flip_utils.cpp:43-68); the vertex patch suffices for the
 //             exactness above and lets more proposals of a window win.
-//   k_delta<true>   one block per winner evaluates the vertex properties of
-//             the four quad vertices before and after a virtual flip (the
-//             mesh is not touched), including the repulsion with the
-//             post-flip exclusion rings, and reduces them to the property
-//             change of the flip, in double-word arithmetic on the FP32 pipe
-//   k_mclass  Metropolis with T = 1 in slot order (flips.cpp:142-160), phase
-//             1: one block decides every slot whose float-filtered decision
-//             cannot be changed by earlier acceptances (nearly all of them
-//             are rejections) and lists the robustly accepted and the
-//             undecided slots; losers are queued for the next window
-//   k_delta<false>  the listed slots' property changes again, in FP64
-//   k_mwalk   phase 2: one thread walks the listed slots in order with the
-//             FP64 test and the FP64 state updates
+//   k_delta   one block per winner evaluates the vertex properties of the
+//             four quad vertices before and after a virtual flip (the mesh is
+//             not touched), including the repulsion with the post-flip
+//             exclusion rings, and reduces them to the property change of
+//             the flip (stencils in double-word arithmetic on the FP32 pipe)
+//   k_metro   Metropolis with T = 1 in slot order (flips.cpp:142-160): one
+//             block decides every slot whose float-filtered decision cannot
+//             be changed by earlier acceptances and walks the rest, with the
+//             robustly accepted ones, in order with the FP64 test; losers
+//             are queued for the next window
 //   k_commit  accepted flips rewrite their six halfedges, two faces, five
 //             edge rows and four ring rows (one block per flip); patches are
 //             disjoint, so commits never touch the same entries
 // Proposals come from a counter-based SplitMix64 stream of (seed, index), so
 // a sweep is reproducible and matches the CPU port of this algorithm.  The
-// seed lives in the sweep state in device memory, so the 56 launches of a
+// seed lives in the sweep state in device memory, so the 40 launches of a
 // group of eight windows are captured once as a CUDA graph and replayed.
 // A flip is also refused when it would raise a valence above TM_MAXVAL.
 #include <cooperative_groups.h>
@@ -105,12 +102,11 @@ struct FlipState {
   int nacc_win;             // accepted slots of the current window (listed in order)
   float sq[4];  // float-filter constants of props (filter_state)
   long long next_new;  // first proposal not yet in a window
-  long long nn_next;   // next_new after the current window (committed by k_mclass)
+  long long nn_next;   // next_new after the current window (committed by k_metro)
   long long nflips;
   int acc;
   int limit;
   int npend;
-  int nwalk;  // slots listed for the ordered walk of the current window
   int status;
   int W;
   int wid;
@@ -249,7 +245,7 @@ __device__ __forceinline__ double flip_energy(const FlipE& f, const double* p) {
 }
 
 // Float filter of the Metropolis test E(props - dp) - E(props) <= -log u
-// (k_mclass): the energy change is written without cancellation (quadratic
+// (k_metro): the energy change is written without cancellation (quadratic
 // penalties as k t (t - 2 d0), d0 = props/ref - 1 of the current state,
 // t = dp/ref; the linear terms as -k dp) and evaluated from float copies.
 struct FlipEF {
@@ -449,120 +445,11 @@ __device__ bool repulsion_near8(int v, d3 xv, const double* P, const EP& ep, con
   return true;
 }
 
-// Per ring position m of vertex v (face (v, r_m, r_m-1), edge (v, r_m)):
-// half edge length x dihedral angle, face area, face volume, bond; summed
-// over the ring by a butterfly over the variant's 8 lanes (every lane ends
-// with the same sums) and written by lane 0 as the vertex's area, volume,
-// curvature, bending and tether values o[0..4].  With n <= 8 every lane
-// holds one position and the normal of the next face comes from the next
-// lane (the same cross product: (x_r(m+1) - x_v) x (x_r(m) - x_v)).
-// Lanes past the ring and positions without a face compute nothing; the
-// next face's normal is used only where that face exists, and then its
-// lane has computed it.
-__device__ void ring_terms_fp64(const double* P, const EP& ep, const double2* __restrict__ sct, int v,
-                                const int* sr, const unsigned char* sf, int n, int w8, int gbase, unsigned gmask,
-                                double* o) {
-  const d3 xv = ld3(P, v);
-  double sc = 0.0, sa = 0.0, sv = 0.0, stt = 0.0;
-  auto terms = [&](d3 xj, d3 xk, d3 ev, double el, double il, double n0s, double r0, const d3& N0, bool have1,
-                   const d3& N1, double n1s, double r1) {
-    double th = 0.0;
-    if (have1 && n0s != 0.0 && n1s != 0.0) {
-      // dihedral angle from cosine and signed sine (N0 x N1 lies along the
-      // edge; its sign is the reference's test (N0 x N1) . e >= 0)
-      double inv = r0 * r1;
-      double sd = dot(cross(N0, N1), ev) * (inv * il);
-      double a = angle_sc(fabs(sd), dot(N0, N1) * inv, sct);
-      th = sd >= 0.0 ? a : -a;
-    }
-    double fa = 0.5 * (n0s * r0);
-    double tt = 0.0;
-    if (ep.btype == 0) {
-      int r = ep.r;
-      // threshold tests on the length's bits (l >= 0 orders like its bits)
-      if (__double_as_longlong(el) > __double_as_longlong(ep.lc0))
-        tt = ep.br1 * ipow(el - ep.lc0, r);
-      else if (__double_as_longlong(el) < __double_as_longlong(ep.lc1))
-        tt = exp(el * (1.0 / (el - ep.lc1))) * ipow(il, r);
-    } else {
-      double qa = fa / ep.a0 - 1.0;
-      tt = qa * qa;
-    }
-    sc += 0.5 * el * th;
-    sa += fa;
-    sv += dot(cross(xj, xk), xv) * (1.0 / 6.0);
-    stt += tt;
-  };
-  if (n <= 8) {
-    const int m = w8 < n ? w8 : 0;
-    const int mn = m + 1 == n ? 0 : m + 1;
-    const bool act = w8 < n && sf[m];
-    d3 xj = mk(0, 0, 0), xk = xj, ev = xj, N0 = xj;
-    double il = 0.0, el = 0.0, n0s = 0.0, r0 = 0.0;
-    if (act) {
-      xj = ld3(P, sr[m]);
-      xk = ld3(P, sr[m == 0 ? n - 1 : m - 1]);
-      ev = xj - xv;
-      double l2 = dot(ev, ev);
-      il = rsqrt(l2);
-      el = l2 * il;
-      N0 = cross(ev, xk - xv);
-      n0s = dot(N0, N0);
-      r0 = rsqrt(n0s);
-    }
-    const int src = gbase + mn;
-    d3 N1;
-    N1.x = __shfl_sync(gmask, N0.x, src);
-    N1.y = __shfl_sync(gmask, N0.y, src);
-    N1.z = __shfl_sync(gmask, N0.z, src);
-    const double n1s = __shfl_sync(gmask, n0s, src);
-    const double r1 = __shfl_sync(gmask, r0, src);
-    if (act) terms(xj, xk, ev, el, il, n0s, r0, N0, sf[mn] != 0, N1, n1s, r1);
-  } else {
-    for (int m = w8; m < n; m += 8) {
-      if (!sf[m]) continue;
-      int j = sr[m], k = sr[m == 0 ? n - 1 : m - 1];
-      int mn = m + 1 == n ? 0 : m + 1;
-      d3 xj = ld3(P, j), xk = ld3(P, k);
-      d3 ev = xj - xv;
-      double l2 = dot(ev, ev);
-      double il = rsqrt(l2);
-      double el = l2 * il;
-      d3 N0 = cross(ev, xk - xv);
-      double n0s = dot(N0, N0);
-      double r0 = rsqrt(n0s);
-      d3 N1 = mk(0, 0, 0);
-      double n1s = 0.0, r1 = 0.0;
-      const bool have1 = sf[mn] != 0;
-      if (have1) {
-        N1 = cross(ld3(P, sr[mn]) - xv, ev);
-        n1s = dot(N1, N1);
-        r1 = rsqrt(n1s);
-      }
-      terms(xj, xk, ev, el, il, n0s, r0, N0, have1, N1, n1s, r1);
-    }
-  }
-#pragma unroll
-  for (int q = 4; q > 0; q >>= 1) {
-    sc += __shfl_xor_sync(gmask, sc, q);
-    sa += __shfl_xor_sync(gmask, sa, q);
-    sv += __shfl_xor_sync(gmask, sv, q);
-    stt += __shfl_xor_sync(gmask, stt, q);
-  }
-  if (w8 == 0) {
-    const double A = sa * (1.0 / 3.0), C = 0.5 * sc;
-    o[0] = A;
-    o[1] = sv * (1.0 / 3.0);
-    o[2] = C;
-    o[3] = 2 * C * C / A;
-    o[4] = stt * ep.itdiv;
-  }
-}
-
 // The sign of the dihedral angle of edge (v, j) between the faces (v, j, k)
-// and (v, l, j) exactly as ring_terms_fp64 decides it, in FP64 with the same
-// operations.  A fold (angle near +-pi) is where the angle's value jumps
-// from pi to -pi, and there the sign must be the FP64 one.
+// and (v, l, j) as an FP64 evaluation of the stencil decides it (the test of
+// the CPU port: the sign of (N0 x N1) . e, from the same operations).  A
+// fold (angle near +-pi) is where the angle's value jumps from pi to -pi,
+// and there the sign must be the FP64 one.
 __device__ __noinline__ bool fold_sign_fp64(const double* P, int v, int j, int k, int l) {
   const d3 xv = ld3(P, v), xj = ld3(P, j), xk = ld3(P, k), xl = ld3(P, l);
   const d3 ev = xj - xv;
@@ -576,14 +463,22 @@ __device__ __noinline__ bool fold_sign_fp64(const double* P, int v, int j, int k
   return sd >= 0.0;
 }
 
-// The same terms in double-words on the FP32 pipe, positions relative to
-// x_v (the face normal N0 = (x_j - x_v) x (x_k - x_v), the volume term
-// x_v . N0 / 6 = (x_j x x_k) . x_v / 6), the dihedral angle by angle_dw.
-// The results differ from the FP64 ones by rounding (about 1e-14 of the
-// terms), far inside the filter's margin; at a fold (cosine < 0, |sine| <
-// 1e-6: the double-word sine is good to about 1e-14, so its sign could
-// differ from the FP64 one only far inside that band) the sign comes from
-// fold_sign_fp64.
+// Per ring position m of vertex v (face (v, r_m, r_m-1), edge (v, r_m)):
+// half edge length x dihedral angle, face area, face volume, bond, in
+// double-words on the FP32 pipe with positions relative to x_v (the face
+// normal N0 = (x_j - x_v) x (x_k - x_v), the volume term x_v . N0 / 6 =
+// (x_j x x_k) . x_v / 6, the dihedral angle by angle_dw); summed over the
+// ring by a butterfly over the variant's 8 lanes (every lane ends with the
+// same sums) and written by lane 0 as the vertex's area, volume, curvature,
+// bending and tether values o[0..4].  With n <= 8 every lane holds one
+// position and the normal of the next face comes from the next lane (the
+// same cross product: (x_r(m+1) - x_v) x (x_r(m) - x_v)); lanes past the
+// ring and positions without a face compute nothing, and the next face's
+// normal is used only where that face exists, so its lane has computed it.
+// The results differ from FP64 ones by rounding (about 1e-14 of the terms);
+// at a fold (cosine < 0, |sine| < 1e-6: the double-word sine is good to
+// about 1e-14, so its sign could differ from the FP64 one only far inside
+// that band) the sign comes from fold_sign_fp64.
 __device__ void ring_terms_dw(const PosDW& X, const double* P, const EP& ep, const EPD& epd,
                               const float4* __restrict__ sctf, int v, const int* sr, const unsigned char* sf, int n,
                               int w8, int gbase, unsigned gmask, double* o) {
@@ -694,23 +589,19 @@ __device__ void ring_terms_dw(const PosDW& X, const double* P, const EP& ep, con
   }
 }
 
-// Property changes of a window's proposals, in two passes of one kernel:
-//  * k_delta<true>: one block of 64 threads per slot of the window (winners
-//    with a valid flip do work): the change in double-word arithmetic on the
-//    FP32 pipe, written as floats for k_mclass's filter, which decides most
-//    proposals (rejections by a wide margin) from them;
-//  * k_delta<false>: one block per slot that k_mclass listed for the ordered
-//    walk (robustly accepted or undecided): the change in FP64, the values
-//    the walk decides with and adds to the state.
-// So the FP64 pipe, a small fraction of the FP32 rate on GB300, evaluates
-// only the few proposals whose decision or state update needs FP64, and
-// every FP64 value the walk uses is the one the FP64 pass computes for the
-// slot alone.
-// Per block: 8 variants (quad vertex sub & 3, before the flip for sub < 4,
-// after it otherwise) x 8 workers.  The ring of each variant goes to shared
-// memory, the workers compute the per-position terms of vertex_properties
-// (src/mesh_properties.cpp:12-49) in parallel and sum them by a butterfly,
-// and the repulsion (FP64 in both passes) comes from the variant's near row.
+// Property changes of a window's proposals (k_delta): one block of 64
+// threads per slot of the window (winners with a valid flip do work): 8
+// variants (quad vertex sub & 3, before the flip for sub < 4, after it
+// otherwise) x 8 workers.  The ring of each variant goes to shared memory,
+// the workers compute the per-position terms of vertex_properties
+// (src/mesh_properties.cpp:12-49) in double-word arithmetic on the FP32 pipe
+// (GB300's FP64 pipe is a small fraction of the FP32 rate) and sum them by a
+// butterfly, and the repulsion comes from the variant's near row in FP64.
+// The change is written in FP64 (the ordered walk's values) and as floats
+// (the filter's).  It differs from an FP64 evaluation of the same stencils
+// by rounding, about 1e-14 of the terms, as the FP64 evaluation differs from
+// the CPU port's by its summation orders: a Metropolis decision could
+// differ only where E(trial) - E lies within that rounding of -log(u).
 struct DeltaShared {
   int sr[8][TM_MAXVAL + 1];
   unsigned char sf[8][TM_MAXVAL + 1];
@@ -719,22 +610,18 @@ struct DeltaShared {
   double rval[8][NEAR_HITS], rterm[8][NEAR_HITS];
 };
 
-template <bool DW>
 __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& t, const FlipState* st,
                                            const long long* win, const double* P, const EP& ep, const EPD& epd,
                                            const PosDW& X, const NLView& nl, double* part, double* dpn, float* dpf,
-                                           const double2* __restrict__ sct, const float4* __restrict__ sctf) {
+                                           const float4* __restrict__ sctf) {
   const unsigned long long seed = st->seed;
   const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
   const int gbase = threadIdx.x & 24;            // warp lane of the variant's lane 0
   const unsigned gmask = 0xffu << gbase;         // the variant's 8 lanes
   const int e = flip_edge_of(seed, win[s], t.ne);
-  if (DW) {
-    const bool ok = flip_ok(t, e);
-    if (!ok) {
-      if (threadIdx.x == 0) dpf[8 * (size_t)s + 7] = 0.0f;
-      return;
-    }
+  if (!flip_ok(t, e)) {
+    if (threadIdx.x == 0) dpf[8 * (size_t)s + 7] = 0.0f;
+    return;
   }
   const Quad q = quad_of(t, e);
   const int v = quad_vertex(q, sub & 3);
@@ -797,10 +684,7 @@ __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& 
   __syncthreads();
   const int n = sh.sn[sub];
   double* o = part + 8 * 8 * (size_t)s + 8 * sub;
-  if (DW)
-    ring_terms_dw(X, P, ep, epd, sctf, v, sh.sr[sub], sh.sf[sub], n, w8, gbase, gmask, o);
-  else
-    ring_terms_fp64(P, ep, sct, v, sh.sr[sub], sh.sf[sub], n, w8, gbase, gmask, o);
+  ring_terms_dw(X, P, ep, epd, sctf, v, sh.sr[sub], sh.sf[sub], n, w8, gbase, gmask, o);
   // repulsion: the near row shared by the variant's 8 lanes, else one lane
   // walks the cell list
   {
@@ -829,51 +713,32 @@ __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& 
       double before = ((op[k] + op[8 + k]) + op[16 + k]) + op[24 + k];
       double after = ((op[40 + k] + op[48 + k]) + op[56 + k]) + op[32 + k];
       const double dk = before - after;
-      if (DW)
-        dpf[8 * (size_t)s + k] = (float)dk;
-      else
-        dpn[8 * (size_t)s + k] = dk;
+      dpn[8 * (size_t)s + k] = dk;
+      dpf[8 * (size_t)s + k] = (float)dk;
     }
     if (threadIdx.x == 0) {
-      const double u = flip_u_of(seed, win[s]);
-      if (DW) {
-        // -log(u) in float for the filter (NaN below float range: the FP64
-        // test decides) and the eligibility flag
-        const float uf = (float)u;
-        dpf[8 * (size_t)s + 6] = uf > 1e-30f ? -logf(uf) : __int_as_float(0x7fc00000);
-        dpf[8 * (size_t)s + 7] = 1.0f;
-      } else {
-        dpn[8 * (size_t)s + 6] = -log(u);  // for the ordered walk
-      }
+      // -log(u) in float for the filter (NaN below float range: the FP64
+      // test decides; k_metro computes -log(u) in FP64 for the slots it
+      // walks) and the eligibility flag
+      const float uf = (float)flip_u_of(seed, win[s]);
+      dpf[8 * (size_t)s + 6] = uf > 1e-30f ? -logf(uf) : __int_as_float(0x7fc00000);
+      dpf[8 * (size_t)s + 7] = 1.0f;
     }
   }
 }
 
-// k_delta<true>: one block per slot of the window; k_delta<false>: the
-// listed slots, every gridDim-th per block
-template <bool DW>
 __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, const long long* win,
-                                              const unsigned char* winner, const int* limit, const int* wl,
-                                              const double* P, EP ep, EPD epd, PosDW X, NLView nl, double* part,
-                                              double* dpn, float* dpf, const double2* __restrict__ sct,
+                                              const unsigned char* winner, const int* limit, const double* P, EP ep,
+                                              EPD epd, PosDW X, NLView nl, double* part, double* dpn, float* dpf,
                                               const float4* __restrict__ sctf) {
   __shared__ DeltaShared sh;
-  if (DW) {
-    const int s = blockIdx.x;
-    if (s >= st->W) return;
-    if (s >= *limit || !winner[s]) {
-      if (threadIdx.x == 0) dpf[8 * (size_t)s + 7] = 0.0f;
-      return;
-    }
-    delta_slot<true>(s, sh, t, st, win, P, ep, epd, X, nl, part, dpn, dpf, sct, sctf);
-  } else {
-    const int nw = st->nwalk;
-    for (int b = blockIdx.x; b < nw; b += gridDim.x) {
-      const int c = wl[b];
-      delta_slot<false>(c >= 0 ? c : -1 - c, sh, t, st, win, P, ep, epd, X, nl, part, dpn, dpf, sct, sctf);
-      __syncthreads();  // the next slot reuses the shared rings
-    }
+  const int s = blockIdx.x;
+  if (s >= st->W) return;
+  if (s >= *limit || !winner[s]) {
+    if (threadIdx.x == 0) dpf[8 * (size_t)s + 7] = 0.0f;
+    return;
   }
+  delta_slot(s, sh, t, st, win, P, ep, epd, X, nl, part, dpn, dpf, sctf);
 }
 
 // Metropolis with T = 1 in slot order (flips.cpp:142-160): slot s is tried on
@@ -929,19 +794,17 @@ __device__ __forceinline__ int2 block_scan2(int a, int b, int* ea, int* eb, int2
 }
 
 constexpr int PREF = 256;  // walked slots whose data is prefetched into shared memory
-
-// Phase 1 (k_mclass, one block): classify every eligible slot by the float
-// filter from the double-word property changes, list the robustly accepted
-// and the undecided slots in order for the walk (wl: s, or -1 - s when the
-// FP64 test must decide) and compact the deferred proposals in order for
-// the next window.
-__global__ void __launch_bounds__(MB) k_mclass(const long long* win, const unsigned char* winner, const float* dpf,
-                                              FlipEF fg, FlipState* st, const int* limit, int* wl, long long* pend) {
+__global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsigned char* winner, const double* dpn,
+                                             const float* dpf, FlipE fe, FlipEF fg, FlipState* st, const int* limit,
+                                             int* accl, long long* pend) {
   constexpr unsigned char SKIP = 0, REJECT = 1, ACCEPT = 2, OPEN = 3;
+  __shared__ int lst[MAXB];
+  __shared__ double sdp[PREF][7];  // dp of the walked slots, and -log(u) of the open ones
   __shared__ int2 wsum[32];
   __shared__ float sb[3][32];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int W = st->W;
+  const unsigned long long seed = st->seed;
   float q[4];
   for (int k = 0; k < 4; ++k) q[k] = st->sq[k];
   // window-wide bound of the state's movement: sum of |dp|/ref of the
@@ -977,6 +840,7 @@ __global__ void __launch_bounds__(MB) k_mclass(const long long* win, const unsig
   ba *= 1.001f;  // float rounding of the sums
   bv *= 1.001f;
   bc *= 1.001f;
+  // phase 1: classify this thread's slots
   unsigned char cls[MS];
   int nopen = 0;
   for (int k = 0; k < MS; ++k) {
@@ -1000,6 +864,8 @@ __global__ void __launch_bounds__(MB) k_mclass(const long long* win, const unsig
     cls[k] = d < -m ? ACCEPT : (d > m ? REJECT : OPEN);  // NaN or overflow: OPEN
     if (cls[k] >= ACCEPT) ++nopen;
   }
+  // slots to walk (robustly accepted or open) and deferred proposals, both
+  // in slot order
   const int lim = *limit;
   int ndef = 0;
   for (int k = 0; k < MS; ++k) {
@@ -1011,44 +877,31 @@ __global__ void __launch_bounds__(MB) k_mclass(const long long* win, const unsig
   for (int k = 0; k < MS; ++k) {
     const int s = tid * MS + k;
     if (s >= W) break;
-    if (cls[k] >= ACCEPT) wl[ew++] = cls[k] == ACCEPT ? s : -1 - s;
+    if (cls[k] >= ACCEPT) lst[ew++] = cls[k] == ACCEPT ? s : -1 - s;
     if (s >= lim || !winner[s]) pend[ed++] = win[s];
   }
-  if (tid == 0) {
-    st->nwalk = tot.x;
-    st->npend = tot.y;
-    st->next_new = st->nn_next;
-  }
-}
-
-// Phase 2 (k_mwalk, one block, after k_delta<false> has written the FP64
-// changes of the listed slots): one thread walks the list in slot order on
-// the FP64 state, the robustly accepted slots with the state update alone,
-// the undecided ones with the FP64 test first; their data is prefetched
-// into shared memory by the block.
-__global__ void __launch_bounds__(MB) k_mwalk(const int* wl, const double* dpn, FlipE fe, FlipState* st, int* accl) {
-  __shared__ double sdp[PREF][7];  // dp of the walked slots, and -log(u) of the open ones
-  const int tid = threadIdx.x;
-  const int nw = st->nwalk;
-  if (tid < PREF && tid < nw) {
-    const int c = wl[tid];
+  __syncthreads();
+  // the walk's data (dp, and -log(u) in FP64 for the open slots) fetched and
+  // computed in parallel
+  if (tid < PREF && tid < tot.x) {
+    const int c = lst[tid];
     const int s = c >= 0 ? c : -1 - c;
     for (int k = 0; k < 6; ++k) sdp[tid][k] = dpn[8 * (size_t)s + k];
-    sdp[tid][6] = c >= 0 ? 0.0 : dpn[8 * (size_t)s + 6];
+    sdp[tid][6] = c >= 0 ? 0.0 : -log(flip_u_of(seed, win[s]));
   }
   __syncthreads();
+  // phase 2: one thread walks the listed slots in order on the FP64 state.
+  // The state's energy is needed only by an FP64 test and at the end, so
+  // after robust acceptances it is computed when next needed (flip_energy of
+  // the same state: the value that computing it at every acceptance gives).
   if (tid == 0) {
-    // the energy of the state is needed only by an FP64 test and at the
-    // end, so after robust acceptances it is computed when next needed
-    // (flip_energy of the same state: the same value as computing it at
-    // every acceptance)
     double sP[6];
     for (int k = 0; k < 6; ++k) sP[k] = st->props[k];
     double se0 = st->e0;
     bool fresh = true;
     int sacc = st->acc, nacc = 0;
-    for (int i = 0; i < nw; ++i) {
-      const int c = wl[i];
+    for (int i = 0; i < tot.x; ++i) {
+      const int c = lst[i];
       const bool robust = c >= 0;
       const int s = robust ? c : -1 - c;
       double o8[7];
@@ -1056,7 +909,7 @@ __global__ void __launch_bounds__(MB) k_mwalk(const int* wl, const double* dpn, 
         for (int k = 0; k < 7; ++k) o8[k] = sdp[i][k];
       } else {
         for (int k = 0; k < 6; ++k) o8[k] = dpn[8 * (size_t)s + k];
-        o8[6] = robust ? 0.0 : dpn[8 * (size_t)s + 6];
+        o8[6] = robust ? 0.0 : -log(flip_u_of(seed, win[s]));
       }
       double trial[6];
       for (int k = 0; k < 6; ++k) trial[k] = sP[k] - o8[k];
@@ -1083,6 +936,8 @@ __global__ void __launch_bounds__(MB) k_mwalk(const int* wl, const double* dpn, 
     filter_state(fe, sP, st->sq);
     st->e0 = se0;
     st->acc = sacc;
+    st->npend = tot.y;
+    st->next_new = st->nn_next;
   }
 }
 
@@ -1132,7 +987,7 @@ __device__ void commit_one(const TopoW& t, long long p, FlipState* st) {
   __syncwarp();
 }
 
-// the window's accepted flips (listed by k_mwalk), every CB-th per block
+// the window's accepted flips (listed by k_metro), every CB-th per block
 constexpr int CB = 152;
 __global__ void __launch_bounds__(32) k_commit(TopoW t, const long long* win, const int* accl, FlipState* st) {
   const int nacc = st->nacc_win;
@@ -1183,7 +1038,6 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   DevBuf<long long>& win = e->fw_win;
   DevBuf<long long>& pend = e->fw_pend;
   DevBuf<unsigned char>& winner = e->fw_winner;
-  DevBuf<int>& wl = e->fw_wl;
   DevBuf<int>& accl = e->fw_accl;
   DevBuf<double>& part = e->fw_part;
   DevBuf<double>& dpn = e->fw_dpn;
@@ -1192,7 +1046,6 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   win.ensure(MAXB);
   pend.ensure(MAXB);
   winner.ensure(MAXB);
-  wl.ensure(MAXB);
   accl.ensure(MAXB);
   part.ensure(64 * (size_t)MAXB);
   dpn.ensure(8 * (size_t)MAXB);
@@ -1250,16 +1103,11 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st, win.get(), limit.get());
       TM_LAUNCH();
       claim_win(coop);
-      k_delta<true><<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), wl.get(), P, ep, epd, X, nlv,
-                                     part.get(), dpn.get(), dpf.get(), e->sct.get(), e->sctf.get());
+      k_delta<<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), P, ep, epd, X, nlv, part.get(),
+                               dpn.get(), dpf.get(), e->sctf.get());
       TM_LAUNCH();
-      k_mclass<<<1, MB, 0, s>>>(win.get(), winner.get(), dpf.get(), fg, st, limit.get(), wl.get(), pend.get());
-      TM_LAUNCH();
-      k_delta<false><<<std::min(B, 256), 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), wl.get(), P, ep,
-                                                     epd, X, nlv, part.get(), dpn.get(), dpf.get(), e->sct.get(),
-                                                     e->sctf.get());
-      TM_LAUNCH();
-      k_mwalk<<<1, MB, 0, s>>>(wl.get(), dpn.get(), fe, st, accl.get());
+      k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(), accl.get(),
+                               pend.get());
       TM_LAUNCH();
       k_commit<<<CB, 32, 0, s>>>(t, win.get(), accl.get(), st);
       TM_LAUNCH();
@@ -1273,8 +1121,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       key.insert(key.end(), b, b + n);
     };
     const void* ptrs[] = {P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(), part.get(),
-                          wl.get(), dpn.get(), dpf.get(), accl.get(), e->sct.get(), e->sctf.get(), X.p,
-                          m->d_to.get(),
+                          dpn.get(), dpf.get(), accl.get(), e->sctf.get(), X.p, m->d_to.get(),
                           m->d_next.get(), m->d_face.get(), m->d_vout.get(), m->d_fhe.get(), m->d_slot.get(),
                           m->d_nbr.get(), m->d_val.get(), m->d_fv.get(), m->d_edge.get()};
     add(ptrs, sizeof ptrs);

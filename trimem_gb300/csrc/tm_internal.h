@@ -219,7 +219,7 @@ struct tm_energy {
   tmg::DevBuf<double2> sct;  // {sin, cos}(k / 128), k < TM_SCT_N
   tmg::DevBuf<float4> sctf;  // the same as double-words (sin hi, sin lo, cos hi, cos lo)
   // flip-sweep workspace, kept between sweeps (grown on demand)
-  tmg::DevBuf<int> fw_owner, fw_limit, fw_accl, fw_wl;
+  tmg::DevBuf<int> fw_owner, fw_limit, fw_accl;
   tmg::DevBuf<long long> fw_win, fw_pend;
   tmg::DevBuf<unsigned char> fw_winner, fw_state;
   tmg::DevBuf<double> fw_part, fw_dpn;
