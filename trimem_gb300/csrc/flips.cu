@@ -807,17 +807,27 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
   const unsigned long long seed = st->seed;
   float q[4];
   for (int k = 0; k < 4; ++k) q[k] = st->sq[k];
+  // this thread's slots' float records (two 16-byte loads each; the
+  // eligibility flag 0 for slots past the window)
+  float4 fa[MS], fb[MS];
+  for (int k = 0; k < MS; ++k) {
+    const int s = tid * MS + k;
+    fa[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    fb[k] = fa[k];
+    if (s < W) {
+      const float4* r = reinterpret_cast<const float4*>(dpf + 8 * (size_t)s);
+      fa[k] = r[0];
+      fb[k] = r[1];
+    }
+  }
   // window-wide bound of the state's movement: sum of |dp|/ref of the
   // eligible slots (area, volume, curvature)
   float ba = 0.0f, bv = 0.0f, bc = 0.0f;
   for (int k = 0; k < MS; ++k) {
-    const int s = tid * MS + k;
-    if (s >= W) break;
-    const float* f8 = dpf + 8 * (size_t)s;
-    if (f8[7] == 0.0f) continue;
-    ba += fabsf(f8[0] * fg.irA);
-    bv += fabsf(f8[1] * fg.irV);
-    bc += fabsf(f8[2] * fg.irC);
+    if (fb[k].w == 0.0f) continue;
+    ba += fabsf(fa[k].x * fg.irA);
+    bv += fabsf(fa[k].y * fg.irV);
+    bc += fabsf(fa[k].z * fg.irC);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -844,11 +854,9 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
   unsigned char cls[MS];
   int nopen = 0;
   for (int k = 0; k < MS; ++k) {
-    const int s = tid * MS + k;
     cls[k] = SKIP;
-    if (s >= W) continue;
-    const float* f8 = dpf + 8 * (size_t)s;
-    if (f8[7] == 0.0f) continue;
+    if (fb[k].w == 0.0f) continue;
+    const float f8[8] = {fa[k].x, fa[k].y, fa[k].z, fa[k].w, fb[k].x, fb[k].y, fb[k].z, fb[k].w};
     const float ta = f8[0] * fg.irA, tv = f8[1] * fg.irV, tc = f8[2] * fg.irC;
     const float xa = fg.ka * ta * (ta - 2.0f * q[0]);
     const float xv = fg.kv * tv * (tv - 2.0f * q[1]);
@@ -874,13 +882,56 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
   }
   int ew = 0, ed = 0;
   const int2 tot = block_scan2(nopen, ndef, &ew, &ed, wsum);
+  bool mine_open = false;
   for (int k = 0; k < MS; ++k) {
     const int s = tid * MS + k;
     if (s >= W) break;
     if (cls[k] >= ACCEPT) lst[ew++] = cls[k] == ACCEPT ? s : -1 - s;
     if (s >= lim || !winner[s]) pend[ed++] = win[s];
+    mine_open = mine_open || cls[k] == OPEN;
   }
-  __syncthreads();
+  if (!__syncthreads_or(mine_open)) {
+    // every listed slot is a robust acceptance (the common case: the float
+    // filter leaves a slot undecided only within about 1e-4 of its terms of
+    // the threshold): the state moves by the sum of their changes, taken by
+    // a fixed-order block reduction instead of one thread's chain of FP64
+    // subtractions (the FP64 pipe's latency makes that chain the window's
+    // longest wait).  The state differs from the ordered walk's by rounding
+    // (1e-16 relative), which an FP64 test of a later window could feel
+    // only for |E(trial) - E + log u| of that order.
+    double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int i = tid; i < tot.x; i += MB) {
+      const int c = lst[i];
+      for (int k = 0; k < 6; ++k) a[k] += dpn[8 * (size_t)c + k];
+      accl[i] = c;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      for (int k = 0; k < 6; ++k) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+    if (lane == 0)
+      for (int k = 0; k < 6; ++k) sdp[w][k] = a[k];
+    __syncthreads();
+    if (w == 0) {
+      for (int k = 0; k < 6; ++k) a[k] = sdp[lane][k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 6; ++k) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+      if (lane == 0) {
+        double sP[6];
+        for (int k = 0; k < 6; ++k) sP[k] = st->props[k] - a[k];
+        if (tot.x > 0) {
+          st->e0 = flip_energy(fe, sP);
+          for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
+          filter_state(fe, sP, st->sq);
+        }
+        st->nacc_win = tot.x;
+        st->acc += tot.x;
+        st->npend = tot.y;
+        st->next_new = st->nn_next;
+      }
+    }
+    return;
+  }
   // the walk's data (dp, and -log(u) in FP64 for the open slots) fetched and
   // computed in parallel
   if (tid < PREF && tid < tot.x) {
