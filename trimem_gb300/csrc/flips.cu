@@ -19,8 +19,8 @@
 //             change of a proposal reads the rings of its quad's vertices and
 //             of their neighbours); in serial mode the window is cut at the
 //             first loser, so proposals are decided in proposal order
-//             (k_claim_win does both in one cooperative launch with a grid
-//             barrier when it fits).  The reference locks a larger patch, the
+//             (k_claim_win does the three in one cooperative launch with a
+//             grid barrier when it fits).  The reference locks a larger patch, the
 //             edges of the faces around the quad's vertices
 //             (flip_utils.cpp:43-68); the vertex patch suffices for the
 //             exactness above and lets more proposals of a window win.
@@ -39,7 +39,7 @@
 //             disjoint, so commits never touch the same entries
 // Proposals come from a counter-based SplitMix64 stream of (seed, index), so
 // a sweep is reproducible and matches the CPU port of this algorithm.  The
-// seed lives in the sweep state in device memory, so the 40 launches of a
+// seed lives in the sweep state in device memory, so the 32 launches of a
 // group of eight windows are captured once as a CUDA graph and replayed.
 // A flip is also refused when it would raise a valence above TM_MAXVAL.
 #include <cooperative_groups.h>
@@ -336,23 +336,37 @@ __global__ void k_winner(TopoW t, const FlipState* st, int mode, const long long
   }
 }
 
-// k_claim and k_winner in one cooperative launch: the claims, a grid-wide
-// barrier, then the ownership test on the same edges (read past L1)
-__global__ void __launch_bounds__(64) k_claim_win(TopoW t, const FlipState* st, int mode, const long long* win,
-                                                 int* owner, unsigned char* winner, int* limit) {
+// k_fill, k_claim and k_winner in one cooperative launch: every thread takes
+// its slot's proposal from the previous window's state (deferred proposals
+// first, then new ones, as k_fill), the claims, a grid-wide barrier, then
+// the window's state is advanced and the ownership test runs on the same
+// vertices (read past L1)
+__global__ void __launch_bounds__(64) k_claim_win(TopoW t, FlipState* st, int B, int mode, const long long* pend,
+                                                 long long* win, int* owner, unsigned char* winner, int* limit) {
   const unsigned long long seed = st->seed;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   const int s = g >> 2, k = g & 3;
-  const int W = st->W, wid = st->wid;
+  const int np = st->npend;
+  const long long nn = st->next_new;
+  const int W = (int)min((long long)B, (long long)np + (st->nflips - nn));
+  const int wid = st->wid + (W > 0 ? 1 : 0);
   const bool act = s < W;  // the four threads of a slot agree
   int v = 0, tag = 0;
+  if (g == 0) *limit = W;
   if (act) {
-    const Quad q = quad_of(t, flip_edge_of(seed, win[s], t.ne));
+    const long long p = s < np ? pend[s] : nn + (s - np);
+    if (k == 0) win[s] = p;
+    const Quad q = quad_of(t, flip_edge_of(seed, p, t.ne));
     tag = owner_tag(wid, s);
     v = quad_vertex(q, k);
     claim_closure(t, v, tag, owner);
   }
-  cooperative_groups::this_grid().sync();
+  cooperative_groups::this_grid().sync();  // every thread has read the state and claimed
+  if (g == 0) {
+    st->W = W;
+    st->wid = wid;
+    st->nn_next = nn + (W - np);
+  }
   if (act) {
     bool ok = __ldcg(&owner[v]) == tag;
     const unsigned gmask = 0xfu << (threadIdx.x & 28);
@@ -603,6 +617,7 @@ __device__ void ring_terms_dw(const PosDW& X, const double* P, const EP& ep, con
 // the CPU port's by its summation orders: a Metropolis decision could
 // differ only where E(trial) - E lies within that rounding of -log(u).
 struct DeltaShared {
+  double part[64];  // per variant: area, volume, curvature, bending, tether, repulsion
   int sr[8][TM_MAXVAL + 1];
   unsigned char sf[8][TM_MAXVAL + 1];
   int sn[8];
@@ -612,7 +627,7 @@ struct DeltaShared {
 
 __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& t, const FlipState* st,
                                            const long long* win, const double* P, const EP& ep, const EPD& epd,
-                                           const PosDW& X, const NLView& nl, double* part, double* dpn, float* dpf,
+                                           const PosDW& X, const NLView& nl, double* dpn, float* dpf,
                                            const float4* __restrict__ sctf) {
   const unsigned long long seed = st->seed;
   const int sub = threadIdx.x >> 3, w8 = threadIdx.x & 7;
@@ -683,7 +698,7 @@ __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& 
   }
   __syncthreads();
   const int n = sh.sn[sub];
-  double* o = part + 8 * 8 * (size_t)s + 8 * sub;
+  double* o = sh.part + 8 * sub;
   ring_terms_dw(X, P, ep, epd, sctf, v, sh.sr[sub], sh.sf[sub], n, w8, gbase, gmask, o);
   // repulsion: the near row shared by the variant's 8 lanes, else one lane
   // walks the cell list
@@ -707,7 +722,7 @@ __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& 
   // of edge_vertex_properties before (va0, va1, vb0, vb1) and after the flip
   // (va1, vb0, vb1, va0)): lane k of warp 0 takes property k
   if (threadIdx.x < 32) {
-    const double* op = part + 64 * (size_t)s;
+    const double* op = sh.part;
     if (threadIdx.x < 6) {
       const int k = threadIdx.x;
       double before = ((op[k] + op[8 + k]) + op[16 + k]) + op[24 + k];
@@ -729,7 +744,7 @@ __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& 
 
 __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, const long long* win,
                                               const unsigned char* winner, const int* limit, const double* P, EP ep,
-                                              EPD epd, PosDW X, NLView nl, double* part, double* dpn, float* dpf,
+                                              EPD epd, PosDW X, NLView nl, double* dpn, float* dpf,
                                               const float4* __restrict__ sctf) {
   __shared__ DeltaShared sh;
   const int s = blockIdx.x;
@@ -738,7 +753,7 @@ __global__ void __launch_bounds__(64, 12) k_delta(TopoW t, const FlipState* st, 
     if (threadIdx.x == 0) dpf[8 * (size_t)s + 7] = 0.0f;
     return;
   }
-  delta_slot(s, sh, t, st, win, P, ep, epd, X, nl, part, dpn, dpf, sctf);
+  delta_slot(s, sh, t, st, win, P, ep, epd, X, nl, dpn, dpf, sctf);
 }
 
 // Metropolis with T = 1 in slot order (flips.cpp:142-160): slot s is tried on
@@ -1090,7 +1105,6 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   DevBuf<long long>& pend = e->fw_pend;
   DevBuf<unsigned char>& winner = e->fw_winner;
   DevBuf<int>& accl = e->fw_accl;
-  DevBuf<double>& part = e->fw_part;
   DevBuf<double>& dpn = e->fw_dpn;
   DevBuf<float>& dpf = e->fw_dpf;
   owner.ensure(std::max(m->nv, 1));
@@ -1098,7 +1112,6 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   pend.ensure(MAXB);
   winner.ensure(MAXB);
   accl.ensure(MAXB);
-  part.ensure(64 * (size_t)MAXB);
   dpn.ensure(8 * (size_t)MAXB);
   dpf.ensure(8 * (size_t)MAXB);
   e->fw_state.ensure(sizeof(FlipState));
@@ -1140,9 +1153,11 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       attr[0].val.cooperative = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      TM_CUDA(cudaLaunchKernelEx(&cfg, k_claim_win, t, (const FlipState*)st, mode, (const long long*)win.get(),
+      TM_CUDA(cudaLaunchKernelEx(&cfg, k_claim_win, t, st, B, mode, (const long long*)pend.get(), win.get(),
                                  owner.get(), winner.get(), limit.get()));
     } else {
+      k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st, win.get(), limit.get());
+      TM_LAUNCH();
       k_claim<<<ncw, 64, 0, s>>>(t, st, win.get(), owner.get());
       TM_LAUNCH();
       k_winner<<<ncw, 64, 0, s>>>(t, st, mode, win.get(), owner.get(), winner.get(), limit.get());
@@ -1151,11 +1166,9 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
   };
   auto launch_group = [&](bool coop) {
     for (int k = 0; k < GROUP; ++k) {
-      k_fill<<<nblk(B, 256), 256, 0, s>>>(B, pend.get(), st, win.get(), limit.get());
-      TM_LAUNCH();
       claim_win(coop);
-      k_delta<<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), P, ep, epd, X, nlv, part.get(),
-                               dpn.get(), dpf.get(), e->sctf.get());
+      k_delta<<<B, 64, 0, s>>>(t, st, win.get(), winner.get(), limit.get(), P, ep, epd, X, nlv, dpn.get(),
+                               dpf.get(), e->sctf.get());
       TM_LAUNCH();
       k_metro<<<1, MB, 0, s>>>(win.get(), winner.get(), dpn.get(), dpf.get(), fe, fg, st, limit.get(), accl.get(),
                                pend.get());
@@ -1171,7 +1184,7 @@ static int flip_sweep(tm_mesh* m, tm_energy* e, const double* P, double ratio, u
       const unsigned char* b = static_cast<const unsigned char*>(p);
       key.insert(key.end(), b, b + n);
     };
-    const void* ptrs[] = {P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(), part.get(),
+    const void* ptrs[] = {P, st, win.get(), pend.get(), limit.get(), owner.get(), winner.get(),
                           dpn.get(), dpf.get(), accl.get(), e->sctf.get(), X.p, m->d_to.get(),
                           m->d_next.get(), m->d_face.get(), m->d_vout.get(), m->d_fhe.get(), m->d_slot.get(),
                           m->d_nbr.get(), m->d_val.get(), m->d_fv.get(), m->d_edge.get()};

@@ -222,7 +222,7 @@ struct tm_energy {
   tmg::DevBuf<int> fw_owner, fw_limit, fw_accl;
   tmg::DevBuf<long long> fw_win, fw_pend;
   tmg::DevBuf<unsigned char> fw_winner, fw_state;
-  tmg::DevBuf<double> fw_part, fw_dpn;
+  tmg::DevBuf<double> fw_dpn;
   tmg::DevBuf<float> fw_dpf;
   cudaStream_t stream = nullptr;
   // second stream: the repulsion pass runs there, concurrent with the
