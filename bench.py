@@ -38,11 +38,11 @@ fp32_stencil, df64_stencil   the other stencil precisions: time and error
 surrogate_force the learned force: time, and its tensor-core FLOP rate
 level6          the 40,962-vertex evaluation loop, GPU and CPU
 batch_replicas  64 membranes of 642-40,962 vertices in one batch
-hmc_chain       device chains (HMC move + flip sweep) from a shared
-                equilibrated start (L-BFGS + flip rounds to the 0.65 volume
-                target, long-trajectory heating): per-move times,
-                acceptance, ESS/s of the bending energy and the reduced
-                volume, quarter means and a drift test of the bending trace
+hmc_chain       device chains (HMC move + flip sweep, 2,000 steps) from the
+                committed equilibrated state of the 0.65-target membrane:
+                per-move times, acceptance, ESS/s of the bending energy and
+                the reduced volume, quarter means and a drift test of the
+                bending trace
 """
 import argparse
 import json
@@ -391,13 +391,19 @@ def batch_leg(stream, n_per_level=16, levels=(3, 4, 5, 6), n_leapfrog=10, n_step
 def chain_state(stream):
     """The chains' workload and start: the 163,842-vertex membrane with the
     very-large-mesh energy (reduced-volume target 0.65 of the input sphere's
-    volume at its area), brought to that target by rounds of device L-BFGS
-    and flip sweeps, then heated at T 1 by long-trajectory HMC moves
-    (equilibrated_state), so that the measured chains sample at
-    equilibrium instead of relaxing the sphere's collapse."""
+    volume at its area) at equilibrium: the state saved by
+    ``python -m trimem_gb300.mc.equilibrate`` (the sphere brought to the
+    volume target by rounds of device L-BFGS and flip sweeps, heated by
+    long-trajectory HMC moves, then 30,000 steps of the chains' own moves)
+    when it is present, else equilibrated_state alone (its chains then still
+    relax slowly: the drift test shows it)."""
     from trimem_gb300.mc.device import equilibrated_state
+    from trimem_gb300.mc.equilibrate import load_state
 
     p, f, prm = workload()
+    st = load_state(prm, len(p))
+    if st is not None:
+        return st
     return equilibrated_state(p, f, prm, stream=stream)
 
 
@@ -534,16 +540,24 @@ def run_profile(args):
         return
     if args.profile_flips:
         # sweeps of ratio 0.2 (98,304 proposals, windows of 4,096) on the
-        # benchmark membrane as constructed (area and volume targets at that
-        # state); each sweep timed with CUDA events on its stream
-        prm0 = dict(prm, cont_lambda=0.0)
-        mesh = capi.Mesh(p, f)
-        en = capi.Energy(mesh, capi.params(**prm0))
+        # chains' equilibrated membrane, each after one HMC move; the sweeps
+        # run inside the NVTX range "flip_sweeps" (ncu --nvtx-include
+        # "flip_sweeps/" captures only them) and are timed with CUDA events
+        # on their stream
+        from trimem_gb300.mc.device import DeviceChain
+
         side = torch.cuda.Stream()
         sp = ctypes.c_void_p(side.cuda_stream)
+        state = chain_state(side.cuda_stream)
+        mesh, en, x = _chain_handles(state, 2)
         capi.check(L.tm_energy_update_repulsion_device(en.h, mesh.h, ctypes.c_void_p(x.data_ptr()), sp))
+        ch = DeviceChain(mesh, en, x, dt=state["info"]["warm_dt"], n_leapfrog=20, flip_ratio=0.0, seed=3,
+                         stream=side.cuda_stream)
         ms, accs = [], []
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("flip_sweeps")
         for k in range(args.profile_flips):
+            ch.step()
             acc = ctypes.c_int32()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(side)
@@ -553,6 +567,7 @@ def run_profile(args):
             torch.cuda.synchronize()
             ms.append(a.elapsed_time(b))
             accs.append(acc.value)
+        torch.cuda.nvtx.range_pop()
         print("profile flip sweeps done:", args.profile_flips, "ms per sweep:", [round(v, 3) for v in ms],
               "accepted:", accs)
         return
@@ -582,7 +597,8 @@ def main():
     ap.add_argument("--profile-surrogate", type=int, default=0,
                     help="only run this many surrogate force evaluations (for ncu captures) and exit")
     ap.add_argument("--profile-flips", type=int, default=0,
-                    help="only run this many flip sweeps (ratio 0.2) (for ncu captures) and exit")
+                    help="only run this many flip sweeps (ratio 0.2) on the chains' equilibrated membrane "
+                         "(for ncu captures) and exit")
     ap.add_argument("--profile-batch", type=int, default=0,
                     help="only run this many HMC steps of the 64-replica batch (for ncu captures) and exit")
     ap.add_argument("--cpu-sample", type=float, default=0.0,

@@ -126,24 +126,28 @@ def test_surrogate_hmc_step_uses_the_exact_hamiltonian(C):
 @pytest.fixture(scope="module")
 def eq065(C):
     """The learned-surrogate chains' state: the 163,842-vertex benchmark
-    membrane brought to the reduced-volume target 0.65 (one of the training
-    volumes) and heated at T 1 (equilibrated_state, ~35 s)."""
+    membrane at the reduced-volume target 0.65 (one of the training volumes)
+    in equilibrium at T 1 (the committed chain state; else equilibrated_state,
+    about a minute)."""
     from trimem_gb300 import surrogate as S
     from trimem_gb300.mc.device import equilibrated_state
+    from trimem_gb300.mc.equilibrate import load_state
     from trimem_gb300.workloads import workload_params as wp
 
     if not __import__("os").path.exists(S.WEIGHTS_L7):
         pytest.skip("no trained weights")
     p, f = meshgen.jittered_icosphere(7, seed=0)
     prm = wp(p, f, kappa_b=20.0, vfrac=0.65)
-    return equilibrated_state(p, f, prm, seed=4242)
+    st = load_state(prm, len(p))
+    return st if st is not None else equilibrated_state(p, f, prm, seed=4242)
 
 
 def _handles(C, st):
     import torch
 
     mesh = C.Mesh(st["x"], st["faces"])
-    mesh.set_topology(st["topo"])
+    if st["topo"] is not None:
+        mesh.set_topology(st["topo"])
     en = C.Energy(mesh, C.params(**st["prm"]))
     en.set_initial_props(st["initial"])
     x = torch.tensor(st["x"], dtype=torch.float64, device="cuda").contiguous()

@@ -125,7 +125,7 @@ def tune_dt(mesh, energy, x, candidates=(5e-5, 2e-5, 1e-5, 5e-6, 2e-6, 1e-6), n_
     return candidates[-1], seen
 
 
-def equilibrated_state(p, f, prm, rounds=8, maxiter=3000, sweeps=3, warm_steps=100, heat_steps=200,
+def equilibrated_state(p, f, prm, rounds=12, maxiter=4000, sweeps=3, warm_steps=100, heat_steps=300,
                        heat_leapfrog=200, dt_candidates=(5e-6, 2e-6, 1e-6, 5e-7, 2e-7), seed=1000, stream=None):
     """A start for chains that sample at equilibrium, from the input mesh
     (p, f) whose energy targets (area, volume: fractions of the input's) may
