@@ -239,9 +239,10 @@ VOLUMES = (0.65, 0.75, 0.85)
 
 def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, max_valence=16, log=print):
     """Training states: for each reduced volume, the 163,842-vertex membrane
-    (level-7 icosphere, kb 20, the other parameters of the benchmark)
-    brought to that volume target and heated by equilibrated_state (the
-    start of the benchmark's chains), then a plain device HMC chain (20
+    (level-7 icosphere, kb 20, the other parameters of the benchmark) at
+    that volume target: the committed equilibrated chain state where one
+    exists for it (the benchmark chains' start), else brought to the target
+    and heated by equilibrated_state; then a plain device HMC chain (20
     velocity-Verlet steps at the warm-up's time step + a flip sweep of ratio
     0.2 per step) whose every `every`-th state gives one snapshot: the
     network inputs and the target g_local - g_exact.  Everything stays in
@@ -249,6 +250,7 @@ def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, m
     torch = _torch()
     from . import capi, meshgen
     from .mc.device import DeviceChain, equilibrated_state
+    from .mc.equilibrate import load_state
     from .workloads import workload_params
 
     p, f = meshgen.jittered_icosphere(level, seed=0)
@@ -259,9 +261,12 @@ def generate(n_per_volume, volumes=VOLUMES, every=2, burn=10, level=7, seed=5, m
     for vi, v in enumerate(volumes):
         prm = workload_params(p, f, kappa_b=20.0, vfrac=v)
         t0 = time.perf_counter()
-        st = equilibrated_state(p, f, prm, seed=1000 + 100 * vi)
+        st = load_state(prm, len(p))  # the committed equilibrated state (0.65 target)
+        if st is None:
+            st = equilibrated_state(p, f, prm, seed=1000 + 100 * vi)
         mesh = capi.Mesh(st["x"], st["faces"])
-        mesh.set_topology(st["topo"])
+        if st["topo"] is not None:
+            mesh.set_topology(st["topo"])
         en = capi.Energy(mesh, capi.params(**prm))
         en.set_initial_props(st["initial"])
         if scales is None:
