@@ -1086,23 +1086,27 @@ static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, 
   int ne = m.ne();
   long nflips = (long)(ne * ratio);
   Props props = E.properties(m);
-  // Metropolis energy as the device's flip_energy: reciprocals of the
-  // reference properties instead of divisions, same summation order
+  // the Metropolis energy change E(props - dp) - E(props) as the device's
+  // flip_delta: the penalty energy (src/kernel.h:110-122) with the
+  // reciprocals of the reference properties instead of divisions, written
+  // without cancellation (k t (t - 2 d0) for the quadratic penalties,
+  // d0 = props/ref - 1, t = dp/ref; -k dp for the linear terms), the same
+  // operations in the same order
   const Props ref = E.ref_props();
   const double irA = 1.0 / ref.area, irV = 1.0 / ref.volume, irC = 1.0 / ref.curvature;
   const om_params& q = E.prm;
-  auto flip_energy = [&](const Props& p) {
-    double da = p.area * irA - 1.0, dv = p.volume * irV - 1.0, dc = p.curvature * irC - 1.0;
-    double tot = 0.0;
-    tot += q.kappa_a * da * da;
-    tot += q.kappa_v * dv * dv;
-    tot += q.kappa_c * dc * dc;
-    tot += q.kappa_t * p.tethering;
-    tot += q.kappa_r * p.repulsion;
-    tot += q.kappa_b * p.bending;
-    return tot;
+  auto flip_delta = [&](const Props& p, const Props& dp) {
+    const double da = p.area * irA - 1.0, dv = p.volume * irV - 1.0, dc = p.curvature * irC - 1.0;
+    const double ta = dp.area * irA, tv = dp.volume * irV, tc = dp.curvature * irC;
+    double de = 0.0;
+    de += q.kappa_a * ta * (ta - 2.0 * da);
+    de += q.kappa_v * tv * (tv - 2.0 * dv);
+    de += q.kappa_c * tc * (tc - 2.0 * dc);
+    de -= q.kappa_t * dp.tethering;
+    de -= q.kappa_r * dp.repulsion;
+    de -= q.kappa_b * dp.bending;
+    return de;
   };
-  double e0 = flip_energy(props);
   // per vertex: the lowest slot of the window whose patch claims it
   std::vector<int> owner(m.nv(), std::numeric_limits<int>::max());
   std::vector<long> pending;
@@ -1203,13 +1207,8 @@ static int flip_windowed(Mesh& m, const Energy& E, double ratio, uint64_t seed, 
     // E(props - dp) - E <= -log(u) (the device's k_metro decides the same)
     for (int s = 0; s < limit; ++s) {
       if (!ok[s]) continue;
-      Props trial = props;
-      trial -= dps[s];
-      double en = flip_energy(trial);
-      double de = en - e0;
-      if (de <= -std::log(flip_u_of(seed, win[s]))) {
-        props = trial;
-        e0 = en;
+      if (flip_delta(props, dps[s]) <= -std::log(flip_u_of(seed, win[s]))) {
+        props -= dps[s];
         acc += 1;
         m.flip(flip_edge_of(seed, win[s], ne));
       }

@@ -97,7 +97,6 @@ __device__ __forceinline__ double flip_u_of(unsigned long long seed, long long p
 // other without the host; W = 0 once every proposal is decided.
 struct FlipState {
   double props[8];
-  double e0;
   unsigned long long seed;  // proposal stream of the sweep
   int nacc_win;             // accepted slots of the current window (listed in order)
   float sq[4];  // float-filter constants of props (filter_state)
@@ -226,48 +225,49 @@ struct TableExclW {
 
 
 // ---- window kernels --------------------------------------------------------
-// Energy of a property set for the Metropolis test: the penalty energy of
-// src/kernel.h:110-122 in its summation order, with the reciprocals of the
-// reference properties (rounded once on the host) in place of divisions.
+// The Metropolis test's energy change E(props - dp) - E(props) for the
+// penalty energy of src/kernel.h:110-122, with the reciprocals of the
+// reference properties (rounded once on the host) in place of divisions,
+// written without cancellation: the quadratic penalties as k t (t - 2 d0)
+// with d0 = props/ref - 1 of the current state and t = dp/ref, the linear
+// terms as -k dp.  Equal to the difference of the two energies in exact
+// arithmetic; in FP64 its rounding is relative to the change's own terms,
+// while the difference of two totals carries the totals' rounding (an
+// unrelaxed membrane's energy reaches 1e12, whose last bit is 1e-4).  The
+// CPU port of the sweep evaluates the same expression.
 struct FlipE {
   double irA, irV, irC, ka, kv, kc, kt, kr, kb;
 };
-__device__ __forceinline__ double flip_energy(const FlipE& f, const double* p) {
-  double da = p[0] * f.irA - 1.0, dv = p[1] * f.irV - 1.0, dc = p[2] * f.irC - 1.0;
-  double tot = 0.0;
-  tot += f.ka * da * da;
-  tot += f.kv * dv * dv;
-  tot += f.kc * dc * dc;
-  tot += f.kt * p[4];
-  tot += f.kr * p[5];
-  tot += f.kb * p[3];
-  return tot;
+__device__ __forceinline__ double flip_delta(const FlipE& f, const double* p, const double* dp) {
+  const double da = p[0] * f.irA - 1.0, dv = p[1] * f.irV - 1.0, dc = p[2] * f.irC - 1.0;
+  const double ta = dp[0] * f.irA, tv = dp[1] * f.irV, tc = dp[2] * f.irC;
+  double de = 0.0;
+  de += f.ka * ta * (ta - 2.0 * da);
+  de += f.kv * tv * (tv - 2.0 * dv);
+  de += f.kc * tc * (tc - 2.0 * dc);
+  de -= f.kt * dp[4];
+  de -= f.kr * dp[5];
+  de -= f.kb * dp[3];
+  return de;
 }
 
-// Float filter of the Metropolis test E(props - dp) - E(props) <= -log u
-// (k_metro): the energy change is written without cancellation (quadratic
-// penalties as k t (t - 2 d0), d0 = props/ref - 1 of the current state,
-// t = dp/ref; the linear terms as -k dp) and evaluated from float copies.
+// Float filter of the same test (k_metro), from float copies of dp and of
+// the state's d0
 struct FlipEF {
   float irA, irV, irC, ka, kv, kc, kt, kr, kb;
 };
-// per-state constants of the filter: d0 of area, volume, curvature and the
-// FP64 rounding bound of the exact test (1e-12 of the energy's magnitude)
+// per-state constants of the filter: d0 of area, volume and curvature
 __device__ __forceinline__ void filter_state(const FlipE& f, const double* p, float* q) {
-  double da = p[0] * f.irA - 1.0, dv = p[1] * f.irV - 1.0, dc = p[2] * f.irC - 1.0;
-  double mag = fabs(f.ka * da * da) + fabs(f.kv * dv * dv) + fabs(f.kc * dc * dc) + fabs(f.kt * p[4]) +
-               fabs(f.kr * p[5]) + fabs(f.kb * p[3]);
-  q[0] = (float)da;
-  q[1] = (float)dv;
-  q[2] = (float)dc;
-  q[3] = (float)(1e-12 * mag);
+  q[0] = (float)(p[0] * f.irA - 1.0);
+  q[1] = (float)(p[1] * f.irV - 1.0);
+  q[2] = (float)(p[2] * f.irC - 1.0);
+  q[3] = 0.0f;
 }
 
 __global__ void k_flip_init(FlipE fe, const Globals* g, long long nflips, unsigned long long seed, FlipState* st) {
   if (threadIdx.x || blockIdx.x) return;
   st->seed = seed;
   for (int k = 0; k < 6; ++k) st->props[k] = g->props[k];
-  st->e0 = flip_energy(fe, st->props);
   filter_state(fe, st->props, st->sq);
   st->next_new = 0;
   st->nn_next = 0;
@@ -495,7 +495,7 @@ __device__ __noinline__ bool fold_sign_fp64(const double* P, int v, int j, int k
 // that band) the sign comes from fold_sign_fp64.
 __device__ void ring_terms_dw(const PosDW& X, const double* P, const EP& ep, const EPD& epd,
                               const float4* __restrict__ sctf, int v, const int* sr, const unsigned char* sf, int n,
-                              int w8, int gbase, unsigned gmask, double* o) {
+                              int w8, int gbase, unsigned gmask, float2* o) {
   const df3 xw = X.at(v);
   const df zero = df_make(0.0f);
   const df3 zero3 = {zero, zero, zero};
@@ -595,11 +595,13 @@ __device__ void ring_terms_dw(const PosDW& X, const double* P, const EP& ep, con
   }
   if (w8 == 0) {
     const df A = mul_s(sa, third()), C = half(sc);
-    o[0] = df_to(A);
-    o[1] = df_to(mul_s(sv, third()));
-    o[2] = df_to(C);
-    o[3] = df_to(ldexp2(mul_s(mul_s(C, C), rcp_dw(A)), 2.0f));
-    o[4] = df_to(mul_s(stt, epd.inv_tdiv));
+    const df Vv = mul_s(sv, third()), B = ldexp2(mul_s(mul_s(C, C), rcp_dw(A)), 2.0f);
+    const df T = mul_s(stt, epd.inv_tdiv);
+    o[0] = make_float2(A.hi, A.lo);
+    o[1] = make_float2(Vv.hi, Vv.lo);
+    o[2] = make_float2(C.hi, C.lo);
+    o[3] = make_float2(B.hi, B.lo);
+    o[4] = make_float2(T.hi, T.lo);
   }
 }
 
@@ -617,7 +619,7 @@ __device__ void ring_terms_dw(const PosDW& X, const double* P, const EP& ep, con
 // the CPU port's by its summation orders: a Metropolis decision could
 // differ only where E(trial) - E lies within that rounding of -log(u).
 struct DeltaShared {
-  double part[64];  // per variant: area, volume, curvature, bending, tether, repulsion
+  float2 part[64];  // per variant, as double-words: area, volume, curvature, bending, tether, repulsion
   int sr[8][TM_MAXVAL + 1];
   unsigned char sf[8][TM_MAXVAL + 1];
   int sn[8];
@@ -698,7 +700,7 @@ __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& 
   }
   __syncthreads();
   const int n = sh.sn[sub];
-  double* o = sh.part + 8 * sub;
+  float2* o = sh.part + 8 * sub;
   ring_terms_dw(X, P, ep, epd, sctf, v, sh.sr[sub], sh.sf[sub], n, w8, gbase, gmask, o);
   // repulsion: the near row shared by the variant's 8 lanes, else one lane
   // walks the cell list
@@ -715,21 +717,26 @@ __device__ __forceinline__ void delta_slot(int s, DeltaShared& sh, const TopoW& 
       near = repulsion_near8(v, xv, P, ep, nl, x, w8, gmask, sh.rkey[sub], sh.rval[sub], sh.rterm[sub], &pot);
       if (!near && w8 == 0) pot = repulsion_of(v, xv, P, ep, nl, x);
     }
-    if (w8 == 0) o[5] = pot;
+    if (w8 == 0) {
+      float ph, pl;
+      split_bits(pot, &ph, &pl);
+      o[5] = make_float2(ph, pl);
+    }
   }
   __syncthreads();
   // the property change of the flip (before - after, in the summation orders
   // of edge_vertex_properties before (va0, va1, vb0, vb1) and after the flip
   // (va1, vb0, vb1, va0)): lane k of warp 0 takes property k
   if (threadIdx.x < 32) {
-    const double* op = sh.part;
+    const float2* op = sh.part;
     if (threadIdx.x < 6) {
       const int k = threadIdx.x;
-      double before = ((op[k] + op[8 + k]) + op[16 + k]) + op[24 + k];
-      double after = ((op[40 + k] + op[48 + k]) + op[56 + k]) + op[32 + k];
-      const double dk = before - after;
-      dpn[8 * (size_t)s + k] = dk;
-      dpf[8 * (size_t)s + k] = (float)dk;
+      auto at = [&](int q) { return df{op[q].x, op[q].y}; };
+      const df before = add_s(add_s(add_s(at(k), at(8 + k)), at(16 + k)), at(24 + k));
+      const df after = add_s(add_s(add_s(at(40 + k), at(48 + k)), at(56 + k)), at(32 + k));
+      const df dk = sub_s(before, after);
+      dpn[8 * (size_t)s + k] = df_to(dk);
+      dpf[8 * (size_t)s + k] = __fadd_rn(dk.hi, dk.lo);
     }
     if (threadIdx.x == 0) {
       // -log(u) in float for the filter (NaN below float range: the FP64
@@ -882,7 +889,7 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
                     fabsf(fg.kc * tc) * (fabsf(tc) + 2.0f * fabsf(q[2])) + fabsf(fg.kt * f8[4]) +
                     fabsf(fg.kr * f8[5]) + fabsf(fg.kb * f8[3]);
     const float shift = 2.0f * (fabsf(fg.ka * ta) * ba + fabsf(fg.kv * tv) * bv + fabsf(fg.kc * tc) * bc);
-    const float m = 1e-4f * S + 2.0f * q[3] + 1e-6f * fabsf(f8[6]) + 2e-7f + 1.01f * shift;
+    const float m = 1e-4f * S + 1e-6f * fabsf(f8[6]) + 2e-7f + 1.01f * shift;
     const float d = ((xa + xv) + xc - xl) - f8[6];
     cls[k] = d < -m ? ACCEPT : (d > m ? REJECT : OPEN);  // NaN or overflow: OPEN
     if (cls[k] >= ACCEPT) ++nopen;
@@ -909,25 +916,20 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
     // every listed slot is a robust acceptance (the common case: the float
     // filter leaves a slot undecided only within about 1e-4 of its terms of
     // the threshold): the state moves by the sum of their changes, taken by
-    // a fixed-order block reduction instead of one thread's chain of FP64
+    // a fixed-order warp reduction instead of one thread's chain of FP64
     // subtractions (the FP64 pipe's latency makes that chain the window's
-    // longest wait).  The state differs from the ordered walk's by rounding
-    // (1e-16 relative), which an FP64 test of a later window could feel
-    // only for |E(trial) - E + log u| of that order.
-    double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int i = tid; i < tot.x; i += MB) {
-      const int c = lst[i];
-      for (int k = 0; k < 6; ++k) a[k] += dpn[8 * (size_t)c + k];
-      accl[i] = c;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-      for (int k = 0; k < 6; ++k) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
-    if (lane == 0)
-      for (int k = 0; k < 6; ++k) sdp[w][k] = a[k];
-    __syncthreads();
+    // longest wait); one warp, since a window accepts tens of flips and
+    // FP64 work of more warps would only queue on this SM's FP64 pipe.  The
+    // state differs from the ordered walk's by rounding (1e-16 relative),
+    // which an FP64 test of a later window could feel only for
+    // |E(trial) - E + log u| of that order.
     if (w == 0) {
-      for (int k = 0; k < 6; ++k) a[k] = sdp[lane][k];
+      double a[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+      for (int i = lane; i < tot.x; i += 32) {
+        const int c = lst[i];
+        for (int k = 0; k < 6; ++k) a[k] += dpn[8 * (size_t)c + k];
+        accl[i] = c;
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1)
         for (int k = 0; k < 6; ++k) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
@@ -935,7 +937,6 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
         double sP[6];
         for (int k = 0; k < 6; ++k) sP[k] = st->props[k] - a[k];
         if (tot.x > 0) {
-          st->e0 = flip_energy(fe, sP);
           for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
           filter_state(fe, sP, st->sq);
         }
@@ -956,15 +957,11 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
     sdp[tid][6] = c >= 0 ? 0.0 : -log(flip_u_of(seed, win[s]));
   }
   __syncthreads();
-  // phase 2: one thread walks the listed slots in order on the FP64 state.
-  // The state's energy is needed only by an FP64 test and at the end, so
-  // after robust acceptances it is computed when next needed (flip_energy of
-  // the same state: the value that computing it at every acceptance gives).
+  // phase 2: one thread walks the listed slots in order on the FP64 state:
+  // the robustly accepted ones move it, the undecided ones are tested first
   if (tid == 0) {
     double sP[6];
     for (int k = 0; k < 6; ++k) sP[k] = st->props[k];
-    double se0 = st->e0;
-    bool fresh = true;
     int sacc = st->acc, nacc = 0;
     for (int i = 0; i < tot.x; ++i) {
       const int c = lst[i];
@@ -977,30 +974,15 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
         for (int k = 0; k < 6; ++k) o8[k] = dpn[8 * (size_t)s + k];
         o8[6] = robust ? 0.0 : -log(flip_u_of(seed, win[s]));
       }
-      double trial[6];
-      for (int k = 0; k < 6; ++k) trial[k] = sP[k] - o8[k];
-      if (robust) {
-        for (int k = 0; k < 6; ++k) sP[k] = trial[k];
-        fresh = false;
-        sacc += 1;
-        accl[nacc++] = s;
-        continue;
-      }
-      if (!fresh) se0 = flip_energy(fe, sP);
-      fresh = true;
-      const double en = flip_energy(fe, trial);
-      if (en - se0 <= o8[6]) {
-        for (int k = 0; k < 6; ++k) sP[k] = trial[k];
-        se0 = en;
+      if (robust || flip_delta(fe, sP, o8) <= o8[6]) {
+        for (int k = 0; k < 6; ++k) sP[k] = sP[k] - o8[k];
         sacc += 1;
         accl[nacc++] = s;
       }
     }
-    if (!fresh) se0 = flip_energy(fe, sP);
     st->nacc_win = nacc;
     for (int k = 0; k < 6; ++k) st->props[k] = sP[k];
     filter_state(fe, sP, st->sq);
-    st->e0 = se0;
     st->acc = sacc;
     st->npend = tot.y;
     st->next_new = st->nn_next;
