@@ -931,13 +931,12 @@ def main():
             except Exception as exc:
                 cb["chain_step"] = {"error": f"{type(exc).__name__}: {exc}"}
 
-    # this library's kernels per step: 9 per double-word evaluation (k_split_dw,
-    # k_face_dw, k_edge_dw, k_bond_short_dw, k_moved, k_rep_fast, k_rep_slow,
-    # k_vertex_dw, k_grad_dw) and 14
-    # per cell-list rebuild (box 2, table 1, insert 1, counts 1, scan 3,
-    # starts 1, scatter 1, sort 1, near-row check / build / done 3); the
-    # displacement and L2-flush kernels are torch's
-    launches_per_step = 9 * EVALS_PER_STEP + 14
+    # this library's kernels per step: 8 per double-word evaluation (k_split_dw,
+    # k_face_dw, k_edge_dw, k_moved, k_rep_fast, k_rep_slow, k_vertex_dw,
+    # k_grad_dw) and 14 per cell-list rebuild (box 2, table 1, insert 1,
+    # counts 1, scan 3, starts 1, scatter 1, sort 1, near-row check / build /
+    # done 3); the displacement and L2-flush kernels are torch's
+    launches_per_step = 8 * EVALS_PER_STEP + 14
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

@@ -81,50 +81,6 @@ __global__ void __launch_bounds__(256) k_face_dw(Topo t, PosDW X, float4* __rest
   fav[f] = make_float4(A.hi, A.lo, V.hi, V.lo);
 }
 
-// elt: (l theta, bond value) as (hi, lo, hi, lo), compact for k_vertex_dw
-// (the bond value of short edges is filled in by k_bond_short_dw)
-__global__ void __launch_bounds__(256) k_edge_dw(Topo t, PosDW X, const float4* __restrict__ fd,
-                                                float4* __restrict__ ed, float4* __restrict__ elt, EP ep, EPD epd,
-                                                int* __restrict__ blist, int* __restrict__ bcnt,
-                                                const float4* __restrict__ sct) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= t.ne) return;
-  const int4 E = t.edge[e];
-  const df3 ev = sub3(X.at(E.y), X.at(E.x));
-  const df l2 = dot3(ev, ev);
-  const df il = rsqrt_dw(l2);
-  const df l = mul_s(l2, il);
-  df th = df_make(0.0f);
-  const bool interior = E.z >= 0 && E.w >= 0;
-  if (interior) {
-    const float4 a0 = __ldg(fd + 4 * (size_t)E.z), a1 = __ldg(fd + 4 * (size_t)E.z + 1);
-    const float4 b0 = __ldg(fd + 4 * (size_t)E.w), b1 = __ldg(fd + 4 * (size_t)E.w + 1);
-    const df3 n0 = {{a0.x, a0.y}, {a0.z, a0.w}, {a1.x, a1.y}};
-    const df3 n1 = {{b0.x, b0.y}, {b0.z, b0.w}, {b1.x, b1.y}};
-    // n0 x n1 lies along the shared edge: its projection on the unit edge
-    // is the signed sine, with the sign of the reference's test
-    // (n0 x n1) . e >= 0
-    const df sd = mul_s(dot3(cross3(n0, n1), ev), il);
-    th = angle_dw(sd, dot3(n0, n1), sct);
-  }
-  // flat-bottom edge penalty: above the flat bottom inline (products only),
-  // below it (exp) through the short-edge list
-  df val = df_make(0.0f), db = df_make(0.0f);
-  const bool shortb = ep.btype == 0 && df_less(l, epd.lc1);
-  if (ep.btype == 0 && !shortb && df_less(epd.lc0, l) && ep.r >= 1) {
-    const df d = sub_s(l, epd.lc0);
-    const df dr1 = ipow_dw(d, ep.r - 1);
-    val = mul_s(epd.br1, mul_s(dr1, d));
-    db = mul_s(epd.br2, dr1);
-  }
-  warp_append(shortb, e, blist, bcnt);
-  const df ils = interior ? il : neg(il);
-  ed[2 * (size_t)e] = make_float4(l.hi, l.lo, th.hi, th.lo);
-  ed[2 * (size_t)e + 1] = make_float4(db.hi, db.lo, ils.hi, ils.lo);
-  const df lt = mul_s(l, th);
-  elt[e] = make_float4(lt.hi, lt.lo, val.hi, val.lo);
-}
-
 // Flat-bottom bond of an edge shorter than lc1 (src/mesh_tether.h:29-85)
 // in double-word arithmetic: value e^(l/(l-lc1)) / l^r, derivative
 // -(lc1/(l-lc1)^2 + r/l) e^(l/(l-lc1)) / l^r (plus the l > lc0 branch when
@@ -147,28 +103,58 @@ __device__ __forceinline__ void edge_bond_short_dw(const EP& ep, const EPD& epd,
   *fac = mul_s(mul_s(f, ilr), ex);
 }
 
-__global__ void k_bond_short_dw(float4* __restrict__ ed, float4* __restrict__ elt, EP ep, EPD epd,
-                                const int* __restrict__ blist, const int* __restrict__ bcnt) {
-  const int n = *bcnt;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const int e = blist[i];
-    const float4 r0 = ed[2 * (size_t)e];
-    const df l = {r0.x, r0.y};
-    df val, fac;
+// elt: (l theta, bond value) as (hi, lo, hi, lo), compact for k_vertex_dw
+__global__ void __launch_bounds__(256) k_edge_dw(Topo t, PosDW X, const float4* __restrict__ fd,
+                                                float4* __restrict__ ed, float4* __restrict__ elt, EP ep, EPD epd,
+                                                const float4* __restrict__ sct) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= t.ne) return;
+  const int4 E = t.edge[e];
+  const df3 ev = sub3(X.at(E.y), X.at(E.x));
+  const df l2 = dot3(ev, ev);
+  const df il = rsqrt_dw(l2);
+  const df l = mul_s(l2, il);
+  df th = df_make(0.0f);
+  const bool interior = E.z >= 0 && E.w >= 0;
+  if (interior) {
+    const float4 a0 = __ldg(fd + 4 * (size_t)E.z), a1 = __ldg(fd + 4 * (size_t)E.z + 1);
+    const float4 b0 = __ldg(fd + 4 * (size_t)E.w), b1 = __ldg(fd + 4 * (size_t)E.w + 1);
+    const df3 n0 = {{a0.x, a0.y}, {a0.z, a0.w}, {a1.x, a1.y}};
+    const df3 n1 = {{b0.x, b0.y}, {b0.z, b0.w}, {b1.x, b1.y}};
+    // n0 x n1 lies along the shared edge: its projection on the unit edge
+    // is the signed sine, with the sign of the reference's test
+    // (n0 x n1) . e >= 0
+    const df sd = mul_s(dot3(cross3(n0, n1), ev), il);
+    th = angle_dw(sd, dot3(n0, n1), sct);
+  }
+  // flat-bottom edge penalty: above the flat bottom products only, below it
+  // the exponential (a warp with any short edge takes that branch; on the
+  // jittered benchmark membrane nearly every warp has one, which costs less
+  // than a list of short edges and a kernel of their own)
+  df val = df_make(0.0f), db = df_make(0.0f);
+  const bool shortb = ep.btype == 0 && df_less(l, epd.lc1);
+  if (ep.btype == 0 && !shortb && df_less(epd.lc0, l) && ep.r >= 1) {
+    const df d = sub_s(l, epd.lc0);
+    const df dr1 = ipow_dw(d, ep.r - 1);
+    val = mul_s(epd.br1, mul_s(dr1, d));
+    db = mul_s(epd.br2, dr1);
+  }
+  if (shortb) {
     if (ep.r >= 1) {
-      edge_bond_short_dw(ep, epd, l, &val, &fac);
+      edge_bond_short_dw(ep, epd, l, &val, &db);
     } else {  // non-positive exponents: FP64
       double v, f;
       const double ld = df_to(l);
       edge_bond(ep, ld, 1.0 / ld, &v, &f);
       val = df_from(v);
-      fac = df_from(f);
+      db = df_from(f);
     }
-    ed[2 * (size_t)e + 1].x = fac.hi;
-    ed[2 * (size_t)e + 1].y = fac.lo;
-    elt[e].z = val.hi;
-    elt[e].w = val.lo;
   }
+  const df ils = interior ? il : neg(il);
+  ed[2 * (size_t)e] = make_float4(l.hi, l.lo, th.hi, th.lo);
+  ed[2 * (size_t)e + 1] = make_float4(db.hi, db.lo, ils.hi, ils.lo);
+  const df lt = mul_s(l, th);
+  elt[e] = make_float4(lt.hi, lt.lo, val.hi, val.lo);
 }
 
 // Per-vertex ring sums, the six properties, the curvature weights
@@ -445,12 +431,7 @@ void energy_eval_df(tm_energy* e, tm_mesh* m, const double* P, bool want_grad, d
   if (t.nf) k_face_dw<<<nblk(t.nf, 256), 256, 0, s>>>(t, X, fd, fav);
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[1], s));
-  int* blist = e->slow.get() + std::max(m->nv, 1) + 1;
-  int* bcnt = blist + std::max(m->ne, 1);
-  TM_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(int), s));
-  if (t.ne) k_edge_dw<<<nblk(t.ne, 256), 256, 0, s>>>(t, X, fd, ed, eb, ep, epd, blist, bcnt, e->sctf.get());
-  TM_LAUNCH();
-  if (t.ne) k_bond_short_dw<<<std::min(nblk(t.ne, 256), 4 * 152), 256, 0, s>>>(ed, eb, ep, epd, blist, bcnt);
+  if (t.ne) k_edge_dw<<<nblk(t.ne, 256), 256, 0, s>>>(t, X, fd, ed, eb, ep, epd, e->sctf.get());
   TM_LAUNCH();
   if (ev) TM_CUDA(cudaEventRecord(ev[2], s));
   if (conc)
