@@ -93,13 +93,14 @@ __device__ __forceinline__ double flip_u_of(unsigned long long seed, long long p
 }
 
 // Sweep state in device memory.  A window's size W and number wid are set
-// by k_fill from the state the previous window left, so windows follow each
-// other without the host; W = 0 once every proposal is decided.
+// by the window fill (k_claim_win, or k_fill) from the state the previous
+// window left, so windows follow each other without the host; W = 0 once
+// every proposal is decided.
 struct FlipState {
   double props[8];
   unsigned long long seed;  // proposal stream of the sweep
   int nacc_win;             // accepted slots of the current window (listed in order)
-  float sq[4];  // float-filter constants of props (filter_state)
+  float sq[3];  // the filter's d0 of area, volume, curvature (filter_state)
   long long next_new;  // first proposal not yet in a window
   long long nn_next;   // next_new after the current window (committed by k_metro)
   long long nflips;
@@ -261,7 +262,6 @@ __device__ __forceinline__ void filter_state(const FlipE& f, const double* p, fl
   q[0] = (float)(p[0] * f.irA - 1.0);
   q[1] = (float)(p[1] * f.irV - 1.0);
   q[2] = (float)(p[2] * f.irC - 1.0);
-  q[3] = 0.0f;
 }
 
 __global__ void k_flip_init(FlipE fe, const Globals* g, long long nflips, unsigned long long seed, FlipState* st) {
@@ -827,8 +827,8 @@ __global__ void __launch_bounds__(MB) k_metro(const long long* win, const unsign
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int W = st->W;
   const unsigned long long seed = st->seed;
-  float q[4];
-  for (int k = 0; k < 4; ++k) q[k] = st->sq[k];
+  float q[3];
+  for (int k = 0; k < 3; ++k) q[k] = st->sq[k];
   // this thread's slots' float records (two 16-byte loads each; the
   // eligibility flag 0 for slots past the window)
   float4 fa[MS], fb[MS];
