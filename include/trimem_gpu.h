@@ -296,10 +296,12 @@ int tm_surrogate_train_status(tm_strain* t);
  * replicas whose vertex counts share a power of two); the element kernels
  * run per class with block sizes the autotuner picks for that class at
  * creation, side by side on the classes' streams, and the vertex stage and
- * repulsion run once for all replicas.  Positions live on the device in a
- * padded layout: replica r occupies vertices [offsets[r], offsets[r] +
- * n_points[r]) of [0, n_total) (see tm_batch_layout); padding vertices are
- * inert. */
+ * repulsion run once for all replicas.  The replicas share one kind of
+ * neighbour list (params[r].n_search all 0, the cell list, or all 1, the
+ * Verlet list; each at the replica's own cut-off), else TM_ERR_ARG.
+ * Positions live on the device in a padded layout: replica r occupies
+ * vertices [offsets[r], offsets[r] + n_points[r]) of [0, n_total) (see
+ * tm_batch_layout); padding vertices are inert. */
 typedef struct tm_batch tm_batch;
 int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_points, const int32_t* const* faces,
                     const int64_t* n_faces, const tm_params* params, tm_batch** out);

@@ -52,6 +52,35 @@ def test_batch_matches_single_meshes(C):
         assert abs(eb[r] - eo) <= 1e-5 * abs(eo), r
 
 
+def test_batch_with_verlet_lists_matches_single_meshes(C):
+    """The same replicas with Verlet lists (src/nlists/verlet_list.h): each
+    replica's energy and gradient equal its single-mesh evaluation with a
+    Verlet list, and a batch cannot mix the two kinds of list."""
+    reps = [(p, f, dict(prm, n_search=1)) for p, f, prm in _replicas()]
+    b = C.Batch([(p, f) for p, f, _ in reps], [C.params(**prm) for _, _, prm in reps])
+    eb, gb = b.energy(with_grad=True)
+    for r, (p, f, prm) in enumerate(reps):
+        m = C.Mesh(p, f)
+        e = C.Energy(m, C.params(**prm))
+        e.set_stencil_precision(1)
+        es, gs = e.gradient(m, with_energy=True)
+        assert abs(eb[r] - es) <= 1e-12 * abs(es), (r, eb[r], es)
+        assert np.linalg.norm(gb[r] - gs) <= 1e-12 * np.linalg.norm(gs), r
+    eo = O.Energy(O.Mesh(reps[3][0], reps[3][1]), O.default_params(**reps[3][2]))
+    assert abs(eb[3] - eo.energy(O.Mesh(reps[3][0], reps[3][1]))) <= 1e-5 * abs(eb[3])
+    mixed = [C.params(**prm) for _, _, prm in _replicas()]
+    mixed[1] = C.params(**reps[1][2])
+    with pytest.raises(RuntimeError):
+        C.Batch([(p, f) for p, f, _ in reps], mixed)
+    # HMC steps on the Verlet batch: finite, deterministic
+    acc = b.hmc(4, 5, 1e-6, seed=3)
+    b2 = C.Batch([(p, f) for p, f, _ in reps], [C.params(**prm) for _, _, prm in reps])
+    acc2 = b2.hmc(4, 5, 1e-6, seed=3)
+    assert np.array_equal(acc, acc2)
+    for x, x2 in zip(b.positions(), b2.positions()):
+        assert np.array_equal(x, x2) and np.isfinite(x).all()
+
+
 def test_batch_hmc_graph_replay_is_deterministic(C):
     reps = _replicas()
     runs = []

@@ -19,7 +19,9 @@
 // classes' streams inside the captured step, each with the block size the
 // autotuner picked for that class when the batch was created; the
 // repulsion and the vertex stage (with the per-replica reductions) run once
-// for all replicas.  Each replica keeps its own exclusion level.
+// for all replicas.  Each replica keeps its own exclusion level; the
+// replicas share the kind of neighbour list (cells, or Verlet rows built
+// from the replica-tagged cells at each replica's cut-off).
 #include <algorithm>
 #include <climits>
 #include <cmath>
@@ -250,13 +252,15 @@ static void upload_eps(tm_batch* b) {
 // once, and the cells' candidate rows, rebuilt every time, serve instead
 // (the rows never depend on the cells, and stale rows are never used).
 static void rebuild_nlist(tm_batch* b, bool near_rows = true) {
-  // near rows when every replica's cells are at least its repulsion cut-off
-  bool near = near_rows;
+  const bool verlet = b->prm[0].n_search == 1;
+  // near rows (cell lists) when every replica's cells are at least its
+  // repulsion cut-off
+  bool near = near_rows && !verlet;
   for (const tm_params& p : b->prm) near = near && p.rep_lc1 > 0 && p.rlist >= p.rep_lc1;
   int excl = 0;
   for (const tm_params& p : b->prm) excl = std::max(excl, (int)p.exclusion_level);
   nlist_make_batch(&b->en->nl, b->mesh.get(), b->R, b->vrep.get(), b->rblocks.get(), b->rlist.get(), excl,
-                   b->rexcl.get(), b->x.get(), b->stream, b->eps.get(), near);
+                   b->rexcl.get(), b->x.get(), b->stream, b->eps.get(), near, verlet);
 }
 
 // Size classes: runs of consecutive replicas whose vertex counts have the
@@ -380,7 +384,9 @@ int tm_batch_create(int n_rep, const double* const* points, const int64_t* n_poi
   std::unique_ptr<tm_batch> b(new tm_batch());
   b->R = n_rep;
   for (int r = 0; r < n_rep; ++r) {
-    if (params[r].n_search != 0) fail(TM_ERR_ARG, "batches use the cell list");
+    if (params[r].n_search != 0 && params[r].n_search != 1) fail(TM_ERR_ARG, "Unknown neighbour search algorithm.");
+    if (params[r].n_search != params[0].n_search)
+      fail(TM_ERR_ARG, "the replicas of a batch use one neighbour search (cell list or Verlet list)");
     if (params[r].bond_type != 0 && params[r].bond_type != 1) fail(TM_ERR_ARG, "Unknown bond potential");
     if (params[r].exclusion_level < 0 || params[r].exclusion_level > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
     b->prm.push_back(params[r]);

@@ -387,6 +387,58 @@ __global__ void k_cell_pairs(int nv, const double* P, NLView nl, Topo t, const i
   if (!pass) cnt[a] = n;
 }
 
+// Verlet rows of a batch of replicas (src/nlists/verlet_list.h:18-35): the
+// members of the 27 build-time neighbour cells of vertex a in its own
+// replica's grid (replica-tagged cell keys) closer than that replica's
+// cut-off rlist[rep], not excluded at that replica's level; padding
+// vertices have empty rows.  pass 0 counts, pass 1 writes (then ordered by
+// k_verlet_sort like the single-mesh rows).
+__global__ void k_verlet_batch(int nv, const double* P, NLView nl, Topo t, const int* vcoord,
+                               const double* __restrict__ rlist, int pass, int* cnt, const int* off, double* od,
+                               int* oj) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nv) return;
+  const int rep = rep_of(nl, a);
+  if (rep < 0) {
+    if (!pass) cnt[a] = 0;
+    return;
+  }
+  const NLGeom& G = nl.geom[rep];
+  const double rd = rlist[rep];
+  const int excl = excl_of(nl, a);
+  const d3 pa = ld3(P, a);
+  int n = 0;
+  int base = pass ? off[a] : 0;
+  for (int x = -1; x < 2; ++x) {
+    int ii = vcoord[3 * a] + x;
+    if (ii < 0 || ii >= G.shape[0]) continue;
+    for (int y = -1; y < 2; ++y) {
+      int jj = vcoord[3 * a + 1] + y;
+      if (jj < 0 || jj >= G.shape[1]) continue;
+      for (int z = -1; z < 2; ++z) {
+        int kk = vcoord[3 * a + 2] + z;
+        if (kk < 0 || kk >= G.shape[2]) continue;
+        long long cid = ii * G.stride[0] + jj * G.stride[1] + kk * G.stride[2];
+        int st = 0;
+        int c = cell_lookup(nl, cell_key(cid, rep), &st);
+        for (int q = 0; q < c; ++q) {
+          int b = nl.cell_verts[st + q];
+          if (b == a) continue;
+          double dd = exact_dist(pa, ld3(P, b));
+          if (!(dd <= rd)) continue;
+          if (nl_excluded(t, excl, a, b)) continue;
+          if (pass) {
+            od[base + n] = dd;
+            oj[base + n] = b;
+          }
+          ++n;
+        }
+      }
+    }
+  }
+  if (!pass) cnt[a] = n;
+}
+
 // candidate rows: members of the 27 build-time neighbour cells of vertex a in
 // the reference's scan order (x outer, z inner; members ascending), self
 // excluded.  pass 0 counts, pass 1 writes.
@@ -785,11 +837,11 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* P, c
 
 void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
                       const double* d_rlist, int excl, const int* d_rexcl, const double* P, cudaStream_t s,
-                      const EP* d_eps, bool near) {
+                      const EP* d_eps, bool near, bool verlet) {
   if (excl < 0 || excl > 2) fail(TM_ERR_ARG, "Unsupported exclusion level");
   int nv = m->nv;
   nl->nv = nv;
-  nl->prm.n_search = 0;
+  nl->prm.n_search = verlet ? 1 : 0;
   nl->prm.exclusion_level = excl;
   NLView& V = nl->view;
   V = NLView{};
@@ -807,6 +859,37 @@ void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const 
   }
   k_bbox_final_batch<<<R, BB, 0, s>>>(d_rblocks, nl->bbox.get(), d_rlist, nl->geom.get());
   TM_LAUNCH();
+  if (verlet) {
+    // Verlet rows at each replica's cut-off, ordered like the single-mesh
+    // rows (the reference's insertion order)
+    build_cells(nl, V, nv, P, s, false);
+    nl->vrow.ensure((size_t)nv + 1);
+    Topo t = m->topo();
+    int total = 0;
+    if (nv > 0) {
+      nl->cnt.ensure((size_t)nv + 1);
+      k_verlet_batch<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), d_rlist, 0, nl->cnt.get(),
+                                                   nullptr, nullptr, nullptr);
+      TM_LAUNCH();
+      TM_CUDA(cudaMemsetAsync(nl->cnt.get() + nv, 0, sizeof(int), s));
+      exclusive_scan_int(nl->cnt.get(), nl->vrow.get(), nv + 1, &total, nl->tmp, s);
+      nl->vcol.ensure(std::max(total, 1));
+      nl->d_res.ensure(std::max(total, 1));
+      k_verlet_batch<<<nblk(nv, 256), 256, 0, s>>>(nv, P, V, t, nl->vcoord.get(), d_rlist, 1, nullptr,
+                                                   nl->vrow.get(), nl->d_res.get(), nl->vcol.get());
+      TM_LAUNCH();
+      k_verlet_sort<<<nblk(nv, 128), 128, 0, s>>>(nv, nl->vrow.get(), nl->vcol.get(), nl->d_res.get(),
+                                                  nl->vcid.get(), nl->vcoord.get(), nl->vrank.get());
+      TM_LAUNCH();
+    } else {
+      TM_CUDA(cudaMemsetAsync(nl->vrow.get(), 0, sizeof(int), s));
+      nl->vcol.ensure(1);
+    }
+    V.kind = 1;
+    V.vrow = nl->vrow.get();
+    V.vcol = nl->vcol.get();
+    return;
+  }
   // candidate rows as well: unrelaxed replicas can move a skin's width
   // within a few steps, and then the candidate rows keep most vertices off
   // the cell walk

@@ -301,10 +301,11 @@ void nlist_make(tm_nlist* nl, tm_mesh* m, const tm_params& p, const double* d_po
 int64_t nlist_distance_matrix(tm_nlist* nl, tm_mesh* m, const double* d_points, double rdist, cudaStream_t s);
 // cell list over a batch of replicas (disjoint-union mesh with replica-aligned
 // 256-vertex blocks): per-replica boxes and cut-offs, replica-tagged cells
-// excl: the largest level of the replicas, d_rexcl: each replica's level
+// excl: the largest level of the replicas, d_rexcl: each replica's level;
+// verlet: Verlet rows at each replica's cut-off on top of the cells
 void nlist_make_batch(tm_nlist* nl, tm_mesh* m, int R, const int* d_vrep, const int2* d_rblocks,
                       const double* d_rlist, int excl, const int* d_rexcl, const double* d_points, cudaStream_t s,
-                      const EP* d_eps, bool near);
+                      const EP* d_eps, bool near, bool verlet);
 int64_t nlist_point_distances(tm_nlist* nl, tm_mesh* m, const double* d_points, int pid, double rdist,
                               cudaStream_t s);
 // smallest double T with sqrt(T) >= d (IEEE round-to-nearest sqrt), so that
