@@ -43,6 +43,6 @@ def minimize_scipy(energy, mesh, maxiter=1000):
         energy.update_repulsion(mesh)
         return energy.gradient(mesh).ravel()
 
-    res = minimize(fun, pts.ravel().copy(), jac=grad, method="L-BFGS-B", options={"maxiter": maxiter, "disp": 0})
+    res = minimize(fun, pts.ravel().copy(), jac=grad, method="L-BFGS-B", options={"maxiter": maxiter})
     pts[:] = res.x.reshape(shape)
     return res.nit, float(res.fun)
