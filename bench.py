@@ -445,8 +445,8 @@ def chain_leg(stream, state, stencil, dt=None, n_burn=20, n_steps=2000, weights=
     """ESS/s of the bending energy of a device chain: per step one HMC move
     (20 velocity-Verlet steps, m 1, T 1) and one flip sweep (ratio 0.2,
     98,304 attempts), neighbour list rebuilt every step.  dt: the largest of
-    DT_CANDIDATES (from 5e-5, the large-mesh runs' step) with pilot
-    acceptance >= 0.5 unless given.  The trace's quarter means show whether
+    DT_CANDIDATES (from 5e-5, the large-mesh runs' step) whose acceptance
+    over 12 pilot moves is >= 0.5, unless given.  The trace's quarter means show whether
     it is still drifting (an ESS of a drifting trace is a lower bound)."""
     import torch
 
@@ -459,7 +459,7 @@ def chain_leg(stream, state, stencil, dt=None, n_burn=20, n_steps=2000, weights=
     sg = capi.Surrogate(mesh, weights) if weights is not None else None
     pilot = None
     if dt is None:
-        dt, pilot = tune_dt(mesh, en, x, candidates=DT_CANDIDATES, stream=stream, force=sg)
+        dt, pilot = tune_dt(mesh, en, x, candidates=DT_CANDIDATES, pilot=12, stream=stream, force=sg)
     ch = DeviceChain(mesh, en, x, dt=dt, n_leapfrog=20, flip_ratio=0.2, seed=11, stream=stream, force=sg)
     ch.run(n_burn)
     torch.cuda.synchronize()
