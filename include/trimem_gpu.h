@@ -176,9 +176,10 @@ int tm_nlist_fetch(tm_nlist* nl, double* d, int32_t* i, int32_t* j);
  * Metropolis edge-flip sweep over floor(n_edges * ratio) proposals.
  * mode 0 (flip): proposals are evaluated in proposal order; mode 1 (pflip):
  * proposals are evaluated in conflict-free batches of `batch`, a proposal
- * whose patch overlaps a lower one waits for the next batch (1 <= batch
- * <= 4096; pflip's default is 4096).  ratio > 1 is TM_ERR_RANGE in mode 1.
- * Deterministic for a given seed. */
+ * whose quad lies within one edge of a lower proposal's quad waits for the
+ * next batch (1 <= batch <= 4096; pflip's default is 4096).  ratio > 1 is
+ * TM_ERR_RANGE in mode 1.  Deterministic for a given seed, and the same
+ * flips as the CPU port of the sweep (om_flip_windowed of the oracle). */
 int tm_flip(tm_mesh* m, tm_energy* e, double ratio, uint64_t seed, int mode, int batch, int32_t* accepted);
 /* The same sweep on device-resident positions (n_vertices*3 doubles); the
  * topology of m is updated in place, *accepted is returned after the sweep. */
