@@ -20,8 +20,8 @@
 //             of their neighbours); in serial mode the window is cut at the
 //             first loser, so proposals are decided in proposal order
 //             (k_claim_win does the three in one cooperative launch with a
-//             grid barrier when it fits).  The reference locks a larger patch, the
-//             edges of the faces around the quad's vertices
+//             grid barrier when it fits).  The reference locks a larger
+//             patch, the edges of the faces around the quad's vertices
 //             (flip_utils.cpp:43-68); the vertex patch suffices for the
 //             exactness above and lets more proposals of a window win.
 //   k_delta   one block per winner evaluates the vertex properties of the
@@ -32,8 +32,11 @@
 //   k_metro   Metropolis with T = 1 in slot order (flips.cpp:142-160): one
 //             block decides every slot whose float-filtered decision cannot
 //             be changed by earlier acceptances and walks the rest, with the
-//             robustly accepted ones, in order with the FP64 test; losers
-//             are queued for the next window
+//             robustly accepted ones, in order with the FP64 test of the
+//             energy change (written without cancellation); when the filter
+//             decides every slot, the state moves by one warp's reduction of
+//             the accepted changes instead; losers are queued for the next
+//             window
 //   k_commit  accepted flips rewrite their six halfedges, two faces, five
 //             edge rows and four ring rows (one block per flip); patches are
 //             disjoint, so commits never touch the same entries
